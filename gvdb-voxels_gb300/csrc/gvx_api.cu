@@ -1,0 +1,691 @@
+// gvx_api.cu -- extern "C" entry points of libgvx (declared in include/gvx.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "gvx_grid.cuh"
+
+static thread_local char t_err[1024] = "";
+
+void gvx_set_error(const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof(t_err), fmt, ap);
+    va_end(ap);
+}
+
+gvx_status gvx_cuda_fail(cudaError_t e, const char* what)
+{
+    gvx_set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    return GVX_ERR_DEVICE;
+}
+
+cudaError_t gvx_ensure(DevBuf& b, size_t bytes)
+{
+    if (bytes <= b.cap && b.p) return cudaSuccess;
+    if (b.p) {
+        cudaError_t e = cudaFree(b.p);
+        if (e != cudaSuccess) return e;
+    }
+    b.p = nullptr;
+    b.cap = 0;
+    const size_t want = bytes + bytes / 4 + 256;  // slack so that slowly growing sizes do not reallocate each call
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return e;
+    }
+    b.cap = want;
+    return cudaSuccess;
+}
+
+void gvx_free(DevBuf& b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+#define GVX_GUARD(g)                                \
+    do {                                            \
+        if (!(g)) {                                 \
+            gvx_set_error("null grid handle");      \
+            return GVX_ERR_INVALID_ARG;             \
+        }                                           \
+        cudaError_t _se = cudaSetDevice((g)->device); \
+        if (_se != cudaSuccess) return gvx_cuda_fail(_se, "cudaSetDevice"); \
+    } while (0)
+
+static int type_bytes(int type, int* ncomp)
+{
+    switch (type) {
+    case GVX_T_FLOAT: *ncomp = 1; return 4;
+    case GVX_T_FLOAT3: *ncomp = 4; return 16;  // stored as 4 floats (AL.cpp:395)
+    case GVX_T_FLOAT4: *ncomp = 4; return 16;
+    case GVX_T_UCHAR: *ncomp = 1; return 1;
+    case GVX_T_UCHAR4: *ncomp = 4; return 4;
+    }
+    return 0;
+}
+
+gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need)
+{
+    const int64_t amax = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
+    if (need <= amax) return GVX_OK;
+    // AtlasResize (AL.cpp:622-650): Z grows to ceil(used / (sx*sy)); data kept, new bricks zero
+    const int nz = (int)ceil((double)need / (double)((int64_t)g->sub[0] * g->sub[1]));
+    const int64_t slots = (int64_t)g->sub[0] * g->sub[1] * nz;
+    const int64_t P3 = (int64_t)g->P * g->P * g->P;
+    for (int c = 0; c < GVX_MAXCH; c++) {
+        GvxChannel& ch = g->ch[c];
+        if (!ch.used) continue;
+        DevBuf nb;
+        GVX_CK(gvx_ensure(nb, (size_t)(slots * P3 * ch.elem_bytes)));
+        GVX_CK(cudaMemsetAsync(nb.p, 0, (size_t)(slots * P3 * ch.elem_bytes), g->stream));
+        if (ch.data.p && ch.slots)
+            GVX_CK(cudaMemcpyAsync(nb.p, ch.data.p, (size_t)(std::min(ch.slots, slots) * P3 * ch.elem_bytes),
+                                   cudaMemcpyDeviceToDevice, g->stream));
+        GVX_CK(cudaStreamSynchronize(g->stream));
+        gvx_free(ch.data);
+        ch.data = nb;
+        ch.slots = slots;
+    }
+    g->sub[2] = nz;
+    return GVX_OK;
+}
+
+__global__ void k_fill(unsigned char* data, int64_t n, int eb, uint4 pattern)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned char* src = (const unsigned char*)&pattern;
+        for (int k = 0; k < eb; k++) data[i * eb + k] = src[k];
+    }
+}
+
+__global__ void k_pnode(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t n,
+                        uint32_t invalid_key, LeafLookup L, int* pnode)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = skeys[i];
+    int leaf = -1;
+    if (k < invalid_key) {
+        int c[3];
+        ks_unpack(L.ks, k, 0, c);
+        leaf = ll_find(L, c[0], c[1], c[2]);
+    }
+    pnode[svals[i]] = leaf;
+}
+
+extern "C" {
+
+const char* gvx_last_error(void) { return t_err; }
+const char* gvx_version(void) { return "gvx 0.1 (sm_103a)"; }
+
+gvx_status gvx_create(int device, gvx_grid** out)
+{
+    if (!out) {
+        gvx_set_error("gvx_create: null output");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        gvx_set_error("gvx_create: no CUDA device (%s)", e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+        return GVX_ERR_DEVICE;
+    }
+    if (device < 0 || device >= ndev) {
+        gvx_set_error("gvx_create: device %d of %d", device, ndev);
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaSetDevice(device));
+    gvx_grid* g = new gvx_grid();
+    g->device = device;
+    e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete g;
+        return gvx_cuda_fail(e, "cudaStreamCreate");
+    }
+    g->own_stream = true;
+    *out = g;
+    return GVX_OK;
+}
+
+gvx_status gvx_destroy(gvx_grid* g)
+{
+    if (!g) return GVX_OK;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    DevBuf* bufs[] = {&g->bm_a, &g->bm_a_prefix, &g->bm_b, &g->bm_b_prefix, &g->remap, &g->leaf_key, &g->leaf_range,
+                      &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos, &g->own_vel, &g->own_w,
+                      &g->own_r, &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
+                      &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
+                      &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
+                      &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->sc_tmp};
+    for (DevBuf* b : bufs) gvx_free(*b);
+    for (int l = 0; l < GVX_MAXLEV; l++) {
+        gvx_free(g->nodes[l]);
+        gvx_free(g->clist[l]);
+    }
+    for (int c = 0; c < GVX_MAXCH; c++) gvx_free(g->ch[c].data);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return GVX_OK;
+}
+
+gvx_status gvx_set_stream(gvx_grid* g, void* stream)
+{
+    GVX_GUARD(g);
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    if (g->own_stream) cudaStreamDestroy(g->stream);
+    g->stream = (cudaStream_t)stream;
+    g->own_stream = false;
+    return GVX_OK;
+}
+
+gvx_status gvx_sync(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return gvx_check_device_error(g, "sync");
+}
+
+gvx_status gvx_configure(gvx_grid* g, int levels, const int* logdim, const int* init_counts)
+{
+    GVX_GUARD(g);
+    (void)init_counts;  // pools grow to the exact counts of each rebuild
+    if (levels < 2 || levels > GVX_MAXLEV || !logdim) {
+        gvx_set_error("Configure: levels must be 2..%d", GVX_MAXLEV);
+        return GVX_ERR_INVALID_ARG;
+    }
+    int64_t range = 1;
+    for (int l = 0; l < levels; l++) {
+        const int r = logdim[l] == 0 ? 1 : logdim[l];  // VG.cpp:2397
+        if (r < 1 || r > 6) {
+            gvx_set_error("Configure: log2 resolution %d at level %d (1..6 supported)", logdim[l], l);
+            return GVX_ERR_INVALID_ARG;
+        }
+        g->logdim[l] = r;
+        g->res[l] = 1 << r;
+        range = (l == 0) ? g->res[0] : range * g->res[l];
+        if (range > (int64_t(1) << 30)) {
+            gvx_set_error("Configure: index-space extent exceeds 2^30 voxels");
+            return GVX_ERR_INVALID_ARG;
+        }
+        g->range[l] = (int)range;
+        g->tshift[l] = l == 0 ? 0 : g->tshift[l - 1] + r;
+    }
+    g->levels = levels;
+    g->brick = g->res[0];
+    g->P = g->brick + 2 * g->apron;
+    g->configured = true;
+    g->root_level = -1;
+    g->rebuild_topo = true;
+    g->curr_depth = -1;
+    g->lookup_valid = g->group_valid = g->atlas_valid = g->nbr_valid = false;
+    for (int l = 0; l < GVX_MAXLEV; l++) g->count[l] = 0;
+    g->used_leaves = 0;
+    return GVX_OK;
+}
+
+gvx_status gvx_set_channel_default(gvx_grid* g, int cx, int cy, int cz)
+{
+    GVX_GUARD(g);
+    if (cx <= 0 || cy <= 0 || cz <= 0) {
+        gvx_set_error("SetChannelDefault: counts must be positive");
+        return GVX_ERR_INVALID_ARG;
+    }
+    g->defsub[0] = cx;
+    g->defsub[1] = cy;
+    g->defsub[2] = cz;
+    return GVX_OK;
+}
+
+gvx_status gvx_add_channel(gvx_grid* g, int chan, int type, int apron)
+{
+    GVX_GUARD(g);
+    if (!g->configured) {
+        gvx_set_error("AddChannel: Configure was not called");
+        return GVX_ERR_NOT_CONFIGURED;
+    }
+    int ncomp = 0;
+    const int eb = type_bytes(type, &ncomp);
+    if (chan < 0 || chan >= GVX_MAXCH || eb == 0) {
+        gvx_set_error("AddChannel: channel %d type %d", chan, type);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (apron != 0 && apron != 1) {
+        gvx_set_error("AddChannel: apron %d (the apron update supports 0 or 1, OP.cuh:102)", apron);
+        return GVX_ERR_UNSUPPORTED;
+    }
+    bool any = false;
+    for (int c = 0; c < GVX_MAXCH; c++) any |= g->ch[c].used;
+    if (any && apron != g->apron) {
+        gvx_set_error("AddChannel: all channels share one apron (%d)", g->apron);
+        return GVX_ERR_INVALID_ARG;
+    }
+    g->apron = apron;
+    g->P = g->brick + 2 * apron;
+    if (!g->have_atlas) {
+        g->sub[0] = g->defsub[0];
+        g->sub[1] = g->defsub[1];
+        g->sub[2] = g->defsub[2];
+        g->have_atlas = true;
+    }
+    GvxChannel& ch = g->ch[chan];
+    gvx_free(ch.data);
+    ch.used = true;
+    ch.type = type;
+    ch.ncomp = ncomp;
+    ch.elem_bytes = eb;
+    ch.slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
+    const size_t bytes = (size_t)ch.slots * g->P * g->P * g->P * eb;
+    GVX_CK(gvx_ensure(ch.data, bytes));
+    GVX_CK(cudaMemsetAsync(ch.data.p, 0, bytes, g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_clear_channel(gvx_grid* g, int chan)
+{
+    GVX_GUARD(g);
+    if (chan < 0 || chan >= GVX_MAXCH || !g->ch[chan].used) {
+        gvx_set_error("ClearChannel: channel %d does not exist", chan);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const GvxChannel& ch = g->ch[chan];
+    GVX_CK(cudaMemsetAsync(ch.data.p, 0, (size_t)ch.slots * g->P * g->P * g->P * ch.elem_bytes, g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_fill_channel(gvx_grid* g, int chan, const float value[4])
+{
+    GVX_GUARD(g);
+    if (chan < 0 || chan >= GVX_MAXCH || !g->ch[chan].used || !value) {
+        gvx_set_error("FillChannel: channel %d does not exist", chan);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const GvxChannel& ch = g->ch[chan];
+    uint4 pat = make_uint4(0, 0, 0, 0);
+    unsigned char* pb = (unsigned char*)&pat;
+    if (ch.type == GVX_T_FLOAT) {
+        memcpy(pb, value, 4);
+    } else if (ch.elem_bytes == 16) {
+        memcpy(pb, value, 16);
+    } else {
+        for (int k = 0; k < ch.elem_bytes; k++) pb[k] = (unsigned char)value[k];
+    }
+    const int64_t n = ch.slots * g->P * g->P * g->P;
+    k_fill<<<1216, 256, 0, g->stream>>>((unsigned char*)ch.data.p, n, ch.elem_bytes, pat);
+    g->launches++;
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
+gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, int pos_stride, const void* vel,
+                          int vel_offset, int vel_stride, const void* clr, int clr_offset, int clr_stride)
+{
+    GVX_GUARD(g);
+    if (n < 0 || (n > 0 && !pos) || pos_stride < 12 || (pos_offset & 3) || (pos_stride & 3) ||
+        (vel && (vel_stride < 12 || (vel_stride & 3) || (vel_offset & 3)))) {
+        gvx_set_error("SetPoints: need float3 positions with a stride >= 12 and 4-byte alignment");
+        return GVX_ERR_INVALID_ARG;
+    }
+    g->pts.n = n;
+    g->pts.pos = (const char*)pos;
+    g->pts.pos_off = pos_offset;
+    g->pts.pos_stride = pos_stride;
+    g->pts.vel = (const char*)vel;
+    g->pts.vel_off = vel_offset;
+    g->pts.vel_stride = vel_stride;
+    g->pts.clr = (const char*)clr;
+    g->pts.clr_off = clr_offset;
+    g->pts.clr_stride = clr_stride;
+    g->group_valid = false;
+    return GVX_OK;
+}
+
+gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* radius)
+{
+    GVX_GUARD(g);
+    g->pts.weight = weight;
+    g->pts.radius = radius;
+    return GVX_OK;
+}
+
+gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_stride, const void* vel,
+                                  int vel_stride, const float* weight, const float* radius)
+{
+    GVX_GUARD(g);
+    if (n <= 0 || !pos || pos_stride < 12 || (vel && vel_stride < 12)) {
+        gvx_set_error("CommitData: invalid host points");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(gvx_ensure(g->own_pos, (size_t)n * 12));
+    GVX_CK(cudaMemcpy2DAsync(g->own_pos.p, 12, pos, pos_stride, 12, n, cudaMemcpyHostToDevice, g->stream));
+    if (vel) {
+        GVX_CK(gvx_ensure(g->own_vel, (size_t)n * 12));
+        GVX_CK(cudaMemcpy2DAsync(g->own_vel.p, 12, vel, vel_stride, 12, n, cudaMemcpyHostToDevice, g->stream));
+    }
+    if (weight) {
+        GVX_CK(gvx_ensure(g->own_w, (size_t)n * 4));
+        GVX_CK(cudaMemcpyAsync(g->own_w.p, weight, (size_t)n * 4, cudaMemcpyHostToDevice, g->stream));
+    }
+    if (radius) {
+        GVX_CK(gvx_ensure(g->own_r, (size_t)n * 4));
+        GVX_CK(cudaMemcpyAsync(g->own_r.p, radius, (size_t)n * 4, cudaMemcpyHostToDevice, g->stream));
+    }
+    gvx_status rc = gvx_set_points(g, n, g->own_pos.p, 0, 12, vel ? g->own_vel.p : nullptr, 0, 12, nullptr, 0, 0);
+    if (rc) return rc;
+    return gvx_set_point_attribs(g, weight ? g->own_w.as<float>() : nullptr, radius ? g->own_r.as<float>() : nullptr);
+}
+
+gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
+{
+    GVX_GUARD(g);
+    if (mode < GVX_TOPO_AUTO || mode > GVX_TOPO_ACCUMULATE) {
+        gvx_set_error("RebuildTopology: mode %d", mode);
+        return GVX_ERR_INVALID_ARG;
+    }
+    return gvx_topo_rebuild(g, n, radius, orig, mode, min_depth);
+}
+
+gvx_status gvx_request_full_rebuild(gvx_grid* g, int on)
+{
+    GVX_GUARD(g);
+    g->rebuild_topo = on != 0;
+    return GVX_OK;
+}
+
+gvx_status gvx_finish_topology(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    return gvx_topo_compute_bounds(g);
+}
+
+gvx_status gvx_update_atlas(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    return gvx_topo_update_atlas(g);
+}
+
+gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* pnode_out)
+{
+    GVX_GUARD(g);
+    gvx_status rc = gvx_topo_group_points(g, n, trans);
+    if (rc || !pnode_out) return rc;
+    DevBuf tmp;
+    GVX_CK(gvx_ensure(tmp, (size_t)n * 4));
+    k_pnode<<<(n + 255) / 256, 256, 0, g->stream>>>(g->keys[g->sorted_buf].as<uint32_t>(),
+                                                    g->vals[g->sorted_buf].as<uint32_t>(), (uint32_t)n,
+                                                    1u << g->lookup.ks.total_bits, g->lookup, tmp.as<int>());
+    g->launches++;
+    cudaError_t e = cudaMemcpyAsync(pnode_out, tmp.p, (size_t)n * 4, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    gvx_free(tmp);
+    if (e != cudaSuccess) return gvx_cuda_fail(e, "InsertPoints readback");
+    return GVX_OK;
+}
+
+gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3], int expand)
+{
+    GVX_GUARD(g);
+    (void)amp;  // unused by the reference kernel as well (PT.cuh:525-573)
+    return gvx_scatter_ref(g, n, radius, trans, expand);
+}
+
+gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                                     int* sc_len)
+{
+    GVX_GUARD(g);
+    (void)subcell;
+    (void)radius;
+    (void)sc_len;
+    gvx_status rc = gvx_topo_group_points(g, n, trans);
+    if (rc) return rc;
+    gvx_set_error("InsertPointsSubcell: not available yet");
+    return GVX_ERR_UNSUPPORTED;
+}
+
+gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                              int chan_density, int accum)
+{
+    GVX_GUARD(g);
+    (void)subcell; (void)n; (void)radius; (void)trans; (void)chan_density; (void)accum;
+    gvx_set_error("GatherDensity: not available yet");
+    return GVX_ERR_UNSUPPORTED;
+}
+
+gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                               int chan_levelset, int accum)
+{
+    GVX_GUARD(g);
+    (void)subcell; (void)n; (void)radius; (void)trans; (void)chan_levelset; (void)accum;
+    gvx_set_error("GatherLevelSet: not available yet");
+    return GVX_ERR_UNSUPPORTED;
+}
+
+gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_density,
+                     int chan_vel, int accum)
+{
+    GVX_GUARD(g);
+    return gvx_splat_run(g, mode, n, radius, trans, chan_density, chan_vel, accum);
+}
+
+gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval)
+{
+    GVX_GUARD(g);
+    return gvx_apron_run(g, chan, boundval);
+}
+
+gvx_status gvx_update_apron_all(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    for (int c = 0; c < GVX_MAXCH; c++) {
+        if (!g->ch[c].used) continue;
+        gvx_status rc = gvx_apron_run(g, c, 0.0f);
+        if (rc) return rc;
+    }
+    return GVX_OK;
+}
+
+static int top_lev_of(const gvx_grid* g)
+{
+    int tlev = 1;
+    for (int n = g->levels - 1; n >= 0; n--)
+        if (g->count[n] == 1) tlev = n;
+    return tlev;
+}
+
+gvx_status gvx_get_info(gvx_grid* g, gvx_info* out)
+{
+    GVX_GUARD(g);
+    if (!out) {
+        gvx_set_error("get_info: null output");
+        return GVX_ERR_INVALID_ARG;
+    }
+    memset(out, 0, sizeof(*out));
+    out->levels = g->levels;
+    for (int l = 0; l < GVX_MAXLEV; l++) {
+        out->logdim[l] = g->logdim[l];
+        out->node_count[l] = g->count[l];
+    }
+    out->brick_res = g->brick;
+    out->apron = g->apron;
+    out->root_level = g->root_level;
+    out->top_lev = g->root_level >= 0 ? top_lev_of(g) : -1;
+    out->used_leaves = g->used_leaves;
+    for (int a = 0; a < 3; a++) {
+        out->atlas_subdim[a] = g->sub[a];
+        out->atlas_res[a] = g->sub[a] * g->P;
+        out->root_pos[a] = g->root_pos[a];
+        out->bbox_min[a] = g->bbox_min[a];
+        out->bbox_max[a] = g->bbox_max[a];
+        out->obj_min[a] = g->obj_min[a];
+        out->obj_max[a] = g->obj_max[a];
+    }
+    int nch = 0;
+    for (int c = 0; c < GVX_MAXCH; c++) nch += g->ch[c].used;
+    out->channels = nch;
+    out->last_rebuild = g->last_rebuild;
+    return GVX_OK;
+}
+
+gvx_status gvx_read_nodes(gvx_grid* g, int level, void* out, int64_t cap_nodes)
+{
+    GVX_GUARD(g);
+    if (level < 0 || level >= g->levels || !out || cap_nodes < g->count[level]) {
+        gvx_set_error("read_nodes: level %d, capacity %lld < %lld", level, (long long)cap_nodes,
+                      (long long)(level >= 0 && level < GVX_MAXLEV ? g->count[level] : 0));
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (g->count[level])
+        GVX_CK(cudaMemcpyAsync(out, g->nodes[level].p, (size_t)g->count[level] * sizeof(GvxNode),
+                               cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_read_childlist(gvx_grid* g, int level, uint64_t* out, int64_t cap)
+{
+    GVX_GUARD(g);
+    if (level <= 0 || level >= g->levels || !out) {
+        gvx_set_error("read_childlist: level %d", level);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const int64_t n = g->count[level] * (int64_t)g->res[level] * g->res[level] * g->res[level];
+    if (cap < n) {
+        gvx_set_error("read_childlist: capacity %lld < %lld", (long long)cap, (long long)n);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (n)
+        GVX_CK(cudaMemcpyAsync(out, g->clist[level].p, (size_t)n * 8, cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_read_atlas_map(gvx_grid* g, int32_t* out4, int64_t cap_slots)
+{
+    GVX_GUARD(g);
+    const int64_t slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
+    if (!g->atlas_valid || !out4 || cap_slots < slots) {
+        gvx_set_error("read_atlas_map: no atlas or capacity %lld < %lld", (long long)cap_slots, (long long)slots);
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaMemcpyAsync(out4, g->amap.p, (size_t)slots * 16, cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_channel_bytes(gvx_grid* g, int chan, int64_t* bytes)
+{
+    GVX_GUARD(g);
+    if (chan < 0 || chan >= GVX_MAXCH || !g->ch[chan].used || !bytes) {
+        gvx_set_error("channel_bytes: channel %d", chan);
+        return GVX_ERR_INVALID_ARG;
+    }
+    *bytes = g->ch[chan].slots * g->P * g->P * g->P * g->ch[chan].elem_bytes;
+    return GVX_OK;
+}
+
+gvx_status gvx_read_channel(gvx_grid* g, int chan, void* out, int64_t cap)
+{
+    int64_t bytes = 0;
+    gvx_status rc = gvx_channel_bytes(g, chan, &bytes);
+    if (rc) return rc;
+    if (!out || cap < bytes) {
+        gvx_set_error("read_channel: capacity %lld < %lld", (long long)cap, (long long)bytes);
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaMemcpyAsync(out, g->ch[chan].data.p, (size_t)bytes, cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return GVX_OK;
+}
+
+gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap)
+{
+    int64_t bytes = 0;
+    gvx_status rc = gvx_channel_bytes(g, chan, &bytes);
+    if (rc) return rc;
+    if (!out || cap < bytes) {
+        gvx_set_error("read_channel_dense: capacity %lld < %lld", (long long)cap, (long long)bytes);
+        return GVX_ERR_INVALID_ARG;
+    }
+    std::vector<unsigned char> tmp((size_t)bytes);
+    GVX_CK(cudaMemcpyAsync(tmp.data(), g->ch[chan].data.p, (size_t)bytes, cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    const int P = g->P, eb = g->ch[chan].elem_bytes;
+    const int64_t W = (int64_t)g->sub[0] * P, H = (int64_t)g->sub[1] * P;
+    unsigned char* o = (unsigned char*)out;
+    for (int64_t s = 0; s < g->ch[chan].slots; s++) {
+        const int64_t bx = s % g->sub[0], by = (s / g->sub[0]) % g->sub[1], bz = s / ((int64_t)g->sub[0] * g->sub[1]);
+        for (int z = 0; z < P; z++)
+            for (int y = 0; y < P; y++) {
+                const int64_t src = (((s * P + z) * P + y) * P) * eb;
+                const int64_t dst = (((bz * P + z) * H + (by * P + y)) * W + bx * P) * eb;
+                memcpy(o + dst, tmp.data() + src, (size_t)P * eb);
+            }
+    }
+    return GVX_OK;
+}
+
+gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t* bytes)
+{
+    gvx_status rc = gvx_channel_bytes(g, chan, bytes);
+    if (rc) return rc;
+    if (!dev_ptr) {
+        gvx_set_error("channel_device_ptr: null output");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *dev_ptr = g->ch[chan].data.p;
+    return GVX_OK;
+}
+
+gvx_status gvx_retrieve_brick(gvx_grid* g, int chan, const int corner[3], void* out, int64_t cap)
+{
+    int64_t bytes = 0;
+    gvx_status rc = gvx_channel_bytes(g, chan, &bytes);
+    if (rc) return rc;
+    const int P = g->P, b = g->brick, eb = g->ch[chan].elem_bytes;
+    if (!corner || !out || cap < (int64_t)b * b * b * eb) {
+        gvx_set_error("retrieve_brick: output too small");
+        return GVX_ERR_INVALID_ARG;
+    }
+    const int bx = corner[0] / P, by = corner[1] / P, bz = corner[2] / P;
+    const int ox = corner[0] - bx * P, oy = corner[1] - by * P, oz = corner[2] - bz * P;
+    if (bx < 0 || by < 0 || bz < 0 || bx >= g->sub[0] || by >= g->sub[1] || bz >= g->sub[2] || ox + b > P ||
+        oy + b > P || oz + b > P) {
+        gvx_set_error("retrieve_brick: corner (%d,%d,%d) is not inside one atlas brick", corner[0], corner[1],
+                      corner[2]);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const int64_t s = ((int64_t)bz * g->sub[1] + by) * g->sub[0] + bx;
+    std::vector<unsigned char> tmp((size_t)P * P * P * eb);
+    GVX_CK(cudaMemcpyAsync(tmp.data(), g->ch[chan].data.as<unsigned char>() + s * P * P * P * eb, tmp.size(),
+                           cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    // kernelRetrieveTexXYZ (cuda_gvdb_copydata.cu:74-79) writes buf[(x*ry + y)*rx + z]
+    unsigned char* o = (unsigned char*)out;
+    for (int x = 0; x < b; x++)
+        for (int y = 0; y < b; y++)
+            for (int z = 0; z < b; z++)
+                memcpy(o + (((int64_t)x * b + y) * b + z) * eb,
+                       tmp.data() + ((((int64_t)(oz + z)) * P + (oy + y)) * P + (ox + x)) * eb, (size_t)eb);
+    return GVX_OK;
+}
+
+gvx_status gvx_kernel_launches(gvx_grid* g, int64_t* count)
+{
+    if (!g || !count) {
+        gvx_set_error("kernel_launches: null argument");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *count = g->launches;
+    return GVX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// gvx_grid.cuh -- the grid handle behind gvx_grid* and the host entry points
+// of the topology, splat and apron stages.
+#pragma once
+
+#include "gvx_internal.cuh"
+
+struct GvxChannel {
+    bool used = false;
+    int type = 0;
+    int ncomp = 1;       // components per voxel
+    int elem_bytes = 4;  // bytes per voxel
+    DevBuf data;         // slots * P^3 * elem_bytes, brick-major
+    int64_t slots = 0;
+};
+
+struct GvxPoints {
+    int n = 0;
+    const char* pos = nullptr;
+    int pos_off = 0, pos_stride = 12;
+    const char* vel = nullptr;
+    int vel_off = 0, vel_stride = 12;
+    const char* clr = nullptr;
+    int clr_off = 0, clr_stride = 4;
+    const float* weight = nullptr;
+    const float* radius = nullptr;
+};
+
+// How a key maps to a leaf pool index: a set bit in `a` -> rank in a (+ remap),
+// else a set bit in `b` -> b_offset + rank in b, else -1.
+struct LeafLookup {
+    KeySpace ks;
+    BitRank a;
+    BitRank b;
+    uint32_t b_offset;
+    const int* remap;  // optional rank -> pool index
+};
+
+__device__ inline int ll_find(const LeafLookup& L, int cx, int cy, int cz)
+{
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= (1 << L.ks.bits[0]) || cy >= (1 << L.ks.bits[1]) ||
+        cz >= (1 << L.ks.bits[2]))
+        return -1;
+    const uint32_t key = ks_pack(L.ks, cx, cy, cz, 0);
+    if (br_test(L.a, key)) {
+        const uint32_t r = br_rank(L.a, key);
+        return L.remap ? L.remap[r] : (int)r;
+    }
+    if (L.b.bits && br_test(L.b, key)) return (int)(L.b_offset + br_rank(L.b, key));
+    return -1;
+}
+
+struct gvx_grid {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+
+    // configuration (Configure)
+    bool configured = false;
+    int levels = 0;
+    int logdim[GVX_MAXLEV] = {};
+    int res[GVX_MAXLEV] = {};
+    int range[GVX_MAXLEV] = {};
+    int tshift[GVX_MAXLEV] = {};  // log2(range[l] / res[0]): level-l node size in leaves
+    int brick = 0, apron = 1, P = 0;
+    bool apron_set = false;
+    int defsub[3] = {16, 16, 1};
+
+    // topology state
+    int root_level = -1;
+    int root_pos[3] = {0, 0, 0};
+    bool rebuild_topo = true;  // mRebuildTopo
+    int curr_depth = -1;       // mCurrDepth
+    int last_rebuild = 0;
+    int64_t count[GVX_MAXLEV] = {};
+    int64_t used_leaves = 0;
+    DevBuf nodes[GVX_MAXLEV];
+    DevBuf clist[GVX_MAXLEV];
+    float bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
+    float obj_min[3] = {0, 0, 0}, obj_max[3] = {0, 0, 0};
+
+    // lookup of leaves by key for the current topology
+    LeafLookup lookup{};
+    bool lookup_valid = false;
+    DevBuf bm_a, bm_a_prefix, bm_b, bm_b_prefix;  // level-0 bitmaps backing `lookup`
+    DevBuf remap;
+
+    // per-leaf data
+    DevBuf leaf_key;     // compact level-0 key per leaf (pool order)
+    DevBuf leaf_range;   // int2 [start, end) in the sorted point order
+    DevBuf leaf_slot;    // atlas slot per leaf, -1 if inactive
+    DevBuf slot_leaf;    // leaf per atlas slot (active slots only)
+    DevBuf nbr;          // 27 leaf indices per leaf
+    bool nbr_valid = false;
+
+    // atlas
+    int sub[3] = {0, 0, 0};
+    bool have_atlas = false;
+    bool atlas_valid = false;  // mValue/atlas map reflect the topology
+    int64_t atlas_used = 0;
+    GvxChannel ch[GVX_MAXCH];
+    DevBuf amap;  // 4 ints per slot
+
+    // points
+    GvxPoints pts;
+    DevBuf own_pos, own_vel, own_w, own_r;  // storage of gvx_commit_points_host
+
+    // grouping of points by leaf (sorted order)
+    DevBuf keys[2], vals[2];
+    int sorted_buf = 0;
+    uint32_t n_sorted = 0;
+    bool group_valid = false;
+    float group_trans[3] = {0, 0, 0};
+    const void* group_pos = nullptr;
+    int group_n = -1;
+    DevBuf spos, svel;  // sorted float4 (x,y,z,weight) and (vx,vy,vz,radius)
+    SortScratch sort;
+
+    // scratch of the topology build
+    DevBuf d0_bits, d0_prefix, x0_bits, x0_prefix, masks, upper, lists, tmp_scan, d_counts;
+    DevBuf d_err, d_bbox;
+    DevBuf host_stage;  // pinned staging of small readbacks
+
+    // scratch of the gathers
+    DevBuf sc_tmp;
+
+    int64_t launches = 0;
+};
+
+// topology (gvx_topology.cu)
+gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth);
+gvx_status gvx_topo_update_atlas(gvx_grid* g);
+gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
+gvx_status gvx_topo_compute_bounds(gvx_grid* g);
+gvx_status gvx_check_device_error(gvx_grid* g, const char* stage);
+
+// splats (gvx_splat.cu)
+gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
+                         int chan_v, int accum);
+gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand);
+gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, int n, float radius, float radius_ins,
+                          const float trans[3], int chan, int accum);
+
+// apron (gvx_apron.cu)
+gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval);
+
+// channel storage (gvx_api.cu)
+gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need_slots);

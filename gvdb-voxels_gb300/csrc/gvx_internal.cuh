@@ -1,0 +1,134 @@
+// gvx_internal.cuh -- shared declarations of the libgvx CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "gvx.h"
+
+#define GVX_MAXLEV 10
+#define GVX_MAXCH 32
+
+#define ID_UNDEFL_U64 0xFFFFFFFFull          // ID_UNDEFL (gvdb_types.h:55) stored in 64 bits
+#define ID_UNDEF64_U64 0xFFFFFFFFFFFFFFFFull // ID_UNDEF64 (gvdb_types.h:56)
+#define GVX_NOHIT 1.0e10f                    // NOHIT (gvdb_types.h:53)
+
+// device error word bits
+#define GVX_DERR_TIMEOUT 1u      // a bounded spin-wait gave up
+#define GVX_DERR_CAPACITY 2u     // a kernel found more items than its buffer holds
+#define GVX_DERR_DEGENERATE 4u   // a node lies outside the root / a level-0 key domain
+#define GVX_DERR_BADPOINT 8u     // NaN position
+
+// 64-byte node record, layout of VDBNode (cuda_gvdb_nodes.cuh:24-35) / Node (gvdb_node.h:27-40)
+struct __align__(16) GvxNode {
+    uint8_t lev, flags, prio, pad;
+    int32_t pos[3];
+    int32_t value[3];
+    float vrange[3];
+    uint64_t parent;
+    uint64_t childlist;
+    uint64_t mask;
+};
+static_assert(sizeof(GvxNode) == 64, "node layout");
+
+// Compact level-0 key space of one topology build: leaf coordinates relative to
+// `lo` (aligned to the level depth-1 node size), `bits[a]` bits per axis, packed
+// x-major: key = (x << (by+bz)) | (y << bz) | z, so key order is the reference's
+// (x, y, z) node order.  Level-l coordinates are the level-0 ones >> shift_l.
+struct KeySpace {
+    int lo[3];       // absolute leaf coordinates of compact (0,0,0)
+    int bits[3];     // per-axis bits at level 0
+    int total_bits;  // bx + by + bz
+};
+
+__host__ __device__ inline uint32_t ks_pack(const KeySpace& ks, int cx, int cy, int cz, int shift)
+{
+    int by = ks.bits[1] > shift ? ks.bits[1] - shift : 0;
+    int bz = ks.bits[2] > shift ? ks.bits[2] - shift : 0;
+    return ((uint32_t)cx << (by + bz)) | ((uint32_t)cy << bz) | (uint32_t)cz;
+}
+__host__ __device__ inline void ks_unpack(const KeySpace& ks, uint32_t key, int shift, int* c)
+{
+    int by = ks.bits[1] > shift ? ks.bits[1] - shift : 0;
+    int bz = ks.bits[2] > shift ? ks.bits[2] - shift : 0;
+    c[2] = (int)(key & ((1u << bz) - 1u));
+    c[1] = (int)((key >> bz) & ((1u << by) - 1u));
+    c[0] = (int)(key >> (by + bz));
+}
+__host__ __device__ inline int ks_bits_at(const KeySpace& ks, int shift)
+{
+    int t = 0;
+    for (int a = 0; a < 3; a++) t += ks.bits[a] > shift ? ks.bits[a] - shift : 0;
+    return t;
+}
+__host__ __device__ inline int ks_extent(const KeySpace& ks, int a, int shift)
+{
+    return 1 << (ks.bits[a] > shift ? ks.bits[a] - shift : 0);
+}
+
+// A set of keys held as a bitmap with per-word exclusive prefix popcounts
+// (rank in O(1)).
+struct BitRank {
+    uint32_t* bits;
+    uint32_t* prefix;
+    uint32_t words;
+};
+__device__ inline bool br_test(const BitRank& b, uint32_t key)
+{
+    return (b.bits[key >> 5] >> (key & 31)) & 1u;
+}
+__device__ inline uint32_t br_rank(const BitRank& b, uint32_t key)
+{
+    uint32_t w = b.bits[key >> 5] & ((1u << (key & 31)) - 1u);
+    return b.prefix[key >> 5] + __popc(w);
+}
+
+// host-side growable device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <class T> T* as() const { return (T*)p; }
+};
+
+// error reporting helpers (gvx_api.cu)
+void gvx_set_error(const char* fmt, ...);
+gvx_status gvx_cuda_fail(cudaError_t e, const char* what);
+#define GVX_CK(call)                                                   \
+    do {                                                               \
+        cudaError_t _e = (call);                                       \
+        if (_e != cudaSuccess) return gvx_cuda_fail(_e, #call);        \
+    } while (0)
+
+cudaError_t gvx_ensure(DevBuf& b, size_t bytes);
+void gvx_free(DevBuf& b);
+
+// ---- onesweep radix sort (gvx_sort.cu) -----------------------------------
+struct SortScratch {
+    DevBuf hist;      // passes * 256 counts
+    DevBuf base;      // passes * 256 exclusive bases
+    DevBuf lookback;  // tiles * 256 status words
+    DevBuf counter;   // tile counters, one per pass
+};
+// Sorts (keys, vals) by the low `bits` bits of the keys, stable.  The keys
+// must already be in keys[0]/vals[0]; the result ends in buffer index *result
+// (0 or 1).  If the histogram of the pass digits was accumulated by the
+// producer of the keys (hist_ready), it is used as is.
+gvx_status gvx_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int bits, SortScratch& s,
+                          bool hist_ready, cudaStream_t st, uint32_t* d_err, int* result, int64_t* launches);
+int gvx_sort_passes(int bits);
+// zero the global histogram before a fused key producer accumulates into it
+gvx_status gvx_sort_prepare_hist(SortScratch& s, int bits, cudaStream_t st);
+uint32_t* gvx_sort_hist_ptr(SortScratch& s);
+
+// device helper used by key producers: accumulate digit histograms of a key
+// into the shared histogram `sh` (passes * 256 uint32)
+__device__ inline void gvx_sort_count_key(uint32_t* sh, uint32_t key, int passes)
+{
+    for (int p = 0; p < passes; p++) atomicAdd(&sh[p * 256 + ((key >> (8 * p)) & 255u)], 1u);
+}
+
+// ---- generic exclusive scan of popcounts of a bitmap (gvx_topology.cu) -----
+gvx_status gvx_bitmap_prefix(const uint32_t* bits, uint32_t* prefix, uint32_t words, uint32_t* total,
+                             DevBuf& tmp, cudaStream_t st, int64_t* launches);

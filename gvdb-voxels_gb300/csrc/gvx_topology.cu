@@ -1,0 +1,1078 @@
+// gvx_topology.cu -- dynamic brick topology from points, on the device.
+//
+// Reference path (paths relative to the reference project):
+//   VolumeGVDB::RebuildTopology          gvdb_volume_gvdb.cpp:1181-1218
+//   GetBoundingBox / DetermineDepth      gvdb_volume_gvdb.cpp:5404-5467, 821-837
+//   ActivateBricksGPU                    gvdb_volume_gvdb.cpp:1229-1413
+//   ActivateExtraBricksGPU               gvdb_volume_gvdb.cpp:931-1016
+//   gvdbCalcBrickId / CalcExtraBrickId   cuda_gvdb_particles.cuh:352-382, 467-512
+//   gvdbLinkBricks                       cuda_gvdb_nodes.cuh:470-505
+//   UpdateAtlas                          gvdb_volume_gvdb.cpp:2630-2704
+//
+// The reference computes one 64-bit key per point per level, sorts all of
+// them, copies the unique keys to the host, allocates nodes in a host loop,
+// links them with a root descent per node and repeats the cycle for the
+// dilated ("extra") bricks.  Here the node set of every level is derived on the
+// device from ONE sort of 32-bit compact level-0 keys:
+//   D0 = leaves holding points, X0 = leaves of the dilation boxes not in D0,
+//   level l nodes = parents of (D0 u X0), split the same way,
+// each set held as a bitmap with per-word prefix popcounts, so pool order
+// (sorted direct nodes, then sorted extra nodes: the order of the reference's
+// two passes), parent indices and child-list slots are all O(1) rank lookups.
+// The host reads back 24 bytes (bounding box) and the per-level counts.
+#include <math.h>
+#include <string.h>
+
+#include "gvx_grid.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint32_t f2ord(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+inline float ord2f(uint32_t u)
+{
+    const uint32_t b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+__device__ __forceinline__ void load_pos(const char* base, int off, int stride, uint32_t i, float* w)
+{
+    const float* p = (const float*)(base + (size_t)i * (size_t)stride + off);
+    w[0] = p[0];
+    w[1] = p[1];
+    w[2] = p[2];
+}
+
+inline int ceil_log2(int64_t v)
+{
+    int b = 0;
+    while ((int64_t(1) << b) < v) b++;
+    return b;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// bounding box of pos + orig over ALL points (GetBoundingBox includes points
+// that the key kernel later drops)
+__global__ void k_bbox(const char* pos, int off, int stride, uint32_t n, float ox, float oy, float oz,
+                       uint32_t* out, uint32_t* err)
+{
+    uint32_t mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+    bool nan = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float w[3];
+        load_pos(pos, off, stride, i, w);
+        w[0] += ox;
+        w[1] += oy;
+        w[2] += oz;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (w[a] != w[a]) nan = true;
+            const uint32_t o = f2ord(w[a]);
+            mn[a] = min(mn[a], o);
+            mx[a] = max(mx[a], o);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[a] = min(mn[a], __shfl_xor_sync(0xFFFFFFFFu, mn[a], s));
+            mx[a] = max(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], s));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&out[a], mn[a]);
+            atomicMax(&out[3 + a], mx[a]);
+        }
+    }
+    if (nan) atomicOr(err, GVX_DERR_BADPOINT);
+}
+
+// compact level-0 key of every point (invalid points -> invalid_key, sorted
+// last), identity values, and the digit histograms of the sort
+__global__ void k_keys(const char* pos, int off, int stride, uint32_t n, float ox, float oy, float oz,
+                       KeySpace ks, float inv_b, int passes, uint32_t invalid_key, uint32_t* keys,
+                       uint32_t* vals, uint32_t* hist, uint32_t* err)
+{
+    __shared__ uint32_t sh[4 * 256];
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) sh[i] = 0u;
+    __syncthreads();
+    bool degen = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float w[3];
+        load_pos(pos, off, stride, i, w);
+        w[0] += ox;
+        w[1] += oy;
+        w[2] += oz;
+        uint32_t key = invalid_key;
+        if (w[0] >= 0.f && w[1] >= 0.f && w[2] >= 0.f) {
+            int c[3];
+            bool in = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                c[a] = (int)(w[a] * inv_b) - ks.lo[a];  // floor(w / b), exact for a power-of-two b
+                if (c[a] < 0 || c[a] >= (1 << ks.bits[a])) in = false;
+            }
+            if (in)
+                key = ks_pack(ks, c[0], c[1], c[2], 0);
+            else
+                degen = true;
+        }
+        keys[i] = key;
+        vals[i] = i;
+        gvx_sort_count_key(sh, key, passes);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], sh[i]);
+    if (degen) atomicOr(err, GVX_DERR_DEGENERATE);
+}
+
+// first point of every run of equal valid keys sets the key's bit
+__global__ void k_mark_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t invalid_key, uint32_t* bits)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = skeys[i];
+    if (k >= invalid_key) return;
+    if (i == 0 || skeys[i - 1] != k) atomicOr(&bits[k >> 5], 1u << (k & 31));
+}
+
+// dilation mask of every direct leaf: OR over its points of the leaves touched
+// by the box [int(p)-r, int(p)+2r] (cuda_gvdb_particles.cuh:481-482), encoded
+// as 27 bits (dz+1)*9 + (dy+1)*3 + (dx+1)
+__global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t n,
+                              uint32_t invalid_key, BitRank d0, const char* pos, int off, int stride, float ox,
+                              float oy, float oz, float radius, int brick, uint32_t* masks)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    uint32_t key = live ? skeys[i] : invalid_key;
+    const bool valid = key < invalid_key;
+    uint32_t m = 0u;
+    int leaf = -1;
+    if (valid) {
+        leaf = (int)br_rank(d0, key);
+        float w[3];
+        load_pos(pos, off, stride, svals[i], w);
+        w[0] += ox;
+        w[1] += oy;
+        w[2] += oz;
+        int lo[3], hi[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int ip = (int)w[a];
+            const int bmin = (int)((float)ip - radius);
+            const int bmax = (int)((float)ip + 2.0f * radius);
+            const int cl = ip / brick;
+            lo[a] = bmin / brick - cl;  // C truncation, as bmin/rres*rres
+            hi[a] = bmax / brick - cl;
+            lo[a] = max(lo[a], -1);
+            hi[a] = min(hi[a], 1);
+        }
+        for (int dz = lo[2]; dz <= hi[2]; dz++)
+            for (int dy = lo[1]; dy <= hi[1]; dy++)
+                for (int dx = lo[0]; dx <= hi[0]; dx++) m |= 1u << ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1));
+    }
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? (uint32_t)leaf : 0xFFFFFFFFu);
+    const uint32_t agg = __reduce_or_sync(peers, m);
+    const int lane = threadIdx.x & 31;
+    if (valid && lane == __ffs(peers) - 1) atomicOr(&masks[leaf], agg);
+}
+
+// leaves of the dilation boxes that hold no point -> X0 bitmap
+__global__ void k_dilate(const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ count, KeySpace ks,
+                         const uint32_t* __restrict__ masks, BitRank d0, uint32_t* x0bits, uint32_t* err)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *count) return;
+    const uint32_t m = masks[j] & ~(1u << 13);
+    if (!m) return;
+    int c[3];
+    ks_unpack(ks, dlist[j], 0, c);
+    bool degen = false;
+    for (int b = 0; b < 27; b++) {
+        if (!((m >> b) & 1u)) continue;
+        const int nx = c[0] + (b % 3) - 1, ny = c[1] + (b / 3) % 3 - 1, nz = c[2] + b / 9 - 1;
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= (1 << ks.bits[0]) || ny >= (1 << ks.bits[1]) ||
+            nz >= (1 << ks.bits[2])) {
+            degen = true;  // the reference descends outside the root here
+            continue;
+        }
+        const uint32_t nk = ks_pack(ks, nx, ny, nz, 0);
+        if (!br_test(d0, nk)) atomicOr(&x0bits[nk >> 5], 1u << (nk & 31));
+    }
+    if (degen) atomicOr(err, GVX_DERR_DEGENERATE);
+}
+
+struct UpperDesc {
+    int nlev;                  // levels 1..nlev are described (nlev = depth-1)
+    uint32_t words[GVX_MAXLEV];
+    uint32_t off[GVX_MAXLEV];  // per level: D bits, X bits, D prefix, X prefix (words each)
+    int tshift[GVX_MAXLEV];
+};
+
+// parents of direct leaves -> D_l bitmaps
+__global__ void k_upper_direct(const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ count, KeySpace ks,
+                               UpperDesc ud, uint32_t* upper)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = j < *count;
+    int c[3] = {0, 0, 0};
+    if (valid) ks_unpack(ks, dlist[j], 0, c);
+    for (int l = 1; l <= ud.nlev; l++) {
+        const int t = ud.tshift[l];
+        const uint32_t k = valid ? ks_pack(ks, c[0] >> t, c[1] >> t, c[2] >> t, t) : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1)
+            atomicOr(&upper[ud.off[l] + (k >> 5)], 1u << (k & 31));
+    }
+}
+
+// parents of extra leaves -> A_l bitmaps (X_l = A_l & ~D_l later)
+__global__ void k_upper_extra(const uint32_t* __restrict__ x0bits, uint32_t words, KeySpace ks, UpperDesc ud,
+                              uint32_t* upper)
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= words) return;
+    uint32_t bits = x0bits[w];
+    uint32_t last[GVX_MAXLEV];
+    for (int l = 0; l < GVX_MAXLEV; l++) last[l] = 0xFFFFFFFFu;
+    while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        int c[3];
+        ks_unpack(ks, w * 32u + (uint32_t)b, 0, c);
+        for (int l = 1; l <= ud.nlev; l++) {
+            const int t = ud.tshift[l];
+            const uint32_t k = ks_pack(ks, c[0] >> t, c[1] >> t, c[2] >> t, t);
+            if (k == last[l]) continue;
+            last[l] = k;
+            atomicOr(&upper[ud.off[l] + ud.words[l] + (k >> 5)], 1u << (k & 31));
+        }
+    }
+}
+
+// small bitmaps: one block per (level, D|X); X = A & ~D first; exclusive
+// prefix popcounts, total -> counts[2 + 2*(l-1) + which]
+__global__ void k_prefix_upper(UpperDesc ud, uint32_t* upper, uint32_t* counts)
+{
+    const int l = 1 + blockIdx.x / 2, which = blockIdx.x & 1;
+    if (l > ud.nlev) return;
+    const uint32_t words = ud.words[l];
+    uint32_t* D = upper + ud.off[l];
+    uint32_t* B = upper + ud.off[l] + (which ? words : 0u);
+    uint32_t* pre = upper + ud.off[l] + 2u * words + (which ? words : 0u);
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t base = 0; base < words; base += blockDim.x) {
+        const uint32_t w = base + threadIdx.x;
+        uint32_t v = 0u;
+        if (w < words) {
+            uint32_t bits = B[w];
+            if (which) {
+                bits &= ~D[w];
+                B[w] = bits;
+            }
+            v = __popc(bits);
+        }
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        uint32_t wp = 0u;
+        for (int i = 0; i < warp; i++) wp += s_w[i];
+        uint32_t tot = 0u;
+        for (int i = 0; i < nw; i++) tot += s_w[i];
+        if (w < words) pre[w] = s_carry + wp + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) counts[2 + 2 * (l - 1) + which] = s_carry;
+}
+
+// ---------------------------------------------------------------------------
+// generic exclusive prefix of popcounts over a bitmap (reduce, scan, apply)
+namespace {
+constexpr int kPfxThreads = 256;
+constexpr int kPfxPerThread = 16;
+constexpr uint32_t kPfxChunk = kPfxThreads * kPfxPerThread;
+}  // namespace
+
+__global__ void k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words, uint32_t* block_sums)
+{
+    const uint32_t base = blockIdx.x * kPfxChunk;
+    uint32_t s = 0u;
+    for (uint32_t i = threadIdx.x; i < kPfxChunk; i += kPfxThreads) {
+        const uint32_t w = base + i;
+        if (w < words) s += __popc(bits[w]);
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    __shared__ uint32_t ws[kPfxThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0u;
+        for (int i = 0; i < kPfxThreads / 32; i++) t += ws[i];
+        block_sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_pfx_top(uint32_t* block_sums, uint32_t nblocks, uint32_t* total)
+{
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0u;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t base = 0; base < nblocks; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nblocks ? block_sums[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        uint32_t wp = 0u, tot = 0u;
+        for (int k = 0; k < nw; k++) {
+            if (k < warp) wp += s_w[k];
+            tot += s_w[k];
+        }
+        if (i < nblocks) block_sums[i] = s_carry + wp + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total) *total = s_carry;
+}
+
+__global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, const uint32_t* __restrict__ block_off,
+                            uint32_t* prefix)
+{
+    const uint32_t base = blockIdx.x * kPfxChunk + threadIdx.x * kPfxPerThread;
+    uint32_t cnt[kPfxPerThread];
+    uint32_t s = 0u;
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) {
+        const uint32_t w = base + k;
+        cnt[k] = w < words ? __popc(bits[w]) : 0u;
+        s += cnt[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    __shared__ uint32_t s_w[kPfxThreads / 32];
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t run = block_off[blockIdx.x] + x - s;
+    for (int k = 0; k < warp; k++) run += s_w[k];
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) {
+        const uint32_t w = base + k;
+        if (w < words) prefix[w] = run;
+        run += cnt[k];
+    }
+}
+
+gvx_status gvx_bitmap_prefix(const uint32_t* bits, uint32_t* prefix, uint32_t words, uint32_t* total, DevBuf& tmp,
+                             cudaStream_t st, int64_t* launches)
+{
+    const uint32_t nb = (words + kPfxChunk - 1) / kPfxChunk;
+    GVX_CK(gvx_ensure(tmp, (size_t)(nb + 1) * sizeof(uint32_t)));
+    k_pfx_reduce<<<nb, kPfxThreads, 0, st>>>(bits, words, tmp.as<uint32_t>());
+    k_pfx_top<<<1, 1024, 0, st>>>(tmp.as<uint32_t>(), nb, total);
+    k_pfx_apply<<<nb, kPfxThreads, 0, st>>>(bits, words, tmp.as<uint32_t>(), prefix);
+    *launches += 3;
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
+// set bits -> sorted key list (select)
+__global__ void k_select(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ prefix, uint32_t words,
+                         uint32_t* out)
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= words) return;
+    uint32_t b = bits[w];
+    uint32_t o = prefix[w];
+    while (b) {
+        const int k = __ffs(b) - 1;
+        b &= b - 1u;
+        out[o++] = w * 32u + (uint32_t)k;
+    }
+}
+
+struct NodeLevelArgs {
+    int lev, depth;
+    uint32_t ucount, xcount;
+    const uint32_t* dlist;
+    const uint32_t* xlist;
+    KeySpace ks;
+    int tshift, tshift_parent, logdim_parent, res_parent;
+    int lo[3];         // absolute level-l node coordinates of compact (0,0,0)
+    int root_rel[3];   // root position in level-l node units (when the parent is the root)
+    int range;
+    BitRank pd, px;    // parent level bitmaps (unused when the parent is the root)
+    uint32_t pucount;
+    GvxNode* nodes;
+    uint64_t* pclist;
+    uint32_t* leaf_key;  // level 0 only
+};
+
+// one node per thread: Node record, parent reference, and the parent's child-list slot
+// (SetupNode VG.cpp:2512-2524, gvdbLinkBricks cuda_gvdb_nodes.cuh:470-505)
+__global__ void k_write_nodes(NodeLevelArgs a)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ucount + a.xcount) return;
+    const uint32_t key = i < a.ucount ? a.dlist[i] : a.xlist[i - a.ucount];
+    int c[3];
+    ks_unpack(a.ks, key, a.tshift, c);
+    GvxNode nd;
+    nd.lev = (uint8_t)a.lev;
+    nd.flags = 1;
+    nd.prio = 0;
+    nd.pad = 0;
+    for (int k = 0; k < 3; k++) {
+        nd.pos[k] = (a.lo[k] + c[k]) * a.range;
+        nd.value[k] = -1;
+        nd.vrange[k] = 0.f;
+    }
+    nd.mask = 0ull;
+    nd.childlist = a.lev > 0 ? (1ull | ((uint64_t)a.lev << 8) | ((uint64_t)i << 16)) : ID_UNDEFL_U64;
+    uint32_t pidx;
+    int rel[3];
+    const int res = a.res_parent;
+    if (a.lev + 1 == a.depth) {
+        pidx = 0u;
+        for (int k = 0; k < 3; k++) rel[k] = a.lo[k] + c[k] - a.root_rel[k];
+    } else {
+        const int sh = a.logdim_parent;
+        const uint32_t pk = ks_pack(a.ks, c[0] >> sh, c[1] >> sh, c[2] >> sh, a.tshift_parent);
+        pidx = br_test(a.pd, pk) ? br_rank(a.pd, pk) : a.pucount + br_rank(a.px, pk);
+        for (int k = 0; k < 3; k++) rel[k] = c[k] & (res - 1);
+    }
+    nd.parent = ((uint64_t)pidx << 16) | ((uint64_t)(a.lev + 1) << 8);
+    const int bit = (rel[2] * res + rel[1]) * res + rel[0];
+    a.pclist[(size_t)pidx * res * res * res + bit] = ((uint64_t)i << 16) | ((uint64_t)a.lev << 8);
+    a.nodes[i] = nd;
+    if (a.leaf_key) a.leaf_key[i] = key;
+}
+
+__global__ void k_write_root(GvxNode* root, int lev, int px, int py, int pz)
+{
+    GvxNode nd;
+    nd.lev = (uint8_t)lev;
+    nd.flags = 1;
+    nd.prio = 0;
+    nd.pad = 0;
+    nd.pos[0] = px;
+    nd.pos[1] = py;
+    nd.pos[2] = pz;
+    for (int k = 0; k < 3; k++) {
+        nd.value[k] = -1;
+        nd.vrange[k] = 0.f;
+    }
+    nd.parent = ID_UNDEFL_U64;
+    nd.childlist = 1ull | ((uint64_t)lev << 8);
+    nd.mask = 0ull;
+    *root = nd;
+}
+
+// run of equal keys in sorted order -> [start, end) of its leaf
+__global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t invalid_key, LeafLookup L,
+                             int2* leaf_range)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = skeys[i];
+    if (k >= invalid_key) return;
+    const bool first = i == 0 || skeys[i - 1] != k;
+    const bool last = i + 1 == n || skeys[i + 1] != k;
+    if (!first && !last) return;
+    int c[3];
+    ks_unpack(L.ks, k, 0, c);
+    const int leaf = ll_find(L, c[0], c[1], c[2]);
+    if (leaf < 0) return;
+    if (first) leaf_range[leaf].x = (int)i;
+    if (last) leaf_range[leaf].y = (int)(i + 1);
+}
+
+// 27-neighbourhood of every leaf (leaf pool indices, -1 where no leaf)
+__global__ void k_neighbors(const uint32_t* __restrict__ leaf_key, uint32_t nleaves, LeafLookup L, int* nbr)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nleaves * 27u) return;
+    const uint32_t leaf = t / 27u, d = t % 27u;
+    int c[3];
+    ks_unpack(L.ks, leaf_key[leaf], 0, c);
+    nbr[t] = ll_find(L, c[0] + (int)(d % 3u) - 1, c[1] + (int)((d / 3u) % 3u) - 1, c[2] + (int)(d / 9u) - 1);
+}
+
+// active leaves (mFlags) -> bitmap over pool indices
+__global__ void k_flag_bits(const GvxNode* __restrict__ nodes, uint32_t n, uint32_t* bits)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool f = i < n && nodes[i].flags;
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, f);
+    if ((threadIdx.x & 31) == 0 && i < ((n + 31u) & ~31u)) bits[i >> 5] = b;
+}
+
+// UpdateAtlas: active leaf k (pool order) -> atlas slot k, mValue, atlas map
+// (VG.cpp:2650-2690, AL.cpp:692-715)
+__global__ void k_atlas_assign(GvxNode* nodes, uint32_t n, const uint32_t* __restrict__ fbits,
+                               const uint32_t* __restrict__ fprefix, int sx, int sy, int P, int apron,
+                               int* leaf_slot, int* slot_leaf, int4* amap)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!((fbits[i >> 5] >> (i & 31)) & 1u)) {
+        leaf_slot[i] = -1;
+        return;
+    }
+    const uint32_t s = fprefix[i >> 5] + __popc(fbits[i >> 5] & ((1u << (i & 31)) - 1u));
+    const int a2 = sx * sy;
+    const int z = (int)s / a2, rem = (int)s - z * a2;
+    const int y = rem / sx, x = rem - y * sx;
+    GvxNode* nd = nodes + i;
+    nd->value[0] = x * P + apron;
+    nd->value[1] = y * P + apron;
+    nd->value[2] = z * P + apron;
+    leaf_slot[i] = (int)s;
+    slot_leaf[s] = (int)i;
+    amap[s] = make_int4(nd->pos[0], nd->pos[1], nd->pos[2], (int)i);
+}
+
+// ComputeBounds (VG.cpp:1792-1816): bbox of active leaves
+__global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int range, int* out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !nodes[i].flags) return;
+    for (int a = 0; a < 3; a++) {
+        atomicMin(&out[a], nodes[i].pos[a]);
+        atomicMax(&out[3 + a], nodes[i].pos[a] + range);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+
+static inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
+{
+    uint32_t e = 0;
+    GVX_CK(cudaMemcpyAsync(&e, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    if (e & GVX_DERR_TIMEOUT) {
+        gvx_set_error("%s: a device spin-wait timed out", stage);
+        return GVX_ERR_TIMEOUT;
+    }
+    if (e & GVX_DERR_CAPACITY) {
+        gvx_set_error("%s: device buffer capacity exceeded", stage);
+        return GVX_ERR_CAPACITY;
+    }
+    if (e & GVX_DERR_BADPOINT) {
+        gvx_set_error("%s: NaN point position", stage);
+        return GVX_ERR_INVALID_ARG;
+    }
+    return GVX_OK;
+}
+
+static gvx_status ensure_grid_scratch(gvx_grid* g)
+{
+    GVX_CK(gvx_ensure(g->d_err, 64));
+    GVX_CK(gvx_ensure(g->d_bbox, 64));
+    GVX_CK(gvx_ensure(g->d_counts, 64 * sizeof(uint32_t)));
+    return GVX_OK;
+}
+
+// sort the points by compact key in key space `ks` (positions + t), fill
+// leaf_range for the leaves of `L` (whose key space must be ks)
+static gvx_status sort_points(gvx_grid* g, int n, const float t[3], const KeySpace& ks, bool fuse_hist)
+{
+    GVX_CK(gvx_ensure(g->keys[0], (size_t)n * 4));
+    GVX_CK(gvx_ensure(g->keys[1], (size_t)n * 4));
+    GVX_CK(gvx_ensure(g->vals[0], (size_t)n * 4));
+    GVX_CK(gvx_ensure(g->vals[1], (size_t)n * 4));
+    const uint32_t invalid_key = 1u << ks.total_bits;
+    const int bits = ks.total_bits + 1;
+    const int passes = gvx_sort_passes(bits);
+    gvx_status rc = gvx_sort_prepare_hist(g->sort, bits, g->stream);
+    if (rc) return rc;
+    const unsigned kb = std::min(blocks_for(n, 256), 152u * 8u);
+    k_keys<<<kb, 256, 0, g->stream>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, t[0], t[1], t[2],
+                                      ks, 1.0f / (float)g->brick, passes, invalid_key, g->keys[0].as<uint32_t>(),
+                                      g->vals[0].as<uint32_t>(), gvx_sort_hist_ptr(g->sort),
+                                      g->d_err.as<uint32_t>());
+    g->launches++;
+    uint32_t* kk[2] = {g->keys[0].as<uint32_t>(), g->keys[1].as<uint32_t>()};
+    uint32_t* vv[2] = {g->vals[0].as<uint32_t>(), g->vals[1].as<uint32_t>()};
+    int res = 0;
+    rc = gvx_sort_pairs(kk, vv, (uint32_t)n, bits, g->sort, fuse_hist, g->stream, g->d_err.as<uint32_t>(), &res,
+                        &g->launches);
+    if (rc) return rc;
+    g->sorted_buf = res;
+    g->n_sorted = (uint32_t)n;
+    return GVX_OK;
+}
+
+static gvx_status fill_leaf_ranges(gvx_grid* g, uint32_t nleaves)
+{
+    GVX_CK(gvx_ensure(g->leaf_range, (size_t)(nleaves + 1) * sizeof(int2)));
+    GVX_CK(cudaMemsetAsync(g->leaf_range.p, 0, (size_t)(nleaves + 1) * sizeof(int2), g->stream));
+    if (g->n_sorted) {
+        k_group_runs<<<blocks_for(g->n_sorted, 256), 256, 0, g->stream>>>(
+            g->keys[g->sorted_buf].as<uint32_t>(), g->n_sorted, 1u << g->lookup.ks.total_bits, g->lookup,
+            g->leaf_range.as<int2>());
+        g->launches++;
+    }
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
+static gvx_status grow_nodes(gvx_grid* g, int lev, int64_t cnt)
+{
+    GVX_CK(gvx_ensure(g->nodes[lev], (size_t)std::max<int64_t>(cnt, 1) * sizeof(GvxNode)));
+    if (lev > 0) {
+        const size_t vc = (size_t)g->res[lev] * g->res[lev] * g->res[lev];
+        GVX_CK(gvx_ensure(g->clist[lev], (size_t)std::max<int64_t>(cnt, 1) * vc * sizeof(uint64_t)));
+    }
+    return GVX_OK;
+}
+
+// FULL rebuild: ActivateBricksGPU + ActivateExtraBricksGPU semantics
+static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], int depth, const int rootpos[3],
+                            const float mn[3], const float mx[3])
+{
+    cudaStream_t st = g->stream;
+    const int b = g->brick;
+    const bool extra = radius >= 1.0f;
+    if (extra && radius > 0.5f * (float)(b - 1)) {
+        gvx_set_error("RebuildTopology: radius %g exceeds (brick-1)/2 = %g (dilation beyond the 26 neighbours)",
+                      radius, 0.5 * (b - 1));
+        return GVX_ERR_UNSUPPORTED;
+    }
+    // ---- compact level-0 key space over the points' bounding box (+ dilation margin), inside the root
+    KeySpace ks;
+    const int root_lo = rootpos[0] / b;
+    const int root_span = g->range[depth] / b;  // leaves per root side
+    const int align = 1 << g->tshift[depth - 1];
+    int64_t total_bits = 0;
+    for (int a = 0; a < 3; a++) {
+        const int rl = rootpos[a] / b;
+        const float lo_v = mn[a] > 0.f ? mn[a] : 0.f;
+        int lo = (int)floorf((lo_v - radius - 2.0f) / (float)b);
+        int hi = mx[a] < 0.f ? rl : (int)floorf((mx[a] + 2.0f * radius + 2.0f) / (float)b);
+        lo = std::max(lo, rl);
+        hi = std::min(hi, rl + root_span - 1);
+        if (hi < lo) hi = lo;
+        lo = rl + ((lo - rl) / align) * align;
+        ks.lo[a] = lo;
+        ks.bits[a] = ceil_log2((int64_t)hi - lo + 1);
+        total_bits += ks.bits[a];
+    }
+    (void)root_lo;
+    if (total_bits > 30) {
+        gvx_set_error("RebuildTopology: point extents span 2^%lld leaf cells; the compact key space holds 2^30",
+                      (long long)total_bits);
+        return GVX_ERR_UNSUPPORTED;
+    }
+    ks.total_bits = (int)total_bits;
+    const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << total_bits) / 32ull));
+    const uint32_t invalid_key = 1u << ks.total_bits;
+
+    // ---- scratch
+    GVX_CK(gvx_ensure(g->d0_bits, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->d0_prefix, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->x0_bits, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->x0_prefix, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->masks, (size_t)std::max(n, 1) * 4));
+    GVX_CK(gvx_ensure(g->leaf_key, (size_t)std::max(n, 1) * 4));
+    GVX_CK(cudaMemsetAsync(g->d0_bits.p, 0, (size_t)words0 * 4, st));
+    GVX_CK(cudaMemsetAsync(g->x0_bits.p, 0, (size_t)words0 * 4, st));
+    GVX_CK(cudaMemsetAsync(g->d_counts.p, 0, 64 * sizeof(uint32_t), st));
+
+    UpperDesc ud;
+    memset(&ud, 0, sizeof(ud));
+    ud.nlev = depth - 1;
+    uint32_t upper_words = 0;
+    for (int l = 1; l <= ud.nlev; l++) {
+        ud.tshift[l] = g->tshift[l];
+        const int bl = ks_bits_at(ks, g->tshift[l]);
+        ud.words[l] = std::max<uint32_t>(1u, (uint32_t)((1ull << bl) / 32ull));
+        ud.off[l] = upper_words;
+        upper_words += 4u * ud.words[l];
+    }
+    GVX_CK(gvx_ensure(g->upper, (size_t)std::max<uint32_t>(upper_words, 1u) * 4));
+    if (upper_words) GVX_CK(cudaMemsetAsync(g->upper.p, 0, (size_t)upper_words * 4, st));
+
+    // ---- one sort of the compact level-0 keys
+    gvx_status rc = sort_points(g, n, o, ks, true);
+    if (rc) return rc;
+    const uint32_t* skeys = g->keys[g->sorted_buf].as<uint32_t>();
+    const uint32_t* svals = g->vals[g->sorted_buf].as<uint32_t>();
+    uint32_t* counts = g->d_counts.as<uint32_t>();
+
+    // ---- D0: leaves holding points
+    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, invalid_key, g->d0_bits.as<uint32_t>());
+    g->launches++;
+    rc = gvx_bitmap_prefix(g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0, counts + 0, g->tmp_scan,
+                           st, &g->launches);
+    if (rc) return rc;
+    BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>());
+    g->launches++;
+
+    // ---- X0: dilation leaves (radius >= 1, VG.cpp:1207-1208)
+    BitRank x0{g->x0_bits.as<uint32_t>(), g->x0_prefix.as<uint32_t>(), words0};
+    if (extra) {
+        GVX_CK(cudaMemsetAsync(g->masks.p, 0, (size_t)n * 4, st));
+        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
+                                                          g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
+                                                          radius, b, g->masks.as<uint32_t>());
+        k_dilate<<<blocks_for(n, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks,
+                                                     g->masks.as<uint32_t>(), d0, x0.bits, g->d_err.as<uint32_t>());
+        g->launches += 2;
+    }
+    rc = gvx_bitmap_prefix(x0.bits, x0.prefix, words0, counts + 1, g->tmp_scan, st, &g->launches);
+    if (rc) return rc;
+
+    // ---- upper levels: parents of D0 (direct) and of X0 (extra)
+    if (ud.nlev > 0) {
+        k_upper_direct<<<blocks_for(n, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks, ud,
+                                                           g->upper.as<uint32_t>());
+        k_upper_extra<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, words0, ks, ud, g->upper.as<uint32_t>());
+        k_prefix_upper<<<2 * ud.nlev, 256, 0, st>>>(ud, g->upper.as<uint32_t>(), counts);
+        g->launches += 3;
+    }
+    GVX_CK(cudaGetLastError());
+
+    // ---- counts to the host (the one mid-build synchronisation)
+    uint32_t hc[64];
+    GVX_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    GVX_CK(cudaStreamSynchronize(st));
+    rc = gvx_check_device_error(g, "RebuildTopology");
+    if (rc) return rc;
+    const uint32_t U0 = hc[0], X0 = hc[1];
+    uint32_t Ul[GVX_MAXLEV] = {}, Xl[GVX_MAXLEV] = {};
+    Ul[0] = U0;
+    Xl[0] = X0;
+    for (int l = 1; l < depth; l++) {
+        Ul[l] = hc[2 + 2 * (l - 1)];
+        Xl[l] = hc[3 + 2 * (l - 1)];
+    }
+
+    // ---- pools and lists
+    for (int l = 0; l < GVX_MAXLEV; l++) g->count[l] = 0;
+    for (int l = 0; l < depth; l++) {
+        rc = grow_nodes(g, l, (int64_t)Ul[l] + Xl[l]);
+        if (rc) return rc;
+        g->count[l] = (int64_t)Ul[l] + Xl[l];
+    }
+    rc = grow_nodes(g, depth, 1);
+    if (rc) return rc;
+    g->count[depth] = 1;
+    for (int l = 1; l <= depth; l++) {
+        const size_t vc = (size_t)g->res[l] * g->res[l] * g->res[l];
+        GVX_CK(cudaMemsetAsync(g->clist[l].p, 0xFF, (size_t)g->count[l] * vc * sizeof(uint64_t), st));
+    }
+    size_t list_words = (size_t)X0 + 1;
+    for (int l = 1; l < depth; l++) list_words += (size_t)Ul[l] + Xl[l];
+    GVX_CK(gvx_ensure(g->lists, list_words * 4));
+    uint32_t* x0list = g->lists.as<uint32_t>();
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, x0.prefix, words0, x0list);
+    g->launches++;
+    uint32_t* lp = x0list + X0 + 1;
+    const uint32_t* dl[GVX_MAXLEV] = {};
+    const uint32_t* xl[GVX_MAXLEV] = {};
+    dl[0] = g->leaf_key.as<uint32_t>();  // D0 list (overwritten in place by k_write_nodes with the same keys)
+    xl[0] = x0list;
+    for (int l = 1; l < depth; l++) {
+        uint32_t* base = g->upper.as<uint32_t>() + ud.off[l];
+        const uint32_t w = ud.words[l];
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base, base + 2 * w, w, lp);
+        dl[l] = lp;
+        lp += Ul[l];
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base + w, base + 3 * w, w, lp);
+        xl[l] = lp;
+        lp += Xl[l];
+        g->launches += 2;
+    }
+    // leaf keys in pool order: D0 (already there) then X0
+    GVX_CK(gvx_ensure(g->leaf_key, (size_t)std::max<uint64_t>((uint64_t)U0 + X0, (uint64_t)n) * 4 + 4));
+    // (ensure may have reallocated: D0 list must be rebuilt in that case)
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>());
+    dl[0] = g->leaf_key.as<uint32_t>();
+    if (X0)
+        GVX_CK(cudaMemcpyAsync(g->leaf_key.as<uint32_t>() + U0, x0list, (size_t)X0 * 4, cudaMemcpyDeviceToDevice, st));
+    g->launches++;
+
+    // ---- nodes, parents and child lists, top-down
+    k_write_root<<<1, 1, 0, st>>>(g->nodes[depth].as<GvxNode>(), depth, rootpos[0], rootpos[1], rootpos[2]);
+    g->launches++;
+    for (int l = depth - 1; l >= 0; l--) {
+        NodeLevelArgs a;
+        memset(&a, 0, sizeof(a));
+        a.lev = l;
+        a.depth = depth;
+        a.ucount = Ul[l];
+        a.xcount = Xl[l];
+        a.dlist = dl[l];
+        a.xlist = xl[l];
+        a.ks = ks;
+        a.tshift = g->tshift[l];
+        a.tshift_parent = g->tshift[l + 1];
+        a.logdim_parent = g->logdim[l + 1];
+        a.res_parent = g->res[l + 1];
+        for (int k = 0; k < 3; k++) {
+            a.lo[k] = ks.lo[k] >> g->tshift[l];
+            a.root_rel[k] = rootpos[k] / g->range[l];
+        }
+        a.range = g->range[l];
+        if (l + 1 < depth) {
+            uint32_t* base = g->upper.as<uint32_t>() + ud.off[l + 1];
+            const uint32_t w = ud.words[l + 1];
+            a.pd = BitRank{base, base + 2 * w, w};
+            a.px = BitRank{base + w, base + 3 * w, w};
+            a.pucount = Ul[l + 1];
+        }
+        a.nodes = g->nodes[l].as<GvxNode>();
+        a.pclist = g->clist[l + 1].as<uint64_t>();
+        a.leaf_key = nullptr;
+        const uint32_t cnt = Ul[l] + Xl[l];
+        if (cnt) {
+            k_write_nodes<<<blocks_for(cnt, 256), 256, 0, st>>>(a);
+            g->launches++;
+        }
+    }
+
+    // ---- leaf lookup, neighbours, point ranges
+    g->lookup.ks = ks;
+    g->lookup.a = d0;
+    g->lookup.b = x0;
+    g->lookup.b_offset = U0;
+    g->lookup.remap = nullptr;
+    g->lookup_valid = true;
+    const uint32_t L0 = U0 + X0;
+    GVX_CK(gvx_ensure(g->nbr, (size_t)std::max<uint32_t>(L0, 1u) * 27 * sizeof(int)));
+    if (L0) {
+        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), L0, g->lookup,
+                                                                        g->nbr.as<int>());
+        g->launches++;
+    }
+    g->nbr_valid = true;
+    rc = fill_leaf_ranges(g, L0);
+    if (rc) return rc;
+    g->group_valid = true;
+    g->group_pos = g->pts.pos;
+    g->group_n = n;
+    for (int a = 0; a < 3; a++) g->group_trans[a] = o[a];
+
+    g->root_level = depth;
+    for (int a = 0; a < 3; a++) g->root_pos[a] = rootpos[a];
+    g->used_leaves = L0;
+    g->atlas_valid = false;
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
+{
+    if (!g->configured) {
+        gvx_set_error("RebuildTopology: Configure was not called");
+        return GVX_ERR_NOT_CONFIGURED;
+    }
+    if (n <= 0 || n > g->pts.n || !g->pts.pos) {
+        gvx_set_error("RebuildTopology: %d points requested, %d bound by SetPoints", n, g->pts.n);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (!(radius >= 0.f)) {
+        gvx_set_error("RebuildTopology: radius must be >= 0");
+        return GVX_ERR_INVALID_ARG;
+    }
+    gvx_status rc = ensure_grid_scratch(g);
+    if (rc) return rc;
+    const float o[3] = {orig ? orig[0] : 0.f, orig ? orig[1] : 0.f, orig ? orig[2] : 0.f};
+    cudaStream_t st = g->stream;
+    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, st));
+
+    // ---- GetBoundingBox: one reduction, 24 bytes to the host
+    uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    GVX_CK(cudaMemcpyAsync(g->d_bbox.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    const unsigned bb = std::min(blocks_for(n, 256), 152u * 8u);
+    k_bbox<<<bb, 256, 0, st>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, o[0], o[1], o[2],
+                               g->d_bbox.as<uint32_t>(), g->d_err.as<uint32_t>());
+    g->launches++;
+    uint32_t hb[6];
+    GVX_CK(cudaMemcpyAsync(hb, g->d_bbox.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    GVX_CK(cudaStreamSynchronize(st));
+    rc = gvx_check_device_error(g, "GetBoundingBox");
+    if (rc) return rc;
+    float mn[3], mx[3];
+    int pmin[3], pmax[3];
+    for (int a = 0; a < 3; a++) {
+        mn[a] = ord2f(hb[a]);
+        mx[a] = ord2f(hb[3 + a]);
+        float lo = mn[a] - 1.0f, hi = mx[a] + 2.0f;  // VG.cpp:5452-5460
+        lo = 0 > lo ? 0 : lo;
+        hi = 0 > hi ? 0 : hi;
+        g->bbox_min[a] = lo;
+        g->bbox_max[a] = hi;
+        pmin[a] = (int)lo;
+        pmax[a] = (int)hi;
+    }
+    // ---- DetermineDepth: lowest level whose node covers posMin and posMax
+    int depth = -1, rootpos[3] = {0, 0, 0};
+    for (int l = 0; l < g->levels; l++) {
+        const int r = g->range[l];
+        if (pmin[0] / r == pmax[0] / r && pmin[1] / r == pmax[1] / r && pmin[2] / r == pmax[2] / r) {
+            depth = l;
+            for (int a = 0; a < 3; a++) rootpos[a] = pmin[a] / r * r;
+            break;
+        }
+    }
+    if (mode == GVX_TOPO_ACCUMULATE && !g->rebuild_topo) {
+        gvx_set_error("AccumulateTopology on an existing topology: incremental rebuild is not available yet");
+        return GVX_ERR_UNSUPPORTED;
+    }
+    if (depth <= 0) {
+        gvx_set_error(depth == 0 ? "RebuildTopology: point extents smaller than 1 brick"
+                                 : "RebuildTopology: point extents exceed the configured levels");
+        return GVX_ERR_DEPTH;
+    }
+    if (depth >= g->levels) {
+        gvx_set_error("RebuildTopology: point extents need %d levels, %d configured", depth + 1, g->levels);
+        return GVX_ERR_DEPTH;
+    }
+    // ---- state machine of RebuildTopology (VG.cpp:1195-1217)
+    if (mode == GVX_TOPO_FULL) g->rebuild_topo = true;
+    if (!g->rebuild_topo && depth != g->curr_depth) {
+        g->rebuild_topo = true;  // "Depth change in rebuild": Clear + full rebuild
+        g->curr_depth = depth;
+    }
+    if (!g->rebuild_topo) {
+        gvx_set_error("RebuildTopology: incremental rebuild is not available yet (use GVX_TOPO_FULL)");
+        return GVX_ERR_UNSUPPORTED;
+    }
+    rc = topo_full(g, n, radius, o, depth, rootpos, mn, mx);
+    if (rc) {
+        g->root_level = -1;
+        g->lookup_valid = false;
+        g->group_valid = false;
+        return rc;
+    }
+    g->rebuild_topo = false;
+    g->last_rebuild = 1;
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_update_atlas(gvx_grid* g)
+{
+    if (g->root_level < 0) {
+        gvx_set_error("UpdateAtlas: no topology");
+        return GVX_ERR_STATE;
+    }
+    if (!g->have_atlas) {
+        gvx_set_error("UpdateAtlas: no channel added");
+        return GVX_ERR_STATE;
+    }
+    cudaStream_t st = g->stream;
+    const int64_t used = g->used_leaves;
+    gvx_status rc = gvx_grow_atlas(g, used);
+    if (rc) return rc;
+    const int64_t slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
+    const uint32_t L0 = (uint32_t)g->count[0];
+    const uint32_t fw = std::max<uint32_t>(1u, (L0 + 31u) / 32u);
+    GVX_CK(gvx_ensure(g->amap, (size_t)slots * sizeof(int4)));
+    GVX_CK(cudaMemsetAsync(g->amap.p, 0xFF, (size_t)slots * sizeof(int4), st));
+    GVX_CK(gvx_ensure(g->leaf_slot, (size_t)std::max<uint32_t>(L0, 1u) * 4));
+    GVX_CK(gvx_ensure(g->slot_leaf, (size_t)std::max<int64_t>(slots, 1) * 4));
+    GVX_CK(gvx_ensure(g->bm_a, (size_t)fw * 4));
+    GVX_CK(gvx_ensure(g->bm_a_prefix, (size_t)fw * 4));
+    GVX_CK(cudaMemsetAsync(g->bm_a.p, 0, (size_t)fw * 4, st));
+    if (L0) {
+        k_flag_bits<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), L0, g->bm_a.as<uint32_t>());
+        g->launches++;
+        rc = gvx_bitmap_prefix(g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), fw, nullptr, g->tmp_scan, st,
+                               &g->launches);
+        if (rc) return rc;
+        k_atlas_assign<<<blocks_for(L0, 256), 256, 0, st>>>(
+            g->nodes[0].as<GvxNode>(), L0, g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), g->sub[0],
+            g->sub[1], g->P, g->apron, g->leaf_slot.as<int>(), g->slot_leaf.as<int>(), g->amap.as<int4>());
+        g->launches++;
+    }
+    GVX_CK(cudaGetLastError());
+    g->atlas_used = used;
+    g->atlas_valid = true;
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_compute_bounds(gvx_grid* g)
+{
+    if (g->root_level < 0) return GVX_OK;
+    const uint32_t L0 = (uint32_t)g->count[0];
+    int init[6] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000, (int)0x80000000};
+    GVX_CK(cudaMemcpyAsync(g->d_bbox.p, init, sizeof(init), cudaMemcpyHostToDevice, g->stream));
+    if (L0) {
+        k_leaf_bounds<<<blocks_for(L0, 256), 256, 0, g->stream>>>(g->nodes[0].as<GvxNode>(), L0, g->range[0],
+                                                                   g->d_bbox.as<int>());
+        g->launches++;
+    }
+    int hb[6];
+    GVX_CK(cudaMemcpyAsync(hb, g->d_bbox.p, sizeof(hb), cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    for (int a = 0; a < 3; a++) {
+        g->obj_min[a] = L0 ? (float)hb[a] : 0.f;
+        g->obj_max[a] = L0 ? (float)hb[3 + a] : 0.f;
+    }
+    return GVX_OK;
+}
+
+// InsertPoints: group the points by leaf for positions + trans, reusing the
+// grouping of the topology build when it was made from the same points
+gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3])
+{
+    if (!g->lookup_valid) {
+        gvx_set_error("InsertPoints: no topology");
+        return GVX_ERR_STATE;
+    }
+    if (n <= 0 || n > g->pts.n || !g->pts.pos) {
+        gvx_set_error("InsertPoints: %d points requested, %d bound", n, g->pts.n);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    if (g->group_valid && g->group_pos == g->pts.pos && g->group_n == n && t[0] == g->group_trans[0] &&
+        t[1] == g->group_trans[1] && t[2] == g->group_trans[2])
+        return GVX_OK;
+    gvx_status rc = ensure_grid_scratch(g);
+    if (rc) return rc;
+    rc = sort_points(g, n, t, g->lookup.ks, true);
+    if (rc) return rc;
+    rc = fill_leaf_ranges(g, (uint32_t)g->count[0]);
+    if (rc) return rc;
+    g->group_valid = true;
+    g->group_pos = g->pts.pos;
+    g->group_n = n;
+    for (int a = 0; a < 3; a++) g->group_trans[a] = t[a];
+    return GVX_OK;
+}

@@ -1,0 +1,302 @@
+"""ctypes binding of libgvx.so (include/gvx.h) for tests, benchmarks and Python callers.
+
+The binding is a thin mirror of the C ABI: every method calls exactly one
+gvx_* entry point and raises GvxError with the library's message when the
+status is not GVX_OK.  There is no fallback: if libgvx.so is missing or has no
+CUDA device to run on, the calls fail.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgvx.so")
+
+OK = 0
+ERR_NAMES = {1: "INVALID_ARG", 2: "NOT_CONFIGURED", 3: "CAPACITY", 4: "DEVICE", 5: "TIMEOUT",
+             6: "UNSUPPORTED", 7: "DEPTH", 8: "STATE"}
+
+T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
+TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
+SPLAT_TRILINEAR, SPLAT_CUBIC = 0, 1
+
+NODE_DTYPE = np.dtype([("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "u1"),
+                       ("pos", "<i4", (3,)), ("value", "<i4", (3,)), ("vrange", "<f4", (3,)),
+                       ("parent", "<u8"), ("childlist", "<u8"), ("mask", "<u8")])
+assert NODE_DTYPE.itemsize == 64
+
+_ELEM = {T_FLOAT: (np.float32, 1), T_FLOAT3: (np.float32, 4), T_FLOAT4: (np.float32, 4),
+         T_UCHAR: (np.uint8, 1), T_UCHAR4: (np.uint8, 4)}
+
+
+class GvxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("gvx status %d (%s): %s" % (status, ERR_NAMES.get(status, "?"), msg))
+        self.status = status
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("levels", ctypes.c_int), ("logdim", ctypes.c_int * 10), ("brick_res", ctypes.c_int),
+                ("apron", ctypes.c_int), ("root_level", ctypes.c_int), ("top_lev", ctypes.c_int),
+                ("node_count", ctypes.c_int64 * 10), ("used_leaves", ctypes.c_int64),
+                ("atlas_subdim", ctypes.c_int * 3), ("atlas_res", ctypes.c_int * 3), ("channels", ctypes.c_int),
+                ("last_rebuild", ctypes.c_int), ("root_pos", ctypes.c_int * 3), ("bbox_min", ctypes.c_float * 3),
+                ("bbox_max", ctypes.c_float * 3), ("obj_min", ctypes.c_float * 3), ("obj_max", ctypes.c_float * 3)]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libgvx.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libgvx.so not built at %s (run __graft_entry__.build())" % p)
+    lib = ctypes.CDLL(p)
+    vp, i, f, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_int64
+    fp = ctypes.POINTER(ctypes.c_float)
+    ip = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "gvx_last_error": ([], ctypes.c_char_p), "gvx_version": ([], ctypes.c_char_p),
+        "gvx_create": ([i, ctypes.POINTER(vp)], i), "gvx_destroy": ([vp], i),
+        "gvx_set_stream": ([vp, vp], i), "gvx_sync": ([vp], i),
+        "gvx_configure": ([vp, i, ip, ip], i), "gvx_set_channel_default": ([vp, i, i, i], i),
+        "gvx_add_channel": ([vp, i, i, i], i), "gvx_clear_channel": ([vp, i], i),
+        "gvx_fill_channel": ([vp, i, fp], i),
+        "gvx_set_points": ([vp, i, vp, i, i, vp, i, i, vp, i, i], i),
+        "gvx_set_point_attribs": ([vp, vp, vp], i),
+        "gvx_commit_points_host": ([vp, i, vp, i, vp, i, vp, vp], i),
+        "gvx_rebuild_topology": ([vp, i, f, fp, i, i], i), "gvx_request_full_rebuild": ([vp, i], i),
+        "gvx_finish_topology": ([vp], i), "gvx_update_atlas": ([vp], i),
+        "gvx_insert_points": ([vp, i, fp, vp], i),
+        "gvx_scatter_density": ([vp, i, f, f, fp, i], i),
+        "gvx_insert_points_subcell": ([vp, i, i, f, fp, ip], i),
+        "gvx_gather_density": ([vp, i, i, f, fp, i, i], i),
+        "gvx_gather_levelset": ([vp, i, i, f, fp, i, i], i),
+        "gvx_splat": ([vp, i, i, f, fp, i, i, i], i),
+        "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
+        "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
+        "gvx_read_nodes": ([vp, i, vp, i64], i), "gvx_read_childlist": ([vp, i, vp, i64], i),
+        "gvx_read_atlas_map": ([vp, vp, i64], i), "gvx_channel_bytes": ([vp, i, ctypes.POINTER(i64)], i),
+        "gvx_read_channel": ([vp, i, vp, i64], i), "gvx_read_channel_dense": ([vp, i, vp, i64], i),
+        "gvx_channel_device_ptr": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(i64)], i),
+        "gvx_retrieve_brick": ([vp, i, ip, vp, i64], i),
+        "gvx_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _f3(v):
+    v = (0.0, 0.0, 0.0) if v is None else v
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+def _ptr(a):
+    """device pointer of a torch tensor / int, or host pointer of a numpy array"""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    raise TypeError(type(a))
+
+
+class Grid:
+    """One gvx_grid handle (one VolumeGVDB)."""
+
+    def __init__(self, device=0, lib=None):
+        self.lib = lib or load()
+        h = ctypes.c_void_p()
+        self._check(self.lib.gvx_create(device, ctypes.byref(h)))
+        self.h = h
+        self._types = {}
+        self._keep = []
+
+    def _check(self, st):
+        if st != OK:
+            raise GvxError(st, self.lib.gvx_last_error().decode(errors="replace"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gvx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- setup
+    def configure(self, logdim=(3, 3, 3, 3, 5)):
+        ld = (ctypes.c_int * len(logdim))(*logdim)
+        self._check(self.lib.gvx_configure(self.h, len(logdim), ld, None))
+        self.logdim = tuple(logdim)
+
+    def set_channel_default(self, cx, cy, cz):
+        self._check(self.lib.gvx_set_channel_default(self.h, cx, cy, cz))
+
+    def add_channel(self, chan, typ, apron=1):
+        self._check(self.lib.gvx_add_channel(self.h, chan, typ, apron))
+        self._types[chan] = typ
+
+    def clear_channel(self, chan):
+        self._check(self.lib.gvx_clear_channel(self.h, chan))
+
+    def fill_channel(self, chan, value):
+        v = (ctypes.c_float * 4)(*(list(value) + [0.0] * (4 - len(value))))
+        self._check(self.lib.gvx_fill_channel(self.h, chan, v))
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.gvx_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def sync(self):
+        self._check(self.lib.gvx_sync(self.h))
+
+    # --- points
+    def set_points(self, n, pos, pos_offset=0, pos_stride=12, vel=None, vel_offset=0, vel_stride=12):
+        self._check(self.lib.gvx_set_points(self.h, n, _ptr(pos), pos_offset, pos_stride, _ptr(vel), vel_offset,
+                                            vel_stride, None, 0, 0))
+
+    def set_point_attribs(self, weight=None, radius=None):
+        self._check(self.lib.gvx_set_point_attribs(self.h, _ptr(weight), _ptr(radius)))
+
+    def commit_points_host(self, pos, vel=None, weight=None, radius=None):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        arrs = [pos]
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float32)
+        weight = None if weight is None else np.ascontiguousarray(weight, dtype=np.float32)
+        radius = None if radius is None else np.ascontiguousarray(radius, dtype=np.float32)
+        arrs += [a for a in (vel, weight, radius) if a is not None]
+        self._keep = arrs
+        n = pos.shape[0]
+        self._check(self.lib.gvx_commit_points_host(self.h, n, _ptr(pos), pos.strides[0], _ptr(vel),
+                                                    vel.strides[0] if vel is not None else 0, _ptr(weight),
+                                                    _ptr(radius)))
+        return n
+
+    # --- topology
+    def rebuild_topology(self, n, radius, orig=None, mode=TOPO_FULL, min_depth=1):
+        self._check(self.lib.gvx_rebuild_topology(self.h, n, float(radius), _f3(orig), mode, min_depth))
+
+    def request_full_rebuild(self, on=True):
+        self._check(self.lib.gvx_request_full_rebuild(self.h, int(on)))
+
+    def finish_topology(self):
+        self._check(self.lib.gvx_finish_topology(self.h))
+
+    def update_atlas(self):
+        self._check(self.lib.gvx_update_atlas(self.h))
+
+    # --- splats
+    def insert_points(self, n, trans=None, want_pnode=False):
+        out = np.empty(n, np.int32) if want_pnode else None
+        self._check(self.lib.gvx_insert_points(self.h, n, _f3(trans), _ptr(out)))
+        return out
+
+    def scatter_density(self, n, radius, amp=1.0, trans=None, expand=True):
+        self._check(self.lib.gvx_scatter_density(self.h, n, float(radius), float(amp), _f3(trans), int(expand)))
+
+    def splat(self, mode, n, radius, trans=None, chan_density=0, chan_vel=-1, accum=False):
+        self._check(self.lib.gvx_splat(self.h, mode, n, float(radius), _f3(trans), chan_density, chan_vel,
+                                       int(accum)))
+
+    def insert_points_subcell(self, subcell, n, radius, trans=None):
+        ln = ctypes.c_int(0)
+        self._check(self.lib.gvx_insert_points_subcell(self.h, subcell, n, float(radius), _f3(trans),
+                                                       ctypes.byref(ln)))
+        return ln.value
+
+    def gather_density(self, subcell, n, radius, trans=None, chan=0, accum=False):
+        self._check(self.lib.gvx_gather_density(self.h, subcell, n, float(radius), _f3(trans), chan, int(accum)))
+
+    def gather_levelset(self, subcell, n, radius, trans=None, chan=0, accum=False):
+        self._check(self.lib.gvx_gather_levelset(self.h, subcell, n, float(radius), _f3(trans), chan, int(accum)))
+
+    def update_apron(self, chan=None, boundval=0.0):
+        if chan is None:
+            self._check(self.lib.gvx_update_apron_all(self.h))
+        else:
+            self._check(self.lib.gvx_update_apron(self.h, chan, float(boundval)))
+
+    # --- queries
+    def info(self):
+        inf = Info()
+        self._check(self.lib.gvx_get_info(self.h, ctypes.byref(inf)))
+        d = {k: getattr(inf, k) for k, _ in Info._fields_}
+        for k, v in list(d.items()):
+            if not isinstance(v, (int, float)):
+                d[k] = list(v)
+        return d
+
+    def read_nodes(self, level):
+        n = self.info()["node_count"][level]
+        out = np.zeros(n, NODE_DTYPE)
+        self._check(self.lib.gvx_read_nodes(self.h, level, _ptr(out), n))
+        return out
+
+    def read_childlist(self, level):
+        inf = self.info()
+        r = 1 << inf["logdim"][level]
+        n = inf["node_count"][level] * r * r * r
+        out = np.zeros(n, np.uint64)
+        self._check(self.lib.gvx_read_childlist(self.h, level, _ptr(out), n))
+        return out
+
+    def read_atlas_map(self):
+        sd = self.info()["atlas_subdim"]
+        n = sd[0] * sd[1] * sd[2]
+        out = np.zeros((n, 4), np.int32)
+        self._check(self.lib.gvx_read_atlas_map(self.h, _ptr(out), n))
+        return out
+
+    def channel_bytes(self, chan):
+        b = ctypes.c_int64(0)
+        self._check(self.lib.gvx_channel_bytes(self.h, chan, ctypes.byref(b)))
+        return b.value
+
+    def read_channel(self, chan):
+        """brick-major native layout: (slots, P, P, P[, ncomp]) with x fastest"""
+        inf = self.info()
+        P = inf["brick_res"] + 2 * inf["apron"]
+        dt, nc = _ELEM[self._types[chan]]
+        nbytes = self.channel_bytes(chan)
+        out = np.zeros(nbytes // np.dtype(dt).itemsize, dt)
+        self._check(self.lib.gvx_read_channel(self.h, chan, _ptr(out), nbytes))
+        shp = (-1, P, P, P) + ((nc,) if nc > 1 else ())
+        return out.reshape(shp)
+
+    def read_channel_dense(self, chan):
+        """the reference's 3D-array layout: (Z, Y, X[, ncomp])"""
+        inf = self.info()
+        dt, nc = _ELEM[self._types[chan]]
+        nbytes = self.channel_bytes(chan)
+        out = np.zeros(nbytes // np.dtype(dt).itemsize, dt)
+        self._check(self.lib.gvx_read_channel_dense(self.h, chan, _ptr(out), nbytes))
+        X, Y, Z = inf["atlas_res"]
+        shp = (Z, Y, X) + ((nc,) if nc > 1 else ())
+        return out.reshape(shp)
+
+    def channel_device_ptr(self, chan):
+        p = ctypes.c_void_p()
+        b = ctypes.c_int64()
+        self._check(self.lib.gvx_channel_device_ptr(self.h, chan, ctypes.byref(p), ctypes.byref(b)))
+        return p.value, b.value
+
+    def kernel_launches(self):
+        c = ctypes.c_int64()
+        self._check(self.lib.gvx_kernel_launches(self.h, ctypes.byref(c)))
+        return c.value

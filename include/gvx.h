@@ -1,0 +1,186 @@
+/*
+ * gvx.h -- C ABI of the GB300 point -> sparse-volume engine (libgvx.so).
+ *
+ * Drop-in boundary for the GVDB point path.  Each entry point replaces one
+ * VolumeGVDB method of the reference (dunyazad/gvdb-voxels, GVDB Voxels
+ * 1.1.1); the citation beside each declaration is the method it stands in for
+ * (file:line relative to the reference project):
+ *   VG.h   = source/gvdb_library/src/gvdb_volume_gvdb.h
+ *   VG.cpp = source/gvdb_library/src/gvdb_volume_gvdb.cpp
+ *
+ * Conventions
+ *  - Every call returns gvx_status (0 = GVX_OK).  Nothing ever calls exit();
+ *    gvx_last_error() returns a thread-local description of the last failure.
+ *  - Point buffers are BORROWED device pointers (as SetDataGPU/SetPoints alias
+ *    caller memory, VG.cpp:4872-4908); the library never frees them.
+ *  - All device work is ordered on the grid's stream (gvx_set_stream); calls
+ *    that return counts to the host synchronise that stream.
+ *  - Channel data lives in HBM in brick-major order: atlas slot s (the atlas
+ *    brick index (z*sy + y)*sx + x of the reference) holds P^3 voxels,
+ *    P = brick + 2*apron, x fastest.  Node mValue and the atlas map keep the
+ *    reference's atlas voxel coordinates, so gvx_read_channel_dense returns the
+ *    reference's 3D-array layout byte for byte.
+ */
+#ifndef GVX_H
+#define GVX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gvx_grid gvx_grid;
+typedef int gvx_status;
+
+#define GVX_OK 0
+#define GVX_ERR_INVALID_ARG 1
+#define GVX_ERR_NOT_CONFIGURED 2
+#define GVX_ERR_CAPACITY 3
+#define GVX_ERR_DEVICE 4
+#define GVX_ERR_TIMEOUT 5
+#define GVX_ERR_UNSUPPORTED 6
+#define GVX_ERR_DEPTH 7
+#define GVX_ERR_STATE 8
+
+/* channel types: gvdb_types.h:70-78 */
+#define GVX_T_UCHAR 0
+#define GVX_T_UCHAR4 2
+#define GVX_T_FLOAT 3
+#define GVX_T_FLOAT3 4
+#define GVX_T_FLOAT4 5
+
+/* topology modes */
+#define GVX_TOPO_AUTO 0       /* RebuildTopology state machine, VG.cpp:1181-1218 */
+#define GVX_TOPO_FULL 1       /* RequestFullRebuild(true) then RebuildTopology, VG.h:432 */
+#define GVX_TOPO_ACCUMULATE 2 /* AccumulateTopology, VG.cpp:1158-1178 */
+
+/* splat modes of gvx_splat */
+#define GVX_SPLAT_TRILINEAR 0 /* cloud-in-cell into the 8 voxels around a point (no reference counterpart) */
+#define GVX_SPLAT_CUBIC 1     /* Monaghan M4 cubic spline, support R = 2h (no reference counterpart) */
+
+#define GVX_NODE_BYTES 64 /* Node, gvdb_node.h:27-40 */
+
+typedef struct gvx_info {
+    int levels;
+    int logdim[10];
+    int brick_res;         /* voxels per brick side, res[0] */
+    int apron;
+    int root_level;        /* -1 before the first topology */
+    int top_lev;           /* VDBInfo.top_lev */
+    int64_t node_count[10];/* getNumTotalNodes(level) */
+    int64_t used_leaves;   /* getNumUsedNodes(0) */
+    int atlas_subdim[3];   /* bricks per atlas axis */
+    int atlas_res[3];      /* voxels per atlas axis */
+    int channels;
+    int last_rebuild;      /* 1 full, 2 incremental, 0 no change */
+    int root_pos[3];
+    float bbox_min[3];     /* getBoundMin(), posMin after GetBoundingBox */
+    float bbox_max[3];
+    float obj_min[3];      /* ComputeBounds result */
+    float obj_max[3];
+} gvx_info;
+
+const char* gvx_last_error(void);
+const char* gvx_version(void);
+
+/* lifecycle: SetCudaDevice + Initialize (VG.h:325-326) */
+gvx_status gvx_create(int device, gvx_grid** out);
+gvx_status gvx_destroy(gvx_grid* g);
+/* explicit stream for every launch (the reference launches on the NULL stream) */
+gvx_status gvx_set_stream(gvx_grid* g, void* cuda_stream);
+gvx_status gvx_sync(gvx_grid* g);
+
+/* Configure(int levs, int* r, int* ncnt) (VG.h:388, VG.cpp:2380-2434);
+ * logdim[0] is the leaf (brick) level.  init_counts may be NULL. */
+gvx_status gvx_configure(gvx_grid* g, int levels, const int* logdim, const int* init_counts);
+/* SetChannelDefault (VG.h:390) */
+gvx_status gvx_set_channel_default(gvx_grid* g, int cx, int cy, int cz);
+/* AddChannel (VG.h:392, VG.cpp:2437-2453); apron 0 or 1 */
+gvx_status gvx_add_channel(gvx_grid* g, int chan, int type, int apron);
+/* ClearChannel / FillChannel (VG.h:393-395) */
+gvx_status gvx_clear_channel(gvx_grid* g, int chan);
+gvx_status gvx_fill_channel(gvx_grid* g, int chan, const float value[4]);
+
+/* SetPoints (VG.h:541, VG.cpp:4900-4908) + SetDataGPU (VG.cpp:4872-4880):
+ * borrowed device pointers, byte offset and byte stride per point.
+ * vel and clr may be NULL. */
+gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, int pos_stride,
+                          const void* vel, int vel_offset, int vel_stride,
+                          const void* clr, int clr_offset, int clr_stride);
+/* per-point FP32 weight and splat radius for gvx_splat (no reference counterpart;
+ * NULL = weight 1 / the call's radius) */
+gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* radius);
+/* CommitData of host points (VG.cpp:532-538): copies n host points (and optional
+ * velocities, weights, radii) into library-owned device buffers and binds them
+ * as by gvx_set_points.  Strides are in bytes. */
+gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_stride,
+                                  const void* vel, int vel_stride, const float* weight,
+                                  const float* radius);
+
+/* RebuildTopology (VG.h:429, VG.cpp:1181-1218) with mode GVX_TOPO_AUTO/FULL,
+ * AccumulateTopology (VG.h:431) with GVX_TOPO_ACCUMULATE (min_depth = iDepth). */
+gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float orig[3], int mode,
+                                int min_depth);
+/* RequestFullRebuild (VG.h:432) */
+gvx_status gvx_request_full_rebuild(gvx_grid* g, int on);
+/* FinishTopology (VG.h:405, VG.cpp:1579-1593) */
+gvx_status gvx_finish_topology(gvx_grid* g);
+/* UpdateAtlas (VG.h:406, VG.cpp:2630-2704) */
+gvx_status gvx_update_atlas(gvx_grid* g);
+
+/* InsertPoints (VG.h:542, VG.cpp:5219-5267): brick of every point, points
+ * grouped by brick for the splats.  If pnode_out is not NULL it receives the
+ * leaf pool index of every point (0xFFFFFFFF if none), host memory. */
+gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* pnode_out);
+/* ScatterDensity (VG.h:555, VG.cpp:5624-5660, kernel PT.cuh:525-573):
+ * (1 - d^2/r^2)^3 at the point's voxel and, with expand, its 6 face
+ * neighbours, summed into channel 0 of the point's own brick (apron included),
+ * without the reference's racy read-modify-write. */
+gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3],
+                               int expand);
+/* InsertPointsSubcell (VG.h:551, VG.cpp:4971-5092): sc_len receives the number
+ * of (point, subcell) entries, as pSCPntsLength */
+gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius,
+                                     const float trans[3], int* sc_len);
+/* GatherDensity / GatherLevelSet (VG.h:556-557, VG.cpp:5318-5373) */
+gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                              int chan_density, int accum);
+gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                               int chan_levelset, int accum);
+/* TRILINEAR / CUBIC splat of weight (and velocity*weight into a FLOAT3/FLOAT4
+ * channel); chan_vel may be -1.  Without accum every voxel of each active brick
+ * is overwritten (apron voxels with 0). */
+gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float trans[3],
+                     int chan_density, int chan_vel, int accum);
+/* UpdateApron(chan, boundval) / UpdateApron() (VG.h:407-408, VG.cpp:4411-4457) */
+gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
+gvx_status gvx_update_apron_all(gvx_grid* g);
+
+/* queries: getNumTotalNodes/getNumUsedNodes (VG.h:637-643), getBoundMin/Max */
+gvx_status gvx_get_info(gvx_grid* g, gvx_info* out);
+/* node pool of one level as 64-byte Node records (host memory) */
+gvx_status gvx_read_nodes(gvx_grid* g, int level, void* out, int64_t cap_nodes);
+/* child lists of one level (>0): res^3 uint64 Elem references per node */
+gvx_status gvx_read_childlist(gvx_grid* g, int level, uint64_t* out, int64_t cap_entries);
+/* atlas map: per atlas slot {pos.x, pos.y, pos.z, leaf id} */
+gvx_status gvx_read_atlas_map(gvx_grid* g, int32_t* out4, int64_t cap_slots);
+/* channel bytes: brick-major native layout, and the reference's dense layout */
+gvx_status gvx_channel_bytes(gvx_grid* g, int chan, int64_t* bytes);
+gvx_status gvx_read_channel(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
+gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
+/* device pointer of a channel (for in-HBM consumers) */
+gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t* bytes);
+/* AtlasRetrieveBrickXYZ (VG.h:412): one brick's interior (res0^3 values of the
+ * channel's element size) at the brick whose interior corner is the atlas
+ * voxel `corner`, into host memory, x fastest */
+gvx_status gvx_retrieve_brick(gvx_grid* g, int chan, const int corner[3], void* out, int64_t cap_bytes);
+
+/* number of kernels the library has launched on this grid (instrumentation) */
+gvx_status gvx_kernel_launches(gvx_grid* g, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

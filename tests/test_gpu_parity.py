@@ -1,0 +1,215 @@
+"""GPU parity tests: libgvx (through the C ABI) against the oracle on the same
+seeded inputs.  Topology, pools, child lists and the atlas map must be
+bit-exact; FP32 densities must be within DENSITY_TOL of the FP64 oracle."""
+import numpy as np
+import pytest
+
+from parity_util import DENSITY_TOL, compare_topology, rel_error, rel_error_significant
+
+pytestmark = pytest.mark.gpu
+
+LOGDIM = (3, 3, 3, 3, 5)
+
+
+def make_pair(gvx, orc, pos, radius, weight=None, vel=None, radius_pp=None, channels=((0, 3),), logdim=LOGDIM,
+              orig=(0, 0, 0)):
+    g = gvx.Grid(0)
+    g.configure(logdim)
+    o = orc.Oracle(logdim)
+    for c, t in channels:
+        g.add_channel(c, t, 1)
+        o.add_channel(c, t)
+    g.commit_points_host(pos, vel=vel, weight=weight, radius=radius_pp)
+    g.rebuild_topology(len(pos), radius, orig=orig, mode=gvx.TOPO_FULL)
+    g.finish_topology()
+    g.update_atlas()
+    assert o.rebuild_topology(pos, radius, orig=orig) == orc.OK
+    o.update_atlas()
+    return g, o
+
+
+@pytest.fixture(scope="module")
+def c1():
+    import workloads
+
+    return workloads.plain_small()
+
+
+@pytest.mark.parametrize("radius", [0.0, 1.0, 2.0, 3.0])
+def test_topology_plain_small(gvx_mod, orc, c1, radius):
+    pos, w = c1
+    g, o = make_pair(gvx_mod, orc, pos, radius)
+    compare_topology(g, o)
+    assert np.array_equal(g.read_atlas_map(), o.atlas_map())
+    assert g.info()["atlas_subdim"] == list(o.atlas_subdim())
+
+
+@pytest.mark.parametrize("logdim", [(3, 3, 3, 3, 4), (2, 3, 3, 3, 3), (4, 4, 3, 3, 3), (3, 4, 5, 5, 5)])
+def test_topology_other_configs(gvx_mod, orc, logdim):
+    rng = np.random.default_rng(11)
+    pos = (rng.random((30_000, 3)) * np.array([700.0, 300.0, 900.0])).astype(np.float32)
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, logdim=logdim)
+    compare_topology(g, o)
+
+
+def test_topology_with_origin_and_negative_points(gvx_mod, orc):
+    rng = np.random.default_rng(4)
+    pos = (rng.normal(60.0, 40.0, (20_000, 3))).astype(np.float32)  # some coordinates < 0 after orig
+    orig = (5.0, -3.0, 2.5)
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, orig=orig)
+    compare_topology(g, o)
+
+
+def test_topology_is_deterministic(gvx_mod, orc, c1):
+    pos, _ = c1
+    g, _o = make_pair(gvx_mod, orc, pos, 1.0)
+    a = [g.read_nodes(l) for l in range(3)]
+    g.rebuild_topology(len(pos), 1.0, mode=gvx_mod.TOPO_FULL)
+    g.update_atlas()
+    b = [g.read_nodes(l) for l in range(3)]
+    for x, y in zip(a, b):
+        assert x.tobytes() == y.tobytes()
+
+
+def test_trilinear_plain_small(gvx_mod, orc, c1):
+    pos, w = c1
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, weight=w)
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w)
+    got, ref = g.read_channel(0), o.read_channel(0)
+    assert got.shape == ref.shape
+    assert rel_error(got, ref) <= DENSITY_TOL
+    assert abs(float(got.astype(np.float64).sum()) - float(w.sum())) <= 1e-5 * float(w.sum())
+
+
+def test_cubic_with_velocity(gvx_mod, orc):
+    rng = np.random.default_rng(2)
+    pos = (rng.random((60_000, 3)) * np.array([128.0, 96.0, 160.0]) + 2.0).astype(np.float32)
+    vel = rng.normal(0, 1, (60_000, 3)).astype(np.float32)
+    g, o = make_pair(gvx_mod, orc, pos, 2.0, vel=vel, channels=((0, 3), (1, 4)))
+    g.splat(gvx_mod.SPLAT_CUBIC, len(pos), 2.0, chan_density=0, chan_vel=1)
+    o.splat(orc.SPLAT_CUBIC, pos, 2.0, vel=vel, chan_vel=1)
+    d, dr = g.read_channel(0), o.read_channel(0)
+    assert rel_error(d, dr) <= DENSITY_TOL
+    v, vr = g.read_channel(1), o.read_channel(1)
+    assert rel_error_significant(v[..., :3], vr[..., :3]) <= 1e-4
+    assert np.abs(v[..., :3] - vr[..., :3]).max() <= 1e-5 * np.abs(vr).max()
+
+
+def test_cubic_per_point_radius_and_weight(gvx_mod, orc):
+    import workloads
+
+    pos, w, r = workloads.differentiable(n=40_000, seed=3, lo=8.0, hi=120.0)
+    g, o = make_pair(gvx_mod, orc, pos, 3.0, weight=w, radius_pp=r)
+    g.splat(gvx_mod.SPLAT_CUBIC, len(pos), 0.0, chan_density=0)
+    o.splat(orc.SPLAT_CUBIC, pos, 0.0, weight=w, radius_pp=r)
+    assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
+
+
+def test_apron_after_trilinear(gvx_mod, orc, c1):
+    pos, w = c1
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, weight=w)
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w)
+    g.update_apron(0, 0.5)
+    o.update_apron(0, 0.5)
+    got, ref = g.read_channel(0), o.read_channel(0)
+    assert rel_error(got, ref) <= DENSITY_TOL
+    # the apron is a copy: bit-exact against the device's own interior values
+    P = got.shape[1]
+    amap = g.read_atlas_map()
+    used = g.info()["used_leaves"]
+    lut = {tuple(amap[s, :3]): s for s in range(used)}
+    s = 0
+    nb = lut.get((amap[s, 0] + 8, amap[s, 1], amap[s, 2]))
+    if nb is not None:
+        assert np.array_equal(got[s][1:P - 1, 1:P - 1, P - 1], got[nb][1:P - 1, 1:P - 1, 1])
+
+
+def test_apron_float3_channel(gvx_mod, orc):
+    rng = np.random.default_rng(9)
+    pos = (rng.random((20_000, 3)) * 90.0 + 1.0).astype(np.float32)
+    vel = rng.normal(0, 1, (20_000, 3)).astype(np.float32)
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, vel=vel, channels=((0, 3), (1, 4)))
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0, chan_vel=1)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, vel=vel, chan_vel=1)
+    g.update_apron(1, -1.0)
+    o.update_apron(1, -1.0)
+    v, vr = g.read_channel(1), o.read_channel(1)
+    assert np.abs(v[..., :3] - vr[..., :3]).max() <= 1e-5 * np.abs(vr).max()
+
+
+def test_ref_scatter(gvx_mod, orc, c1):
+    pos, _ = c1
+    g, o = make_pair(gvx_mod, orc, pos, 0.0)
+    g.clear_channel(0)
+    g.scatter_density(len(pos), 1.5, 1.0, expand=True)
+    o.splat(orc.SPLAT_REF_SCATTER, pos, 1.5, expand=True)
+    got, ref = g.read_channel(0), o.read_channel(0)
+    assert rel_error(got, ref) <= DENSITY_TOL
+
+
+def test_accumulate_adds(gvx_mod, orc, c1):
+    pos, w = c1
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, weight=w)
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0, accum=True)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w, accum=True)
+    assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
+
+
+def test_dense_readback_layout(gvx_mod, orc, c1):
+    pos, w = c1
+    g, _ = make_pair(gvx_mod, orc, pos[:5000], 1.0, weight=w[:5000])
+    g.splat(gvx_mod.SPLAT_TRILINEAR, 5000, 1.0, chan_density=0)
+    bm = g.read_channel(0)
+    dense = g.read_channel_dense(0)
+    inf = g.info()
+    sx, sy, _sz = inf["atlas_subdim"]
+    P = bm.shape[1]
+    for s in (0, 1, 17, 300):
+        if s >= bm.shape[0]:
+            continue
+        bx, by, bz = s % sx, (s // sx) % sy, s // (sx * sy)
+        assert np.array_equal(dense[bz * P:(bz + 1) * P, by * P:(by + 1) * P, bx * P:(bx + 1) * P], bm[s])
+
+
+def test_borrowed_device_pointers(gvx_mod, orc):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(1)
+    pos = (rng.random((10_000, 4)) * 70.0 + 1.0).astype(np.float32)  # stride 16 bytes, xyz + pad
+    dev = torch.from_numpy(pos).cuda()
+    g = gvx_mod.Grid(0)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx_mod.T_FLOAT, 1)
+    g.set_points(len(pos), dev, 0, 16)
+    g.rebuild_topology(len(pos), 1.0, mode=gvx_mod.TOPO_FULL)
+    g.update_atlas()
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+    o = orc.Oracle(LOGDIM)
+    o.add_channel(0, orc.T_FLOAT)
+    o.rebuild_topology(pos[:, :3], 1.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_TRILINEAR, pos[:, :3], 1.0)
+    compare_topology(g, o)
+    assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
+    torch.cuda.synchronize()
+
+
+def test_errors_are_status_codes(gvx_mod):
+    g = gvx_mod.Grid(0)
+    with pytest.raises(gvx_mod.GvxError) as e:
+        g.rebuild_topology(10, 1.0)
+    assert e.value.status == 2  # NOT_CONFIGURED
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx_mod.T_FLOAT, 1)
+    pts = np.full((100, 3), 3.5, np.float32)  # extents inside one brick -> depth 0
+    g.commit_points_host(pts)
+    with pytest.raises(gvx_mod.GvxError) as e:
+        g.rebuild_topology(100, 0.0)
+    assert e.value.status == 7  # DEPTH
+    with pytest.raises(gvx_mod.GvxError):
+        g.add_channel(1, gvx_mod.T_FLOAT, 2)  # apron 2 is not supported by the apron update
+    with pytest.raises(gvx_mod.GvxError):
+        g.splat(gvx_mod.SPLAT_TRILINEAR, 100, 1.0)  # no topology

@@ -1,0 +1,197 @@
+"""CPU tests: the oracle against hand-worked answers derived from the reference
+source (the reference itself ships no tests, fixtures or golden vectors)."""
+import math
+
+import numpy as np
+import pytest
+
+UNDEF64 = 0xFFFFFFFFFFFFFFFF
+
+
+def two_points():
+    return np.array([[10.5, 10.5, 10.5], [300.5, 200.5, 100.5]], np.float32)
+
+
+def test_two_point_topology_r1(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    # bbox (9..302, 9..202, 9..102) -> root at level 2 (range 512), VG.cpp:821-837
+    assert o.root_level() == 2 and o.top_lev() == 2
+    assert [o.num_nodes(l) for l in range(3)] == [3, 2, 1]
+    n2, n1, n0 = o.nodes(2), o.nodes(1), o.nodes(0)
+    assert n2["pos"].tolist() == [[0, 0, 0]]
+    # level 1 in key order (x, y, z): PT.cuh:377-380 + sorted unique keys
+    assert n1["pos"].tolist() == [[0, 0, 0], [256, 192, 64]]
+    # leaves: the two containing leaves, then the extra leaf of the box
+    # [int(p)-r, int(p)+2r] = y in [199, 202] (PT.cuh:481-482) appended after them
+    assert n0["pos"].tolist() == [[8, 8, 8], [296, 200, 96], [296, 192, 96]]
+    # parent references (pid << 16) | ((lev+1) << 8), ND.cuh:496
+    assert n1["parent"].tolist() == [0x200, 0x200]
+    assert n0["parent"].tolist() == [0x100, 0x10100, 0x10100]
+    # child-list references Elem(1, lev, i), VG.cpp:1325 / AL.h:59
+    assert n1["childlist"].tolist() == [0x101, 0x10101]
+    assert n2["childlist"].tolist() == [0x201]
+    root = o.childlist(2)
+    assert {i: int(v) for i, v in enumerate(root) if v != UNDEF64} == {0: 0x100, 92: 0x10100}
+    l1 = o.childlist(1).reshape(2, 512)
+    assert {(n, i): int(l1[n, i]) for n in range(2) for i in range(512) if l1[n, i] != UNDEF64} == {
+        (0, 73): 0x0, (1, 269): 0x10000, (1, 261): 0x20000}
+    o.update_atlas()
+    # atlas slot k -> (k mod 16, k/16 mod 16, k/256) * 10 + 1 (AL.cpp:705-715)
+    assert o.nodes(0)["value"].tolist() == [[1, 1, 1], [11, 1, 1], [21, 1, 1]]
+    amap = o.atlas_map()
+    assert amap[:3].tolist() == [[8, 8, 8, 0], [296, 200, 96, 1], [296, 192, 96, 2]]
+    assert (amap[3:] == -1).all()
+
+
+def test_radius_below_one_has_no_extra_bricks(orc):
+    o = orc.Oracle()
+    assert o.rebuild_topology(two_points(), 0.5) == orc.OK
+    assert o.num_nodes(0) == 2  # VG.cpp:1207: extra bricks only for radius >= 1
+
+
+def test_negative_points_are_dropped(orc):
+    o = orc.Oracle()
+    pts = np.vstack([two_points(), [[-0.5, 5.0, 5.0]]]).astype(np.float32)
+    assert o.rebuild_topology(pts, 0.0) == orc.OK
+    # key lev 255 (PT.cuh:361-371): no leaf for the negative point
+    assert o.nodes(0)["pos"].tolist() == [[8, 8, 8], [296, 200, 96]]
+
+
+def test_single_point_is_degenerate(orc):
+    # one point: every level below the root holds one node, so VDBInfo.top_lev
+    # is level 0 and the reference descends from the wrong node (VG.cpp:3957-3968)
+    o = orc.Oracle()
+    st = o.rebuild_topology(np.array([[100.5, 37.25, 64.0]], np.float32), 0.0, allow_degenerate=True)
+    assert st == orc.ERR_DEGENERATE
+
+
+def test_trilinear_known_values(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    pts = two_points()
+    o.rebuild_topology(pts, 1.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_TRILINEAR, pts, 1.0, weight=np.array([1.0, 2.0], np.float32))
+    d = o.read_channel(0)  # (slots, 10, 10, 10)
+    # leaf 1 = (296,200,96): voxels 300..301, 200..201, 100..101 -> local 4..5, 0..1, 4..5 (+1 apron)
+    blk = d[1]
+    assert np.allclose(blk[5:7, 1:3, 5:7], 0.25)
+    assert math.isclose(blk.sum(), 2.0)
+    # leaf 0: 10.5 -> voxels 10,11 -> local 2,3
+    assert np.allclose(d[0][3:5, 3:5, 3:5], 0.125)
+    assert math.isclose(d.sum(), 3.0)
+
+
+def test_cubic_known_values(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    pts = np.array([[10.5, 10.5, 10.5], [300.0, 203.0, 100.0]], np.float32)
+    o.rebuild_topology(pts, 2.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_CUBIC, pts, 2.0)
+    leaves = o.nodes(0)["pos"].tolist()
+    k = leaves.index([296, 200, 96])
+    blk = o.read_channel(0)[k]
+    c = (100 - 96 + 1, 203 - 200 + 1, 300 - 296 + 1)  # (z, y, x) padded
+    inv_pi = 1.0 / math.pi
+    assert math.isclose(blk[c], inv_pi, rel_tol=1e-12)                       # q = 0
+    assert math.isclose(blk[c[0], c[1], c[2] + 1], 0.25 * inv_pi, rel_tol=1e-12)  # q = 1
+    q = math.sqrt(2.0)
+    assert math.isclose(blk[c[0], c[1] + 1, c[2] + 1], 0.25 * (2 - q) ** 3 * inv_pi, rel_tol=1e-12)
+    assert blk[c[0], c[1], c[2] + 2] == 0.0                                  # q = 2
+
+
+def test_ref_scatter_known_values(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    pts = np.array([[10.5, 10.5, 10.5], [300.25, 200.5, 100.0]], np.float32)
+    o.rebuild_topology(pts, 0.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_REF_SCATTER, pts, 1.0)
+    blk = o.read_channel(0)[1]  # leaf (296,200,96): local p = (4.25, 0.5, 4.0), pi = (4, 0, 4)
+    z, y, x = 4 + 1, 0 + 1, 4 + 1
+    # distFunc (PT.cuh:516-523): (1 - d^2/r^2)^3, unclamped
+    assert math.isclose(blk[z, y, x], (1 - 0.3125) ** 3, rel_tol=1e-12)
+    assert math.isclose(blk[z, y, x - 1], (1 - 1.8125) ** 3, rel_tol=1e-12)
+    assert math.isclose(blk[z, y - 1, x], (1 - 2.3125) ** 3, rel_tol=1e-12)  # the brick's own apron voxel
+
+
+def test_gather_known_values(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    pts = two_points()
+    o.rebuild_topology(pts, 2.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_GATHER_DENSITY, pts, 1.0, subcell=4, radius_ins=2.0)
+    leaves = o.nodes(0)["pos"].tolist()
+    blk = o.read_channel(0)[leaves.index([296, 200, 96])]
+    # GatherDensity (PT.cuh:721-726): max(0, R - |p - v|) at integer voxel positions
+    assert math.isclose(blk[100 - 96 + 1, 1, 300 - 296 + 1], 1.0 - math.sqrt(0.75), rel_tol=1e-9)
+    assert blk[100 - 96 + 1, 1, 299 - 296 + 1] == 0.0
+    o.splat(orc.SPLAT_GATHER_LEVELSET, pts, 1.0, subcell=4, radius_ins=2.0)
+    blk = o.read_channel(0)[leaves.index([296, 200, 96])]
+    assert math.isclose(blk[100 - 96 + 1, 1, 300 - 296 + 1], math.sqrt(0.75) - 1.0, rel_tol=1e-9)
+
+
+def test_apron_copies_neighbours_and_boundary(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    pts = np.array([[10.5, 10.5, 10.5], [303.5, 200.5, 100.5], [304.5, 200.5, 100.5]], np.float32)
+    o.rebuild_topology(pts, 0.0)
+    o.update_atlas()
+    o.splat(orc.SPLAT_TRILINEAR, pts, 1.0)
+    o.update_apron(0, 7.0)
+    leaves = o.nodes(0)["pos"].tolist()
+    d = o.read_channel(0)
+    a, b = d[leaves.index([296, 200, 96])], d[leaves.index([304, 200, 96])]
+    # +x apron of brick a (padded x = 9) holds brick b's interior x = 0 (padded 1)
+    assert np.array_equal(a[1:9, 1:9, 9], b[1:9, 1:9, 1])
+    assert np.array_equal(b[1:9, 1:9, 0], a[1:9, 1:9, 8])
+    # faces with no neighbouring brick take the boundary value
+    assert (a[1:9, 1:9, 0] == 7.0).all() and (a[0, 1:9, 1:9] == 7.0).all()
+
+
+def test_incremental_semantics(orc):
+    base = np.array([[10.5, 10.5, 10.5], [300.5, 200.5, 100.5], [60.5, 40.5, 20.5]], np.float32)
+    o = orc.Oracle()
+    assert o.rebuild_topology(base, 0.0, mode=orc.TOPO_AUTO) == orc.OK
+    assert o.last_mode() == 1
+    # second call: mCurrDepth is still -1, so the reference rebuilds fully again (VG.cpp:1198-1203)
+    assert o.rebuild_topology(base, 0.0, mode=orc.TOPO_AUTO) == orc.OK
+    assert o.last_mode() == 1
+    # third call with a subset: no new node -> markers are not applied (VG.cpp:1066)
+    assert o.rebuild_topology(base[:2], 0.0, mode=orc.TOPO_AUTO) == orc.OK
+    assert o.last_mode() == 0 and o.used_leaves() == 3
+    # a new point in a new leaf: the leaf of point 3 loses its marker and is delinked
+    moved = np.vstack([base[:2], [[120.5, 40.5, 20.5]]]).astype(np.float32)
+    assert o.rebuild_topology(moved, 0.0, mode=orc.TOPO_AUTO) == orc.OK
+    assert o.last_mode() == 2
+    n0 = o.nodes(0)
+    assert n0["pos"].tolist()[-1] == [120, 40, 16]
+    flags = dict(zip(map(tuple, n0["pos"].tolist()), n0["flags"].tolist()))
+    assert flags[(56, 40, 16)] == 0 and flags[(120, 40, 16)] == 1
+    assert n0["parent"][[p.tolist() for p in n0["pos"]].index([56, 40, 16])] == UNDEF64
+    assert o.used_leaves() == 3
+
+
+def test_accumulate_keeps_leaves(orc):
+    base = np.array([[10.5, 10.5, 10.5], [300.5, 200.5, 100.5], [60.5, 40.5, 20.5]], np.float32)
+    o = orc.Oracle()
+    o.rebuild_topology(base, 0.0, mode=orc.TOPO_ACCUMULATE)
+    more = np.vstack([base[:2], [[120.5, 40.5, 20.5]]]).astype(np.float32)
+    assert o.rebuild_topology(more, 0.0, mode=orc.TOPO_ACCUMULATE) == orc.OK
+    assert o.last_mode() == 2 and o.used_leaves() == 4
+
+
+def test_cpu_activate_space_leaf_set(orc):
+    rng = np.random.default_rng(5)
+    pts = (rng.random((3000, 3)) * 200.0 + 3.0).astype(np.float32)
+    leaves, root = orc.activate_space_cpu(pts)
+    o = orc.Oracle()
+    o.rebuild_topology(pts, 0.0)
+    a = {tuple(x) for x in leaves.tolist()}
+    b = {tuple(x) for x in o.nodes(0)["pos"].tolist()}
+    assert a == b
+    assert root == o.root_level()
