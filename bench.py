@@ -1,0 +1,404 @@
+"""Benchmark of the point -> sparse-volume path (topology + splat + apron).
+
+One step = one frame of the SPH slab workload: 4M points in a 1024^3 index
+space, advected by dt * u (30 precomputed frames, cycled), FULL topology
+rebuild with dilation radius 2, cubic-spline splat (R = 2) of density and
+float3 velocity into 8^3 bricks with a 1-voxel apron, then UpdateApron of both
+channels.  Metric: Mpoints/s = points / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same path (the reference's
+host library does not build without OpenGL/X11) on the host cores, on
+bounded sub-box samples of the same workload.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gvdb-voxels_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG)
+
+METRIC = "Mpoints/s (topology+splat+apron, 4M pts)"
+UNIT = "Mpoints/s"
+N_POINTS = 4_000_000
+FRAMES = 30
+DT = 0.5
+RADIUS = 2.0
+LOGDIM = (3, 3, 3, 3, 5)
+BOX = (512.0, 256.0, 1024.0)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def config_dict(points=N_POINTS):
+    return {"workload": "sph_slab: %d points in x<512,y<256,z<1024 of a 1024^3 space, N(0,0.3) jitter, "
+                        "velocity N(0,1), %d frames of Euler advection dt=%.1f cycled; FULL topology rebuild "
+                        "(radius %.0f) + cubic-spline splat R=%.0f of density (float) and velocity (float3) "
+                        "+ UpdateApron of both channels" % (points, FRAMES, DT, RADIUS, RADIUS),
+            "points": points, "frames": FRAMES, "bricks": "8^3 (+1 apron)", "levels": list(LOGDIM),
+            "radius": RADIUS, "rebuild": "full", "l2": "flushed by a 256 MB write before every timed step"}
+
+
+# --------------------------------------------------------------------------
+# CPU side: the oracle (restatement of the reference path) on sub-box samples
+
+def _cpu_sample(args):
+    """one sub-box of the slab at the workload's point density, through the
+    oracle: topology + atlas + cubic splat (density, velocity) + apron x2"""
+    frac, seed = args
+    import numpy as np
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    sub = (BOX[0] * frac[0], BOX[1] * frac[1], BOX[2] * frac[2])
+    n = int(round(N_POINTS * frac[0] * frac[1] * frac[2]))
+    rng = np.random.default_rng(seed)
+    pos = (rng.random((n, 3)) * np.asarray(sub) + 2.0 + rng.normal(0, 0.3, (n, 3))).astype(np.float32)
+    vel = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    t0 = time.perf_counter()
+    o = O.Oracle(LOGDIM)
+    o.add_channel(0, O.T_FLOAT)
+    o.add_channel(1, O.T_FLOAT3)
+    o.rebuild_topology(pos, RADIUS, allow_degenerate=True)
+    o.update_atlas()
+    o.splat(O.SPLAT_CUBIC, pos, RADIUS, vel=vel, chan_density=0, chan_vel=1)
+    o.update_apron(0, 0.0)
+    o.update_apron(1, 0.0)
+    dt = time.perf_counter() - t0
+    o.close()
+    return n, dt
+
+
+SAMPLE_FRAC = (0.25, 0.25, 0.125)  # 1/128 of the slab: 31,250 points at the same density
+
+
+def cpu_pool(workers):
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(workers)
+
+
+def cpu_baseline(pool=None, samples=24):
+    """single-core port: `samples` sub-boxes one after the other"""
+    tot_n, tot_t = 0, 0.0
+    for s in range(samples):
+        n, dt = pool.apply(_cpu_sample, ((SAMPLE_FRAC, 100 + s),)) if pool else _cpu_sample((SAMPLE_FRAC, 100 + s))
+        tot_n += n
+        tot_t += dt
+    return {"value": tot_n / tot_t / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d sub-boxes of 1/128 of the slab (%d points in all, same density), oracle topology + "
+                      "cubic splat (density+velocity) + apron, single thread" % (samples, tot_n)}
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+               0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown", 0x100: "display_clock_setting"}
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], 0, set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 3:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+                bits = int(parts[2], 16)
+            except ValueError:
+                continue
+            for b, name in self.REASONS.items():
+                if bits & b and name != "gpu_idle":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+
+def algorithmic_bytes(n, nb, P):
+    """per frame: positions read by the topology, point attributes
+    read by the splat, every active padded brick written once per channel, and
+    the apron source voxels read once per channel"""
+    ch_bytes = 4 + 16  # density float + velocity float3 stored as float4
+    b_topo = 12 * n
+    b_splat_pts = (12 + 12) * n
+    b_atlas = nb * P ** 3 * ch_bytes
+    b_apron = nb * (P ** 3 - (P - 2) ** 3) * ch_bytes
+    return b_topo, b_splat_pts, b_atlas, b_apron
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "splat_cubic_sph4m_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        if ln.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args, rank, world, pool):
+    import numpy as np
+    import torch
+
+    import gvx
+    import workloads
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        dist.init_process_group("nccl", device_id=dev)
+
+    pos0, vel = workloads.sph_slab(n=N_POINTS, seed=0)
+    n = pos0.shape[0]
+    vel_d = torch.from_numpy(vel).to(dev)
+    pos_d = torch.from_numpy(pos0).to(dev)
+    frames = [pos_d + (f * DT) * vel_d for f in range(FRAMES)]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    g = gvx.Grid(dev.index)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx.T_FLOAT, 1)
+    g.add_channel(1, gvx.T_FLOAT3, 1)
+    g.set_stream(stream.cuda_stream)
+
+    def step(f, events=None):
+        p = frames[f % FRAMES]
+        g.set_points(n, p, 0, 12, vel_d, 0, 12)
+        g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_FULL)
+        g.finish_topology()
+        g.update_atlas()
+        g.insert_points(n)
+        if events:
+            events[0].record(stream)
+        g.splat(gvx.SPLAT_CUBIC, n, RADIUS, chan_density=0, chan_vel=1)
+        if events:
+            events[1].record(stream)
+        g.update_apron(0, 0.0)
+        g.update_apron(1, 0.0)
+
+    with torch.cuda.stream(stream):
+        for w in range(args.warmup):
+            step(w)
+        torch.cuda.synchronize()
+
+        # ---- per-stage breakdown (untimed pass)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
+        p = frames[0]
+        g.set_points(n, p, 0, 12, vel_d, 0, 12)
+        ev[0].record(stream)
+        g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_FULL)
+        g.finish_topology()
+        ev[1].record(stream)
+        g.update_atlas()
+        ev[2].record(stream)
+        g.insert_points(n)
+        ev[3].record(stream)
+        g.splat(gvx.SPLAT_CUBIC, n, RADIUS, chan_density=0, chan_vel=1)
+        ev[4].record(stream)
+        g.update_apron(0, 0.0)
+        ev[5].record(stream)
+        g.update_apron(1, 0.0)
+        ev[6].record(stream)
+        torch.cuda.synchronize()
+        names = ["topology", "update_atlas", "insert_points", "splat", "apron_density", "apron_velocity"]
+        stage_ms = {k: round(ev[i].elapsed_time(ev[i + 1]), 4) for i, k in enumerate(names)}
+
+        # ---- timed region
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        sp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        clocks = ClockSampler(dev.index)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        launches0 = g.kernel_launches()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            starts[k].record(stream)
+            step(args.warmup + k, sp[k])
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        launches = g.kernel_launches() - launches0
+        clk = clocks.stop()
+        if dist:
+            dist.barrier()
+        step_ms = [starts[k].elapsed_time(ends[k]) for k in range(args.steps)]
+        splat_ms = [sp[k][0].elapsed_time(sp[k][1]) for k in range(args.steps)]
+        ms = sum(step_ms) / len(step_ms)
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+
+        inf = g.info()
+        nb = inf["used_leaves"]
+        P = inf["brick_res"] + 2 * inf["apron"]
+
+        # ---- end to end through the C ABI with host buffers (pinned)
+        host_pos = [torch.empty((n, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        host_pos[0].copy_(torch.from_numpy(pos0))
+        host_pos[1].copy_(torch.from_numpy(workloads.advect(pos0, vel, DT)))
+        host_vel = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        host_vel.copy_(torch.from_numpy(vel))
+        e2e_steps = max(3, min(args.steps, 10))
+        res = np.zeros(1 << 16, gvx.NODE_DTYPE)
+        d2h = 0
+        for k in range(2):  # warm
+            g.commit_points_host(host_pos[k % 2], host_vel)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            g.lib.gvx_commit_points_host(g.h, n, host_pos[k % 2].data_ptr(), 12, host_vel.data_ptr(), 12, None,
+                                         None)
+            g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_FULL)
+            g.finish_topology()
+            g.update_atlas()
+            g.insert_points(n)
+            g.splat(gvx.SPLAT_CUBIC, n, RADIUS, chan_density=0, chan_vel=1)
+            g.update_apron(0, 0.0)
+            g.update_apron(1, 0.0)
+            c1 = g.info()["node_count"][1]
+            g._check(g.lib.gvx_read_nodes(g.h, 1, res.ctypes.data, len(res)))
+            d2h = c1 * 64
+        e2e_wall = time.perf_counter() - t0
+    g.close()
+
+    b_topo, b_pts, b_atlas, b_apron = algorithmic_bytes(n, nb, P)
+    splat_bytes = b_pts + b_atlas
+    splat_avg = sum(splat_ms) / len(splat_ms)
+    achieved = splat_bytes / (splat_avg * 1e-3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    traffic = load_traffic()
+    out = {
+        "metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": config_dict(n),
+        "wall_s_timed_region": wall,
+        "stage_ms": stage_ms,
+        "hbm_gbs_step": (b_topo + b_pts + b_atlas + b_apron) / (ms * 1e-3) / 1e9,
+        "active_bricks": nb,
+        "roofline": {"kernel": "k_splat (cubic, density+velocity)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes": splat_bytes, "launch_ms": splat_avg},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "e2e": {"value": world * n * e2e_steps / e2e_wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 24,
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+    }
+    if dist:
+        dist.destroy_process_group()
+    return out
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    workers = max(1, os.cpu_count() or 1)
+    pool = cpu_pool(workers)
+    jobs = [(SAMPLE_FRAC, 1000 + i) for i in range(workers)]
+    for _ in range(args.warmup):
+        pool.map(_cpu_sample, jobs)
+    times, pts = [], 0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        r = pool.map(_cpu_sample, [(SAMPLE_FRAC, 2000 + k * workers + i) for i in range(workers)])
+        times.append(time.perf_counter() - t0)
+        pts = sum(x[0] for x in r)
+    pool.close()
+    ms = 1e3 * sum(times) / len(times)
+    v = pts / (ms * 1e-3) / 1e6
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config_dict(),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                             "sample": "%d independent sub-boxes of 1/128 of the slab per step (%d points, same "
+                                       "density), one per host core" % (workers, pts)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    pool = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool = cpu_pool(1)  # spawned before the first CUDA call
+    out = run_ours(args, rank, world, pool)
+    if rank == 0:
+        if pool is not None:
+            out["cpu_baseline"] = cpu_baseline(pool)
+            pool.close()
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

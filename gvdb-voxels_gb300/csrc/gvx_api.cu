@@ -346,6 +346,7 @@ gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, i
     g->pts.clr_off = clr_offset;
     g->pts.clr_stride = clr_stride;
     g->group_valid = false;
+    g->perm_valid = false;
     return GVX_OK;
 }
 
@@ -354,6 +355,7 @@ gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* 
     GVX_GUARD(g);
     g->pts.weight = weight;
     g->pts.radius = radius;
+    g->perm_valid = false;
     return GVX_OK;
 }
 
@@ -416,7 +418,7 @@ gvx_status gvx_update_atlas(gvx_grid* g)
 gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* pnode_out)
 {
     GVX_GUARD(g);
-    gvx_status rc = gvx_topo_group_points(g, n, trans);
+    gvx_status rc = gvx_prepare_points(g, n, trans, false);
     if (rc || !pnode_out) return rc;
     DevBuf tmp;
     GVX_CK(gvx_ensure(tmp, (size_t)n * 4));
@@ -508,6 +510,8 @@ gvx_status gvx_get_info(gvx_grid* g, gvx_info* out)
         gvx_set_error("get_info: null output");
         return GVX_ERR_INVALID_ARG;
     }
+    gvx_status rc = gvx_topo_read_bounds(g);
+    if (rc) return rc;
     memset(out, 0, sizeof(*out));
     out->levels = g->levels;
     for (int l = 0; l < GVX_MAXLEV; l++) {

@@ -77,6 +77,7 @@ struct gvx_grid {
     DevBuf clist[GVX_MAXLEV];
     float bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
     float obj_min[3] = {0, 0, 0}, obj_max[3] = {0, 0, 0};
+    bool bounds_pending = false;
 
     // lookup of leaves by key for the current topology
     LeafLookup lookup{};
@@ -113,6 +114,11 @@ struct gvx_grid {
     const void* group_pos = nullptr;
     int group_n = -1;
     DevBuf spos, svel;  // sorted float4 (x,y,z,weight) and (vx,vy,vz,radius)
+    bool perm_valid = false;  // spos/svel match the grouping and the bound attributes
+    bool perm_has_svel = false;
+    const void* perm_vel = nullptr;
+    const void* perm_w = nullptr;
+    const void* perm_r = nullptr;
     SortScratch sort;
 
     // scratch of the topology build
@@ -131,6 +137,9 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
 gvx_status gvx_topo_update_atlas(gvx_grid* g);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
+gvx_status gvx_topo_read_bounds(gvx_grid* g);
+// InsertPoints: grouping + sorted attribute arrays
+gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel);
 gvx_status gvx_check_device_error(gvx_grid* g, const char* stage);
 
 // splats (gvx_splat.cu)

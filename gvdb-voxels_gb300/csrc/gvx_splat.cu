@@ -66,12 +66,32 @@ struct SplatArgs {
     uint32_t* err;
 };
 
-// M4 cubic spline (Monaghan & Lattanzio 1985) without the 1/(pi h^3) factor
-__device__ __forceinline__ float m4(float q)
+// M4 cubic spline (Monaghan & Lattanzio 1985) without the 1/(pi h^3) factor,
+// for a voxel at offset (dx, dy, dz) from a point of support R = 2h.  Near the
+// edge of the support the outer branch 0.25 (2-q)^3 loses all precision if
+// 2-q is formed in FP32, so it is evaluated as (R^2 - d^2) / (h (R + d)) with
+// R^2 - d^2 computed from error-free products and sums (fmaf two-product,
+// Knuth two-sum): the result keeps FP32 relative accuracy up to q -> 2.
+__device__ __forceinline__ float m4_offset(float dx, float dy, float dz, float R, float inv_h)
 {
+    const float px = dx * dx, ex = fmaf(dx, dx, -px);
+    const float py = dy * dy, ey = fmaf(dy, dy, -py);
+    const float pz = dz * dz, ez = fmaf(dz, dz, -pz);
+    const float s1 = px + py;
+    float bv = s1 - px;
+    const float e1 = (px - (s1 - bv)) + (py - bv);
+    const float s = s1 + pz;
+    bv = s - s1;
+    const float e2 = (s1 - (s - bv)) + (pz - bv);
+    const float lo = ((ex + ey) + ez) + (e1 + e2);
+    const float r2h = R * R, r2l = fmaf(R, R, -r2h);
+    const float t = (r2h - s) + (r2l - lo);  // R^2 - d^2
+    if (t <= 0.0f) return 0.0f;
+    const float d = sqrtf(s);
+    const float q = d * inv_h;
     if (q < 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
-    const float t = 2.0f - q;
-    return q < 2.0f ? 0.25f * t * t * t : 0.0f;
+    const float u = t / (0.5f * R * (R + d));  // 2 - q
+    return 0.25f * u * u * u;
 }
 
 template <bool HAS_DEN, bool HAS_VEL>
@@ -211,10 +231,9 @@ __global__ void __launch_bounds__(kSplatThreads) k_splat(SplatArgs a)
                     for (int c = lane; c < ncell; c += 32) {
                         const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
                         const int vx = lx0 + cx, vy = ly0 + cy, vz = lz0 + cz;
-                        const float dx = (float)vx - p.x, dy = (float)vy - p.y, dz = (float)vz - p.z;
-                        const float q = sqrtf(dx * dx + dy * dy + dz * dz) * inv_h;
-                        if (q >= 2.0f) continue;
-                        const float wgt = norm * m4(q);
+                        const float m = m4_offset((float)vx - p.x, (float)vy - p.y, (float)vz - p.z, R, inv_h);
+                        if (m == 0.0f) continue;
+                        const float wgt = norm * m;
                         const int t = ((vz - B0z + ap) * P + (vy - B0y + ap)) * P + (vx - B0x + ap);
                         if (HAS_DEN) atomicAdd(&tden[t], wgt);
                         if (HAS_VEL) {
@@ -316,19 +335,34 @@ __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
 
 static inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
-static gvx_status prepare_sorted_attribs(gvx_grid* g, const float t[3], bool need_svel)
+// InsertPoints (VG.cpp:5219-5267): group the points by brick (topology sort,
+// reused when the points and translation are those of the rebuild) and write
+// the sorted float4 attribute arrays the splat kernels stream through
+gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel)
 {
-    const uint32_t n = g->n_sorted;
-    GVX_CK(gvx_ensure(g->spos, (size_t)std::max<uint32_t>(n, 1u) * sizeof(float4)));
-    if (need_svel) GVX_CK(gvx_ensure(g->svel, (size_t)std::max<uint32_t>(n, 1u) * sizeof(float4)));
-    if (n) {
-        k_permute<<<blocks_for(n, 256), 256, 0, g->stream>>>(
-            g->vals[g->sorted_buf].as<uint32_t>(), n, g->pts.pos, g->pts.pos_off, g->pts.pos_stride, g->pts.vel,
+    const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    gvx_status rc = gvx_topo_group_points(g, n, t);
+    if (rc) return rc;
+    if (g->perm_valid && (g->perm_has_svel || !need_svel) && g->perm_vel == g->pts.vel &&
+        g->perm_w == g->pts.weight && g->perm_r == g->pts.radius)
+        return GVX_OK;
+    need_svel = need_svel || g->pts.vel || g->pts.radius;
+    const uint32_t m = g->n_sorted;
+    GVX_CK(gvx_ensure(g->spos, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
+    if (need_svel) GVX_CK(gvx_ensure(g->svel, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
+    if (m) {
+        k_permute<<<blocks_for(m, 256), 256, 0, g->stream>>>(
+            g->vals[g->sorted_buf].as<uint32_t>(), m, g->pts.pos, g->pts.pos_off, g->pts.pos_stride, g->pts.vel,
             g->pts.vel_off, g->pts.vel_stride, g->pts.weight, g->pts.radius, t[0], t[1], t[2], g->spos.as<float4>(),
             need_svel ? g->svel.as<float4>() : nullptr);
         g->launches++;
     }
     GVX_CK(cudaGetLastError());
+    g->perm_valid = true;
+    g->perm_has_svel = need_svel;
+    g->perm_vel = g->pts.vel;
+    g->perm_w = g->pts.weight;
+    g->perm_r = g->pts.radius;
     return GVX_OK;
 }
 
@@ -379,11 +413,8 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         gvx_set_error("Splat: cubic splat needs a radius > 0");
         return GVX_ERR_INVALID_ARG;
     }
-    const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
-    rc = gvx_topo_group_points(g, n, t);
-    if (rc) return rc;
     const bool need_svel = has_v || ppr;
-    rc = prepare_sorted_attribs(g, t, need_svel);
+    rc = gvx_prepare_points(g, n, trans, need_svel);
     if (rc) return rc;
 
     const int P = g->P, P3 = P * P * P;
@@ -435,10 +466,7 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
         gvx_set_error("ScatterDensity: radius must be nonzero");
         return GVX_ERR_INVALID_ARG;
     }
-    const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
-    rc = gvx_topo_group_points(g, n, t);
-    if (rc) return rc;
-    rc = prepare_sorted_attribs(g, t, false);
+    rc = gvx_prepare_points(g, n, trans, false);
     if (rc) return rc;
     const int P = g->P, P3 = P * P * P;
     const size_t smem = (size_t)P3 * 4;

@@ -562,6 +562,12 @@ __global__ void k_atlas_assign(GvxNode* nodes, uint32_t n, const uint32_t* __res
     amap[s] = make_int4(nd->pos[0], nd->pos[1], nd->pos[2], (int)i);
 }
 
+__global__ void k_bounds_init(int* out)
+{
+    if (threadIdx.x < 3) out[threadIdx.x] = 0x7FFFFFFF;
+    else if (threadIdx.x < 6) out[threadIdx.x] = (int)0x80000000;
+}
+
 // ComputeBounds (VG.cpp:1792-1816): bbox of active leaves
 __global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int range, int* out)
 {
@@ -633,6 +639,7 @@ static gvx_status sort_points(gvx_grid* g, int n, const float t[3], const KeySpa
     if (rc) return rc;
     g->sorted_buf = res;
     g->n_sorted = (uint32_t)n;
+    g->perm_valid = false;
     return GVX_OK;
 }
 
@@ -1027,24 +1034,39 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     return GVX_OK;
 }
 
+// ComputeBounds runs on the device; the 24-byte result is read when the host
+// asks for it (gvx_get_info), so FinishTopology adds no synchronisation
 gvx_status gvx_topo_compute_bounds(gvx_grid* g)
 {
     if (g->root_level < 0) return GVX_OK;
+    gvx_status rc = ensure_grid_scratch(g);
+    if (rc) return rc;
     const uint32_t L0 = (uint32_t)g->count[0];
-    int init[6] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000, (int)0x80000000};
-    GVX_CK(cudaMemcpyAsync(g->d_bbox.p, init, sizeof(init), cudaMemcpyHostToDevice, g->stream));
+    GVX_CK(gvx_ensure(g->host_stage, 64));
+    k_bounds_init<<<1, 32, 0, g->stream>>>(g->host_stage.as<int>());
+    g->launches++;
     if (L0) {
         k_leaf_bounds<<<blocks_for(L0, 256), 256, 0, g->stream>>>(g->nodes[0].as<GvxNode>(), L0, g->range[0],
-                                                                   g->d_bbox.as<int>());
+                                                                   g->host_stage.as<int>());
         g->launches++;
     }
+    GVX_CK(cudaGetLastError());
+    g->bounds_pending = true;
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_read_bounds(gvx_grid* g)
+{
+    if (!g->bounds_pending) return GVX_OK;
     int hb[6];
-    GVX_CK(cudaMemcpyAsync(hb, g->d_bbox.p, sizeof(hb), cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaMemcpyAsync(hb, g->host_stage.p, sizeof(hb), cudaMemcpyDeviceToHost, g->stream));
     GVX_CK(cudaStreamSynchronize(g->stream));
+    const bool any = g->count[0] > 0;
     for (int a = 0; a < 3; a++) {
-        g->obj_min[a] = L0 ? (float)hb[a] : 0.f;
-        g->obj_max[a] = L0 ? (float)hb[3 + a] : 0.f;
+        g->obj_min[a] = any ? (float)hb[a] : 0.f;
+        g->obj_max[a] = any ? (float)hb[3 + a] : 0.f;
     }
+    g->bounds_pending = false;
     return GVX_OK;
 }
 
