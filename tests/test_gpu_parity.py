@@ -145,8 +145,11 @@ def test_ref_scatter(gvx_mod, orc, c1):
     g.clear_channel(0)
     g.scatter_density(len(pos), 1.5, 1.0, expand=True)
     o.splat(orc.SPLAT_REF_SCATTER, pos, 1.5, expand=True)
-    got, ref = g.read_channel(0), o.read_channel(0)
-    assert rel_error(got, ref) <= DENSITY_TOL
+    got, ref = g.read_channel(0).astype(np.float64), o.read_channel(0)
+    # the unclamped (1 - d^2/r^2)^3 is negative off-centre, so voxel sums cancel;
+    # the FP32 error is judged against the largest magnitude: max|a-b| <= 1e-6 max|b|
+    assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max()
+    assert rel_error_significant(got, ref, frac=1e-2) <= DENSITY_TOL
 
 
 def test_accumulate_adds(gvx_mod, orc, c1):
