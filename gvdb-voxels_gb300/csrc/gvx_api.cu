@@ -83,16 +83,23 @@ gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need)
     for (int c = 0; c < GVX_MAXCH; c++) {
         GvxChannel& ch = g->ch[c];
         if (!ch.used) continue;
-        DevBuf nb;
-        GVX_CK(gvx_ensure(nb, (size_t)(slots * P3 * ch.elem_bytes)));
-        GVX_CK(cudaMemsetAsync(nb.p, 0, (size_t)(slots * P3 * ch.elem_bytes), g->stream));
-        if (ch.data.p && ch.slots)
-            GVX_CK(cudaMemcpyAsync(nb.p, ch.data.p, (size_t)(std::min(ch.slots, slots) * P3 * ch.elem_bytes),
-                                   cudaMemcpyDeviceToDevice, g->stream));
-        GVX_CK(cudaStreamSynchronize(g->stream));
-        gvx_free(ch.data);
-        ch.data = nb;
+        const size_t old_bytes = (size_t)(ch.slots * P3 * ch.elem_bytes);
+        const size_t new_bytes = (size_t)(slots * P3 * ch.elem_bytes);
+        if (ch.data.p && new_bytes <= ch.data.cap) {
+            // grows inside the allocation: only the new bricks are cleared
+            GVX_CK(cudaMemsetAsync((char*)ch.data.p + old_bytes, 0, new_bytes - old_bytes, g->stream));
+        } else {
+            DevBuf nb;
+            GVX_CK(gvx_ensure(nb, new_bytes));
+            GVX_CK(cudaMemsetAsync((char*)nb.p + old_bytes, 0, new_bytes - old_bytes, g->stream));
+            if (ch.data.p && ch.slots)
+                GVX_CK(cudaMemcpyAsync(nb.p, ch.data.p, old_bytes, cudaMemcpyDeviceToDevice, g->stream));
+            GVX_CK(cudaStreamSynchronize(g->stream));
+            gvx_free(ch.data);
+            ch.data = nb;
+        }
         ch.slots = slots;
+        ch.apron_valid = false;
     }
     g->sub[2] = nz;
     return GVX_OK;
@@ -283,6 +290,7 @@ gvx_status gvx_add_channel(gvx_grid* g, int chan, int type, int apron)
     ch.type = type;
     ch.ncomp = ncomp;
     ch.elem_bytes = eb;
+    ch.apron_valid = false;
     ch.slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
     const size_t bytes = (size_t)ch.slots * g->P * g->P * g->P * eb;
     GVX_CK(gvx_ensure(ch.data, bytes));
@@ -297,8 +305,9 @@ gvx_status gvx_clear_channel(gvx_grid* g, int chan)
         gvx_set_error("ClearChannel: channel %d does not exist", chan);
         return GVX_ERR_INVALID_ARG;
     }
-    const GvxChannel& ch = g->ch[chan];
+    GvxChannel& ch = g->ch[chan];
     GVX_CK(cudaMemsetAsync(ch.data.p, 0, (size_t)ch.slots * g->P * g->P * g->P * ch.elem_bytes, g->stream));
+    ch.apron_valid = false;
     return GVX_OK;
 }
 
@@ -309,7 +318,8 @@ gvx_status gvx_fill_channel(gvx_grid* g, int chan, const float value[4])
         gvx_set_error("FillChannel: channel %d does not exist", chan);
         return GVX_ERR_INVALID_ARG;
     }
-    const GvxChannel& ch = g->ch[chan];
+    GvxChannel& ch = g->ch[chan];
+    ch.apron_valid = false;
     uint4 pat = make_uint4(0, 0, 0, 0);
     unsigned char* pb = (unsigned char*)&pat;
     if (ch.type == GVX_T_FLOAT) {
@@ -478,10 +488,22 @@ gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float tra
     return gvx_splat_run(g, mode, n, radius, trans, chan_density, chan_vel, accum);
 }
 
+static gvx_status update_apron_one(gvx_grid* g, int chan, float boundval)
+{
+    if (chan >= 0 && chan < GVX_MAXCH && g->ch[chan].used && g->ch[chan].apron_valid &&
+        g->ch[chan].apron_bv == boundval && g->atlas_valid)
+        return GVX_OK;  // the apron already holds these copies (written by the splat)
+    gvx_status rc = gvx_apron_run(g, chan, boundval);
+    if (rc) return rc;
+    g->ch[chan].apron_valid = true;
+    g->ch[chan].apron_bv = boundval;
+    return GVX_OK;
+}
+
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval)
 {
     GVX_GUARD(g);
-    return gvx_apron_run(g, chan, boundval);
+    return update_apron_one(g, chan, boundval);
 }
 
 gvx_status gvx_update_apron_all(gvx_grid* g)
@@ -489,7 +511,7 @@ gvx_status gvx_update_apron_all(gvx_grid* g)
     GVX_GUARD(g);
     for (int c = 0; c < GVX_MAXCH; c++) {
         if (!g->ch[c].used) continue;
-        gvx_status rc = gvx_apron_run(g, c, 0.0f);
+        gvx_status rc = update_apron_one(g, c, 0.0f);
         if (rc) return rc;
     }
     return GVX_OK;

@@ -11,6 +11,8 @@ struct GvxChannel {
     int elem_bytes = 4;  // bytes per voxel
     DevBuf data;         // slots * P^3 * elem_bytes, brick-major
     int64_t slots = 0;
+    bool apron_valid = false;  // apron voxels hold the neighbours' interior values / boundval
+    float apron_bv = 0.f;      // the boundary value they were filled with
 };
 
 struct GvxPoints {

@@ -1,12 +1,17 @@
 // gvx_splat.cu -- point -> brick-atlas splats.
 //
 // Modes
-//   TRILINEAR, CUBIC (no reference counterpart): every active brick PULLS the
-//     points of its 27-brick neighbourhood (points are grouped by brick by the
-//     topology sort), keeps those whose footprint reaches its interior, and
-//     accumulates them in a shared-memory copy of the whole padded brick.  The
-//     brick then leaves shared memory in one bulk (TMA) store per channel, so
-//     there are no global atomics and every brick is written exactly once.
+//   TRILINEAR, CUBIC (no reference counterpart): one warp per active brick
+//     PULLS the points of its 27-brick neighbourhood (points are grouped by
+//     brick by the topology sort), keeps those whose footprint reaches the
+//     PADDED brick, and adds them into a shared-memory copy of the whole padded
+//     brick in their global sorted order, one point at a time across the
+//     warp's lanes.  Every voxel is therefore the same sum, added in the same
+//     order, in the brick that owns it and in the bricks that hold it as an
+//     apron voxel: the splat writes interior and apron together, the apron
+//     bit-identical to the neighbours' interior (UpdateApron's copy
+//     semantics), with no atomics, deterministically, and one bulk (TMA) store
+//     per channel and brick.
 //   REF_SCATTER: ScatterDensity semantics (gvdb_volume_gvdb.cpp:5624-5660,
 //     cuda_gvdb_particles.cuh:516-573): (1 - d^2/r^2)^3 at the point's voxel
 //     and its 6 face neighbours, inside the point's own padded brick, summed
@@ -21,9 +26,36 @@
 
 namespace {
 constexpr int kSplatThreads = 256;
-constexpr int kListCap = 1024;
+constexpr int kFusedWarps = 4;
 constexpr float kInvPi = 0.318309886183790671538f;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
 }  // namespace
+
+// apron voxel number e of a padded brick (apron 1) -> padded coordinates:
+// the two z faces, then per inner z layer the two y rows and the two x ends
+__device__ __forceinline__ void apron_voxel_coords(int e, int P, int& x, int& y, int& z)
+{
+    const int P2 = P * P;
+    if (e < 2 * P2) {
+        z = e < P2 ? 0 : P - 1;
+        const int r = e % P2;
+        y = r / P;
+        x = r % P;
+        return;
+    }
+    const int ring = 4 * P - 4;
+    const int j = e - 2 * P2;
+    z = 1 + j / ring;
+    const int r = j % ring;
+    if (r < 2 * P) {
+        y = r < P ? 0 : P - 1;
+        x = r % P;
+    } else {
+        const int r2 = r - 2 * P;
+        y = 1 + r2 / 2;
+        x = (r2 & 1) ? P - 1 : 0;
+    }
+}
 
 // sorted point attributes: (x, y, z, weight) and (vx, vy, vz, radius)
 __global__ void k_permute(const uint32_t* __restrict__ svals, uint32_t n, const char* pos, int poff, int pstride,
@@ -49,10 +81,10 @@ __global__ void k_permute(const uint32_t* __restrict__ svals, uint32_t n, const 
 }
 
 struct SplatArgs {
-    int mode;
     int brick, P, apron;
     uint32_t nslots;
     const int* slot_leaf;
+    const int* leaf_slot;
     const GvxNode* nodes0;
     const int* nbr;
     const int2* leaf_range;
@@ -63,202 +95,228 @@ struct SplatArgs {
     float* den;          // channel data (slot-major, P^3 per slot) or nullptr
     float4* vel;         // or nullptr
     bool accum;
+    float boundval;
     uint32_t* err;
 };
 
-// M4 cubic spline (Monaghan & Lattanzio 1985) without the 1/(pi h^3) factor,
-// for a voxel at offset (dx, dy, dz) from a point of support R = 2h.  Near the
-// edge of the support the outer branch 0.25 (2-q)^3 loses all precision if
-// 2-q is formed in FP32, so it is evaluated as (R^2 - d^2) / (h (R + d)) with
-// R^2 - d^2 computed from error-free products and sums (fmaf two-product,
-// Knuth two-sum): the result keeps FP32 relative accuracy up to q -> 2.
-__device__ __forceinline__ float m4_offset(float dx, float dy, float dz, float R, float inv_h)
+__device__ __forceinline__ void tile_add(float* tden, float4* tvel, int t, float wgt, float ux, float uy, float uz,
+                                         bool has_den, bool has_vel)
 {
-    const float px = dx * dx, ex = fmaf(dx, dx, -px);
-    const float py = dy * dy, ey = fmaf(dy, dy, -py);
-    const float pz = dz * dz, ez = fmaf(dz, dz, -pz);
-    const float s1 = px + py;
-    float bv = s1 - px;
-    const float e1 = (px - (s1 - bv)) + (py - bv);
-    const float s = s1 + pz;
-    bv = s - s1;
-    const float e2 = (s1 - (s - bv)) + (pz - bv);
-    const float lo = ((ex + ey) + ez) + (e1 + e2);
-    const float r2h = R * R, r2l = fmaf(R, R, -r2h);
-    const float t = (r2h - s) + (r2l - lo);  // R^2 - d^2
-    if (t <= 0.0f) return 0.0f;
-    const float d = sqrtf(s);
-    const float q = d * inv_h;
-    if (q < 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
-    const float u = t / (0.5f * R * (R + d));  // 2 - q
-    return 0.25f * u * u * u;
+    if (has_den) tden[t] += wgt;
+    if (has_vel) {
+        float4 o = tvel[t];
+        o.x += wgt * ux;
+        o.y += wgt * uy;
+        o.z += wgt * uz;
+        tvel[t] = o;
+    }
 }
 
-template <bool HAS_DEN, bool HAS_VEL>
-__global__ void __launch_bounds__(kSplatThreads) k_splat(SplatArgs a)
+template <bool HAS_DEN, bool HAS_VEL, int MODE>
+__global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int P = a.P, P3 = P * P * P, b = a.brick, ap = a.apron;
-    float4* tvel = (float4*)smem;                                     // P^3 float4
-    float* tden = (float*)(smem + (HAS_VEL ? (size_t)P3 * 16 : 0));  // P^3 float
-    __shared__ int s_list[kListCap];
-    __shared__ int s_nlist;
-    __shared__ int2 s_rng[27];
-    __shared__ int s_off[28];
-    __shared__ __align__(8) uint64_t s_bar;
-    __shared__ int s_total;
+    const int P = a.P, P3 = P * P * P, ap = a.apron;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t vel_bytes = HAS_VEL ? (uint32_t)P3 * 16u : 0u;
+    const uint32_t den_bytes = HAS_DEN ? (uint32_t)P3 * 4u : 0u;
+    unsigned char* mytile = smem + (size_t)wid * (vel_bytes + den_bytes);
+    float4* tvel = (float4*)mytile;
+    float* tden = (float*)(mytile + vel_bytes);
+    __shared__ __align__(8) uint64_t s_bar[kFusedWarps];
+    __shared__ int s_rs[kFusedWarps][28];
+    __shared__ int s_ro[kFusedWarps][28];
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t den_bytes = (uint32_t)P3 * 4u, vel_bytes = (uint32_t)P3 * 16u;
-    if (tid == 0) {
-        mbar_init(&s_bar, 1);
+    if (lane == 0) {
+        mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
     }
-    __syncthreads();
+    __syncwarp();
     uint32_t phase = 0;
-
-    for (uint32_t s = blockIdx.x; s < a.nslots; s += gridDim.x) {
+    const uint32_t nw = gridDim.x * kFusedWarps;
+    for (uint32_t s = blockIdx.x * kFusedWarps + wid; s < a.nslots; s += nw) {
         const int leaf = a.slot_leaf[s];
-        const GvxNode& nd = a.nodes0[leaf];
-        const int B0x = nd.pos[0], B0y = nd.pos[1], B0z = nd.pos[2];
+        const GvxNode* nd = a.nodes0 + leaf;
+        const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
 
-        // ---- tile init: previous values (accumulate) or zeros
-        if (a.accum) {
-            if (tid == 0) {
-                mbar_expect_tx(&s_bar, (HAS_DEN ? den_bytes : 0u) + (HAS_VEL ? vel_bytes : 0u));
-                if (HAS_DEN) bulk_g2s(tden, a.den + (size_t)s * P3, den_bytes, &s_bar);
-                if (HAS_VEL) bulk_g2s(tvel, a.vel + (size_t)s * P3, vel_bytes, &s_bar);
+        // ---- the 27 neighbour ranges, ordered by their place in the sorted points
+        int2 rg = make_int2(0, 0);
+        bool has_nb = false;
+        if (lane < 27) {
+            const int nl = a.nbr[(size_t)leaf * 27 + lane];
+            if (nl >= 0) {
+                rg = a.leaf_range[nl];
+                has_nb = a.leaf_slot[nl] >= 0;
             }
-            if (!mbar_wait_bounded(&s_bar, phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
+        }
+        const uint32_t nbmask = __ballot_sync(kFull, has_nb);
+        const int len = max(0, rg.y - rg.x);
+        int rank = 0, off = 0, total = 0, m = 0;
+        for (int k = 0; k < 27; k++) {
+            const int sk = __shfl_sync(kFull, rg.x, k), lk = __shfl_sync(kFull, len, k);
+            if (lk > 0) {
+                m++;
+                total += lk;
+                if (sk < rg.x) {
+                    rank++;
+                    off += lk;
+                }
+            }
+        }
+        if (lane < 27 && len > 0) {
+            s_rs[wid][rank] = rg.x;
+            s_ro[wid][rank] = off;
+        }
+        if (lane == 0) s_ro[wid][m] = total;
+
+        // ---- tile: previous values (accumulate) or zeros
+        if (a.accum) {
+            if (lane == 0) {
+                mbar_expect_tx(&s_bar[wid], vel_bytes + den_bytes);
+                if (HAS_DEN) bulk_g2s(tden, a.den + (size_t)s * P3, den_bytes, &s_bar[wid]);
+                if (HAS_VEL) bulk_g2s(tvel, a.vel + (size_t)s * P3, vel_bytes, &s_bar[wid]);
+            }
+            if (!mbar_wait_bounded(&s_bar[wid], phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
             phase ^= 1u;
         } else {
-            for (int i = tid; i < P3; i += kSplatThreads) {
+            for (int i = lane; i < P3; i += 32) {
                 if (HAS_DEN) tden[i] = 0.f;
                 if (HAS_VEL) tvel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
-        if (tid < 27) {
-            const int nl = a.nbr[(size_t)leaf * 27 + tid];
-            s_rng[tid] = nl >= 0 ? a.leaf_range[nl] : make_int2(0, 0);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            int acc = 0;
-            for (int k = 0; k < 27; k++) {
-                s_off[k] = acc;
-                acc += max(0, s_rng[k].y - s_rng[k].x);
-            }
-            s_off[27] = acc;
-            s_total = acc;
-        }
-        __syncthreads();
-        const int total = s_total;
+        __syncwarp();
 
-        // ---- candidates in rounds: filter into the list, then splat the list
-        for (int base = 0; base < total; base += kListCap) {
-            if (tid == 0) s_nlist = 0;
-            __syncthreads();
-            for (int v = base + tid; v < min(total, base + kListCap); v += kSplatThreads) {
-                int k = 0;
-                while (k < 26 && s_off[k + 1] <= v) k++;
-                const int i = s_rng[k].x + (v - s_off[k]);
-                const float4 p = a.spos[i];
-                float R = a.radius;
-                if (a.per_point_radius) R = a.svel[i].w;
-                int lo[3], hi[3];
-                const float pc[3] = {p.x, p.y, p.z};
-                const int B0[3] = {B0x, B0y, B0z};
-                bool hit = true;
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    if (a.mode == GVX_SPLAT_TRILINEAR) {
-                        lo[c] = (int)floorf(pc[c]);
-                        hi[c] = lo[c] + 1;
-                    } else {
-                        lo[c] = (int)floorf(pc[c] - R);
-                        hi[c] = (int)ceilf(pc[c] + R);
-                    }
-                    if (hi[c] < B0[c] || lo[c] >= B0[c] + b) hit = false;
+        // ---- candidates, 32 at a time, in sorted order
+        for (int base = 0; base < total; base += 32) {
+            const int v = base + lane;
+            int idx = -1;
+            if (v < total) {
+                int lo = 0, hi = m - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_ro[wid][mid] <= v)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
                 }
-                if (hit) {
-                    const int slot = atomicAdd(&s_nlist, 1);
-                    s_list[slot] = i;
-                }
+                idx = s_rs[wid][lo] + (v - s_ro[wid][lo]);
             }
-            __syncthreads();
-            const int nlist = s_nlist;
-            if (a.mode == GVX_SPLAT_TRILINEAR) {
-                for (int e = tid; e < nlist; e += kSplatThreads) {
-                    const int i = s_list[e];
-                    const float4 p = a.spos[i];
-                    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (HAS_VEL) u = a.svel[i];
-                    const float fx0 = floorf(p.x), fy0 = floorf(p.y), fz0 = floorf(p.z);
-                    const float f[3] = {p.x - fx0, p.y - fy0, p.z - fz0};
-                    const int i0[3] = {(int)fx0 - B0x, (int)fy0 - B0y, (int)fz0 - B0z};
-#pragma unroll
-                    for (int c = 0; c < 8; c++) {
-                        const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-                        const int lx = i0[0] + dx, ly = i0[1] + dy, lz = i0[2] + dz;
-                        if (lx < 0 || ly < 0 || lz < 0 || lx >= b || ly >= b || lz >= b) continue;
-                        const float wgt = p.w * (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) *
-                                          (dz ? f[2] : 1.f - f[2]);
-                        const int t = ((lz + ap) * P + (ly + ap)) * P + (lx + ap);
-                        if (HAS_DEN) atomicAdd(&tden[t], wgt);
-                        if (HAS_VEL) {
-                            atomicAdd(&tvel[t].x, wgt * u.x);
-                            atomicAdd(&tvel[t].y, wgt * u.y);
-                            atomicAdd(&tvel[t].z, wgt * u.z);
-                        }
-                    }
-                }
-            } else {
-                // one point per warp, lanes over the footprint box clipped to the brick
-                for (int e = warp; e < nlist; e += kSplatThreads / 32) {
-                    const int i = s_list[e];
-                    const float4 p = a.spos[i];
-                    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (HAS_VEL || a.per_point_radius) u = a.svel[i];
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f), u = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool hit = false;
+            if (idx >= 0) {
+                p = a.spos[idx];
+                if (HAS_VEL || a.per_point_radius) u = a.svel[idx];
+                if (MODE == GVX_SPLAT_TRILINEAR) {
+                    const int x0 = (int)floorf(p.x), y0 = (int)floorf(p.y), z0 = (int)floorf(p.z);
+                    hit = x0 + 1 >= Ox && x0 < Ox + P && y0 + 1 >= Oy && y0 < Oy + P && z0 + 1 >= Oz && z0 < Oz + P;
+                } else {
                     const float R = a.per_point_radius ? u.w : a.radius;
+                    hit = (int)ceilf(p.x + R) >= Ox && (int)floorf(p.x - R) < Ox + P && (int)ceilf(p.y + R) >= Oy &&
+                          (int)floorf(p.y - R) < Oy + P && (int)ceilf(p.z + R) >= Oz && (int)floorf(p.z - R) < Oz + P;
+                }
+            }
+            uint32_t hm = __ballot_sync(kFull, hit);
+            while (hm) {
+                const int src = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                const float px = __shfl_sync(kFull, p.x, src), py = __shfl_sync(kFull, p.y, src);
+                const float pz = __shfl_sync(kFull, p.z, src), pw = __shfl_sync(kFull, p.w, src);
+                float ux = 0.f, uy = 0.f, uz = 0.f;
+                if (HAS_VEL) {
+                    ux = __shfl_sync(kFull, u.x, src);
+                    uy = __shfl_sync(kFull, u.y, src);
+                    uz = __shfl_sync(kFull, u.z, src);
+                }
+                if (MODE == GVX_SPLAT_TRILINEAR) {
+                    if (lane < 8) {
+                        const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
+                        const int dx = lane & 1, dy = (lane >> 1) & 1, dz = lane >> 2;
+                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Oz;
+                        if (lx >= 0 && ly >= 0 && lz >= 0 && lx < P && ly < P && lz < P) {
+                            const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
+                            const float wgt =
+                                pw * (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
+                            tile_add(tden, tvel, (lz * P + ly) * P + lx, wgt, ux, uy, uz, HAS_DEN, HAS_VEL);
+                        }
+                    }
+                } else {
+                    // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
+                    // support R = 2h.  Rows (y, z) over the lanes; along a row R^2 - d^2 is
+                    // formed from an error-free c = R^2 - dy^2 - dz^2 (two-product, two-sum)
+                    // so that the outer branch 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3
+                    // keeps FP32 relative accuracy up to the edge of the support.
+                    const float R = a.per_point_radius ? __shfl_sync(kFull, u.w, src) : a.radius;
                     const float h = 0.5f * R, inv_h = 1.0f / h;
-                    const float norm = kInvPi * inv_h * inv_h * inv_h * p.w;
-                    const int lx0 = max((int)floorf(p.x - R), B0x), lx1 = min((int)ceilf(p.x + R), B0x + b - 1);
-                    const int ly0 = max((int)floorf(p.y - R), B0y), ly1 = min((int)ceilf(p.y + R), B0y + b - 1);
-                    const int lz0 = max((int)floorf(p.z - R), B0z), lz1 = min((int)ceilf(p.z + R), B0z + b - 1);
-                    const int nx = lx1 - lx0 + 1, ny = ly1 - ly0 + 1, nz = lz1 - lz0 + 1;
-                    if (nx <= 0 || ny <= 0 || nz <= 0) continue;
-                    const int ncell = nx * ny * nz;
-                    for (int c = lane; c < ncell; c += 32) {
-                        const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-                        const int vx = lx0 + cx, vy = ly0 + cy, vz = lz0 + cz;
-                        const float m = m4_offset((float)vx - p.x, (float)vy - p.y, (float)vz - p.z, R, inv_h);
-                        if (m == 0.0f) continue;
-                        const float wgt = norm * m;
-                        const int t = ((vz - B0z + ap) * P + (vy - B0y + ap)) * P + (vx - B0x + ap);
-                        if (HAS_DEN) atomicAdd(&tden[t], wgt);
-                        if (HAS_VEL) {
-                            atomicAdd(&tvel[t].x, wgt * u.x);
-                            atomicAdd(&tvel[t].y, wgt * u.y);
-                            atomicAdd(&tvel[t].z, wgt * u.z);
+                    const float norm = kInvPi * inv_h * inv_h * inv_h * pw;
+                    const float r2h = R * R, r2l = fmaf(R, R, -r2h);
+                    const int xl = max((int)floorf(px - R), Ox), xh = min((int)ceilf(px + R), Ox + P - 1);
+                    const int yl = max((int)floorf(py - R), Oy), yh = min((int)ceilf(py + R), Oy + P - 1);
+                    const int zl = max((int)floorf(pz - R), Oz), zh = min((int)ceilf(pz + R), Oz + P - 1);
+                    const int ny = yh - yl + 1, nz = zh - zl + 1;
+                    for (int r = lane; r < ny * nz; r += 32) {
+                        const int y = yl + r % ny, z = zl + r / ny;
+                        const float dy = (float)y - py, dz = (float)z - pz;
+                        const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
+                        const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
+                        const float syz = qy + qz;
+                        float bv = syz - qy;
+                        const float e1 = (qy - (syz - bv)) + (qz - bv);
+                        const float c1 = r2h - syz;
+                        bv = c1 - r2h;
+                        const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
+                        const float cl = e2 + r2l - ((ey + ez) + e1);
+                        if (c1 + cl <= 0.0f) continue;
+                        const int t0 = ((z - Oz) * P + (y - Oy)) * P - Ox;
+                        for (int x = xl; x <= xh; x++) {
+                            const float dx = (float)x - px;
+                            const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
+                            if (t <= 0.0f) continue;
+                            const float d = sqrtf(fmaf(dx, dx, syz));
+                            const float q = d * inv_h;
+                            float wm;
+                            if (q < 1.0f) {
+                                wm = 1.0f - 1.5f * q * q + 0.75f * q * q * q;
+                            } else {
+                                const float uu = t / (h * (R + d));  // 2 - q
+                                wm = 0.25f * uu * uu * uu;
+                            }
+                            tile_add(tden, tvel, t0 + x, norm * wm, ux, uy, uz, HAS_DEN, HAS_VEL);
                         }
                     }
                 }
+                __syncwarp();
             }
-            __syncthreads();
         }
 
-        // ---- one bulk store per channel for the whole padded brick
+        // ---- apron voxels with no neighbouring brick take the boundary value
+        if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu) {
+            const int napron = 6 * P * P - 12 * P + 8;
+            for (int e = lane; e < napron; e += 32) {
+                int x, y, z;
+                apron_voxel_coords(e, P, x, y, z);
+                const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
+                const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
+                const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
+                if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
+                const int t = (z * P + y) * P + x;
+                if (HAS_DEN) tden[t] = a.boundval;
+                if (HAS_VEL) tvel[t] = make_float4(a.boundval, a.boundval, a.boundval, a.boundval);
+            }
+            __syncwarp();
+        }
+
+        // ---- one bulk store per channel
         fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
+        __syncwarp();
+        if (lane == 0) {
             if (HAS_DEN) bulk_s2g(a.den + (size_t)s * P3, tden, den_bytes);
             if (HAS_VEL) bulk_s2g(a.vel + (size_t)s * P3, tvel, vel_bytes);
             bulk_commit();
             bulk_wait_read_all();
         }
-        __syncthreads();
+        __syncwarp();
     }
-    if (tid == 0) bulk_wait_all();
+    if (lane == 0) bulk_wait_all();
 }
 
 // ScatterDensity, race-free: own points only, into the own padded tile
@@ -386,6 +444,13 @@ static int sm_count(gvx_grid* g)
     return v > 0 ? v : 152;
 }
 
+template <bool D, bool V>
+static void* fused_kernel(int mode)
+{
+    return mode == GVX_SPLAT_TRILINEAR ? (void*)k_splat_fused<D, V, GVX_SPLAT_TRILINEAR>
+                                       : (void*)k_splat_fused<D, V, GVX_SPLAT_CUBIC>;
+}
+
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
                          int accum)
 {
@@ -413,23 +478,28 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         gvx_set_error("Splat: cubic splat needs a radius > 0");
         return GVX_ERR_INVALID_ARG;
     }
+    if (mode == GVX_SPLAT_CUBIC && !ppr && radius > (float)(g->brick - 1)) {
+        gvx_set_error("Splat: radius %g reaches beyond the 26 neighbouring bricks", radius);
+        return GVX_ERR_UNSUPPORTED;
+    }
     const bool need_svel = has_v || ppr;
     rc = gvx_prepare_points(g, n, trans, need_svel);
     if (rc) return rc;
 
     const int P = g->P, P3 = P * P * P;
-    const size_t smem = (has_v ? (size_t)P3 * 16 : 0) + (has_d ? (size_t)P3 * 4 : 0);
-    if (smem > 200 * 1024) {
-        gvx_set_error("Splat: a %d^3 padded brick of these channels needs %zu bytes of shared memory", P, smem);
+    const size_t tile = (has_v ? (size_t)P3 * 16 : 0) + (has_d ? (size_t)P3 * 4 : 0);
+    const size_t smem = tile * kFusedWarps;
+    if (smem > 220 * 1024) {
+        gvx_set_error("Splat: %d warps of %d^3 padded bricks need %zu bytes of shared memory", kFusedWarps, P, smem);
         return GVX_ERR_UNSUPPORTED;
     }
     SplatArgs a;
-    a.mode = mode;
     a.brick = g->brick;
     a.P = P;
     a.apron = g->apron;
     a.nslots = (uint32_t)g->atlas_used;
     a.slot_leaf = g->slot_leaf.as<int>();
+    a.leaf_slot = g->leaf_slot.as<int>();
     a.nodes0 = g->nodes[0].as<GvxNode>();
     a.nbr = g->nbr.as<int>();
     a.leaf_range = g->leaf_range.as<int2>();
@@ -440,17 +510,34 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     a.den = has_d ? g->ch[chan_d].data.as<float>() : nullptr;
     a.vel = has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
     a.accum = accum != 0;
+    a.boundval = 0.0f;
     a.err = g->d_err.as<uint32_t>();
+    // apron state after the splat: exact copies with boundary value 0, unless an
+    // accumulating splat started from an apron that was not a valid copy
+    bool valid_after = true;
+    if (a.accum) {
+        if (has_d) valid_after &= g->ch[chan_d].apron_valid && g->ch[chan_d].apron_bv == 0.0f;
+        if (has_v) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
+    }
     if (a.nslots == 0) return GVX_OK;
-    void (*kern)(SplatArgs) = has_d ? (has_v ? k_splat<true, true> : k_splat<true, false>)
-                                    : k_splat<false, true>;
+    void* kern = has_d ? (has_v ? fused_kernel<true, true>(mode) : fused_kernel<true, false>(mode))
+                       : fused_kernel<false, true>(mode);
     GVX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSplatThreads, smem));
-    const uint32_t grid = std::min<uint32_t>(a.nslots, (uint32_t)(sm_count(g) * std::max(per_sm, 1)));
-    kern<<<grid, kSplatThreads, smem, g->stream>>>(a);
+    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedWarps * 32, smem));
+    const uint64_t ctas_needed = (a.nslots + kFusedWarps - 1) / kFusedWarps;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g) * std::max(per_sm, 1));
+    void* args[] = {&a};
+    GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kFusedWarps * 32), args, smem, g->stream));
     g->launches++;
-    GVX_CK(cudaGetLastError());
+    if (has_d) {
+        g->ch[chan_d].apron_valid = valid_after;
+        g->ch[chan_d].apron_bv = 0.0f;
+    }
+    if (has_v) {
+        g->ch[chan_v].apron_valid = valid_after;
+        g->ch[chan_v].apron_bv = 0.0f;
+    }
     return GVX_OK;
 }
 
@@ -483,6 +570,7 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
     a.expand = expand;
     a.den = g->ch[0].data.as<float>();
     a.err = g->d_err.as<uint32_t>();
+    g->ch[0].apron_valid = false;
     if (a.nslots == 0) return GVX_OK;
     GVX_CK(cudaFuncSetAttribute(k_scatter_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

@@ -1031,6 +1031,7 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     GVX_CK(cudaGetLastError());
     g->atlas_used = used;
     g->atlas_valid = true;
+    for (int c = 0; c < GVX_MAXCH; c++) g->ch[c].apron_valid = false;  // bricks moved to new slots
     return GVX_OK;
 }
 

@@ -150,8 +150,14 @@ gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, con
 gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
                                int chan_levelset, int accum);
 /* TRILINEAR / CUBIC splat of weight (and velocity*weight into a FLOAT3/FLOAT4
- * channel); chan_vel may be -1.  Without accum every voxel of each active brick
- * is overwritten (apron voxels with 0). */
+ * channel) of the points that lie in active bricks; chan_vel may be -1.
+ * Every voxel of each active brick, apron included, receives the sum of the
+ * contributions at its index-space position, so the apron comes out as the
+ * exact copy UpdateApron(chan, 0) would make (a following UpdateApron with
+ * boundary value 0 has nothing left to do).  Without accum the bricks start
+ * from 0 and apron voxels that no brick owns are set to 0; with accum the
+ * contributions are added to the previous values.  The sum of every voxel is
+ * formed in the points' sorted order: results are deterministic. */
 gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float trans[3],
                      int chan_density, int chan_vel, int accum);
 /* UpdateApron(chan, boundval) / UpdateApron() (VG.h:407-408, VG.cpp:4411-4457) */

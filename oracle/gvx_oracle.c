@@ -847,19 +847,53 @@ static kv* active_leaf_table(orc_grid* g, int* nout)
     return t;
 }
 
+/* adds a contribution at world voxel v to every active brick whose padded box
+ * holds v: the owner's interior voxel and the apron copies in its neighbours */
 static void add_contrib(orc_grid* g, const kv* tab, int nt, int chan_d, int chan_v, int vx, int vy, int vz,
                         double wgt, const double* u)
 {
     if (vx < 0 || vy < 0 || vz < 0) return;
+    int b = g->brick, a = g->apron;
+    int c0[3] = {vx / b, vy / b, vz / b};
+    for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                int k[3] = {c0[0] + dx, c0[1] + dy, c0[2] + dz};
+                if (k[0] < 0 || k[1] < 0 || k[2] < 0) continue;
+                int lx = vx - k[0] * b, ly = vy - k[1] * b, lz = vz - k[2] * b;
+                if (lx < -a || ly < -a || lz < -a || lx >= b + a || ly >= b + a || lz >= b + a) continue;
+                int li = find_leaf(tab, nt, leaf_key(k[0], k[1], k[2]));
+                if (li < 0) continue;
+                orc_node* nd = &g->pools[0].nodes[li];
+                if (chan_d >= 0) *vox_ptr(g, chan_d, nd->value, lx, ly, lz) += wgt;
+                if (chan_v >= 0 && u) {
+                    double* v = vox_ptr(g, chan_v, nd->value, lx, ly, lz);
+                    v[0] += wgt * u[0]; v[1] += wgt * u[1]; v[2] += wgt * u[2];
+                }
+            }
+}
+
+/* apron voxels whose world position lies in no active brick -> value */
+static void apron_unowned(orc_grid* g, const kv* tab, int nt, int chan, double value)
+{
+    if (chan < 0 || g->apron == 0) return;
+    pool* p0 = &g->pools[0];
     int b = g->brick;
-    int li = find_leaf(tab, nt, leaf_key(vx / b, vy / b, vz / b));
-    if (li < 0) return;
-    orc_node* nd = &g->pools[0].nodes[li];
-    int lx = vx - nd->pos[0], ly = vy - nd->pos[1], lz = vz - nd->pos[2];
-    if (chan_d >= 0) *vox_ptr(g, chan_d, nd->value, lx, ly, lz) += wgt;
-    if (chan_v >= 0 && u) {
-        double* v = vox_ptr(g, chan_v, nd->value, lx, ly, lz);
-        v[0] += wgt * u[0]; v[1] += wgt * u[1]; v[2] += wgt * u[2];
+    for (int i = 0; i < p0->cnt; i++) {
+        orc_node* nd = &p0->nodes[i];
+        if (!nd->flags || nd->value[0] < 0) continue;
+        for (int z = -1; z <= b; z++)
+            for (int y = -1; y <= b; y++)
+                for (int x = -1; x <= b; x++) {
+                    if (x >= 0 && x < b && y >= 0 && y < b && z >= 0 && z < b) continue;
+                    int w[3] = {nd->pos[0] + x, nd->pos[1] + y, nd->pos[2] + z};
+                    int li = -1;
+                    if (w[0] >= 0 && w[1] >= 0 && w[2] >= 0)
+                        li = find_leaf(tab, nt, leaf_key(w[0] / b, w[1] / b, w[2] / b));
+                    if (li >= 0) continue;
+                    double* v = vox_ptr(g, chan, nd->value, x, y, z);
+                    for (int c = 0; c < g->ncomp[chan]; c++) v[c] = value;
+                }
     }
 }
 
@@ -893,6 +927,10 @@ static int splat_new(orc_grid* g, int mode, int n, const float* pos, int ps, con
         float wf[3];
         for (int a = 0; a < 3; a++) wf[a] = pos[(int64_t)i * ps + a] + tr[a];
         if (wf[0] < 0 || wf[1] < 0 || wf[2] < 0) continue;
+        /* only points inside an active brick are splatted */
+        if (find_leaf(tab, nt, leaf_key((int)floorf(wf[0]) / g->brick, (int)floorf(wf[1]) / g->brick,
+                                        (int)floorf(wf[2]) / g->brick)) < 0)
+            continue;
         double p[3] = {wf[0], wf[1], wf[2]};
         double w = weight ? (double)weight[i] : 1.0;
         double u[3] = {0, 0, 0};
@@ -924,6 +962,7 @@ static int splat_new(orc_grid* g, int mode, int n, const float* pos, int ps, con
                     }
         }
     }
+    if (!accum) { apron_unowned(g, tab, nt, chan_d, 0.0); apron_unowned(g, tab, nt, chan_v, 0.0); }
     free(tab);
     return ORC_OK;
 }

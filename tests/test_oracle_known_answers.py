@@ -78,10 +78,12 @@ def test_trilinear_known_values(orc):
     # leaf 1 = (296,200,96): voxels 300..301, 200..201, 100..101 -> local 4..5, 0..1, 4..5 (+1 apron)
     blk = d[1]
     assert np.allclose(blk[5:7, 1:3, 5:7], 0.25)
-    assert math.isclose(blk.sum(), 2.0)
+    assert math.isclose(blk[1:9, 1:9, 1:9].sum(), 2.0)
     # leaf 0: 10.5 -> voxels 10,11 -> local 2,3
     assert np.allclose(d[0][3:5, 3:5, 3:5], 0.125)
-    assert math.isclose(d.sum(), 3.0)
+    assert math.isclose(d[:, 1:9, 1:9, 1:9].sum(), 3.0)
+    # the extra leaf (296,192,96) holds the y=200 voxels as +y apron copies (padded y = 9)
+    assert np.array_equal(d[2][5:7, 9, 5:7], blk[5:7, 1, 5:7])
 
 
 def test_cubic_known_values(orc):
