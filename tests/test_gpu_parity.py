@@ -79,7 +79,8 @@ def test_trilinear_plain_small(gvx_mod, orc, c1):
     got, ref = g.read_channel(0), o.read_channel(0)
     assert got.shape == ref.shape
     assert rel_error(got, ref) <= DENSITY_TOL
-    assert abs(float(got.astype(np.float64).sum()) - float(w.sum())) <= 1e-5 * float(w.sum())
+    interior = got[:, 1:-1, 1:-1, 1:-1].astype(np.float64)  # aprons hold copies of neighbours
+    assert abs(float(interior.sum()) - float(w.sum())) <= 1e-5 * float(w.sum())
 
 
 def test_cubic_with_velocity(gvx_mod, orc):
