@@ -99,33 +99,50 @@ struct SplatArgs {
     uint32_t* err;
 };
 
-__device__ __forceinline__ void tile_add(float* tden, float4* tvel, int t, float wgt, float ux, float uy, float uz,
-                                         bool has_den, bool has_vel)
-{
-    if (has_den) tden[t] += wgt;
-    if (has_vel) {
-        float4 o = tvel[t];
-        o.x += wgt * ux;
-        o.y += wgt * uy;
-        o.z += wgt * uz;
-        tvel[t] = o;
+// Shared-memory tile of one padded brick.  Density only: float per voxel.
+// Velocity (with or without density): float4 per voxel (vx, vy, vz, density),
+// so a contribution is one 16-byte shared read-modify-write.
+template <bool HAS_DEN, bool HAS_VEL>
+struct Tile {
+    static constexpr bool VEC = HAS_VEL;
+    static __host__ __device__ size_t bytes(int P3) { return (size_t)P3 * (VEC ? 16 : 4); }
+    __device__ static void add(unsigned char* t, int i, float wgt, float ux, float uy, float uz)
+    {
+        if (VEC) {
+            float4* v = (float4*)t;
+            float4 o = v[i];
+            o.x += wgt * ux;
+            o.y += wgt * uy;
+            o.z += wgt * uz;
+            if (HAS_DEN) o.w += wgt;
+            v[i] = o;
+        } else {
+            ((float*)t)[i] += wgt;
+        }
     }
-}
+    __device__ static void set(unsigned char* t, int i, float val)
+    {
+        if (VEC)
+            ((float4*)t)[i] = make_float4(val, val, val, val);
+        else
+            ((float*)t)[i] = val;
+    }
+};
 
 template <bool HAS_DEN, bool HAS_VEL, int MODE>
 __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
 {
+    using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int P = a.P, P3 = P * P * P, ap = a.apron;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t vel_bytes = HAS_VEL ? (uint32_t)P3 * 16u : 0u;
-    const uint32_t den_bytes = HAS_DEN ? (uint32_t)P3 * 4u : 0u;
-    unsigned char* mytile = smem + (size_t)wid * (vel_bytes + den_bytes);
-    float4* tvel = (float4*)mytile;
-    float* tden = (float*)(mytile + vel_bytes);
+    unsigned char* tile = smem + (size_t)wid * T::bytes(P3);
     __shared__ __align__(8) uint64_t s_bar[kFusedWarps];
     __shared__ int s_rs[kFusedWarps][28];
     __shared__ int s_ro[kFusedWarps][28];
+    // single-channel tiles go to HBM in one bulk (TMA) store; the combined
+    // density+velocity tile is split into the two channels by vector stores
+    constexpr bool BULK = !(HAS_DEN && HAS_VEL);
 
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
@@ -171,18 +188,24 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
 
         // ---- tile: previous values (accumulate) or zeros
         if (a.accum) {
-            if (lane == 0) {
-                mbar_expect_tx(&s_bar[wid], vel_bytes + den_bytes);
-                if (HAS_DEN) bulk_g2s(tden, a.den + (size_t)s * P3, den_bytes, &s_bar[wid]);
-                if (HAS_VEL) bulk_g2s(tvel, a.vel + (size_t)s * P3, vel_bytes, &s_bar[wid]);
+            if (BULK) {
+                if (lane == 0) {
+                    const uint32_t nb = (uint32_t)T::bytes(P3);
+                    mbar_expect_tx(&s_bar[wid], nb);
+                    if (HAS_DEN) bulk_g2s(tile, a.den + (size_t)s * P3, nb, &s_bar[wid]);
+                    else bulk_g2s(tile, a.vel + (size_t)s * P3, nb, &s_bar[wid]);
+                }
+                if (!mbar_wait_bounded(&s_bar[wid], phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
+                phase ^= 1u;
+            } else {
+                float4* tv = (float4*)tile;
+                for (int i = lane; i < P3; i += 32) {
+                    const float4 v = a.vel[(size_t)s * P3 + i];
+                    tv[i] = make_float4(v.x, v.y, v.z, a.den[(size_t)s * P3 + i]);
+                }
             }
-            if (!mbar_wait_bounded(&s_bar[wid], phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
-            phase ^= 1u;
         } else {
-            for (int i = lane; i < P3; i += 32) {
-                if (HAS_DEN) tden[i] = 0.f;
-                if (HAS_VEL) tvel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
+            for (int i = lane; i < P3; i += 32) T::set(tile, i, 0.0f);
         }
         __syncwarp();
 
@@ -210,9 +233,11 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                     const int x0 = (int)floorf(p.x), y0 = (int)floorf(p.y), z0 = (int)floorf(p.z);
                     hit = x0 + 1 >= Ox && x0 < Ox + P && y0 + 1 >= Oy && y0 < Oy + P && z0 + 1 >= Oz && z0 < Oz + P;
                 } else {
+                    // voxels strictly inside (p - R, p + R) on every axis
                     const float R = a.per_point_radius ? u.w : a.radius;
-                    hit = (int)ceilf(p.x + R) >= Ox && (int)floorf(p.x - R) < Ox + P && (int)ceilf(p.y + R) >= Oy &&
-                          (int)floorf(p.y - R) < Oy + P && (int)ceilf(p.z + R) >= Oz && (int)floorf(p.z - R) < Oz + P;
+                    hit = (int)ceilf(p.x + R) - 1 >= Ox && (int)floorf(p.x - R) + 1 < Ox + P &&
+                          (int)ceilf(p.y + R) - 1 >= Oy && (int)floorf(p.y - R) + 1 < Oy + P &&
+                          (int)ceilf(p.z + R) - 1 >= Oz && (int)floorf(p.z - R) + 1 < Oz + P;
                 }
             }
             uint32_t hm = __ballot_sync(kFull, hit);
@@ -236,7 +261,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                             const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
                             const float wgt =
                                 pw * (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
-                            tile_add(tden, tvel, (lz * P + ly) * P + lx, wgt, ux, uy, uz, HAS_DEN, HAS_VEL);
+                            T::add(tile, (lz * P + ly) * P + lx, wgt, ux, uy, uz);
                         }
                     }
                 } else {
@@ -249,9 +274,9 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                     const float h = 0.5f * R, inv_h = 1.0f / h;
                     const float norm = kInvPi * inv_h * inv_h * inv_h * pw;
                     const float r2h = R * R, r2l = fmaf(R, R, -r2h);
-                    const int xl = max((int)floorf(px - R), Ox), xh = min((int)ceilf(px + R), Ox + P - 1);
-                    const int yl = max((int)floorf(py - R), Oy), yh = min((int)ceilf(py + R), Oy + P - 1);
-                    const int zl = max((int)floorf(pz - R), Oz), zh = min((int)ceilf(pz + R), Oz + P - 1);
+                    const int xl = max((int)floorf(px - R) + 1, Ox), xh = min((int)ceilf(px + R) - 1, Ox + P - 1);
+                    const int yl = max((int)floorf(py - R) + 1, Oy), yh = min((int)ceilf(py + R) - 1, Oy + P - 1);
+                    const int zl = max((int)floorf(pz - R) + 1, Oz), zh = min((int)ceilf(pz + R) - 1, Oz + P - 1);
                     const int ny = yh - yl + 1, nz = zh - zl + 1;
                     for (int r = lane; r < ny * nz; r += 32) {
                         const int y = yl + r % ny, z = zl + r / ny;
@@ -280,7 +305,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                                 const float uu = t / (h * (R + d));  // 2 - q
                                 wm = 0.25f * uu * uu * uu;
                             }
-                            tile_add(tden, tvel, t0 + x, norm * wm, ux, uy, uz, HAS_DEN, HAS_VEL);
+                            T::add(tile, t0 + x, norm * wm, ux, uy, uz);
                         }
                     }
                 }
@@ -288,8 +313,8 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
             }
         }
 
-        // ---- apron voxels with no neighbouring brick take the boundary value
-        if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu) {
+        // ---- apron voxels with no neighbouring brick take the boundary value (0)
+        if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
             const int napron = 6 * P * P - 12 * P + 8;
             for (int e = lane; e < napron; e += 32) {
                 int x, y, z;
@@ -298,25 +323,35 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                 const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
                 const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
                 if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
-                const int t = (z * P + y) * P + x;
-                if (HAS_DEN) tden[t] = a.boundval;
-                if (HAS_VEL) tvel[t] = make_float4(a.boundval, a.boundval, a.boundval, a.boundval);
+                T::set(tile, (z * P + y) * P + x, a.boundval);
             }
             __syncwarp();
         }
 
-        // ---- one bulk store per channel
-        fence_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-            if (HAS_DEN) bulk_s2g(a.den + (size_t)s * P3, tden, den_bytes);
-            if (HAS_VEL) bulk_s2g(a.vel + (size_t)s * P3, tvel, vel_bytes);
-            bulk_commit();
-            bulk_wait_read_all();
+        // ---- out to HBM
+        if (BULK) {
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                if (HAS_DEN) bulk_s2g(a.den + (size_t)s * P3, tile, (uint32_t)T::bytes(P3));
+                else bulk_s2g(a.vel + (size_t)s * P3, tile, (uint32_t)T::bytes(P3));
+                bulk_commit();
+                bulk_wait_read_all();
+            }
+            __syncwarp();
+        } else {
+            const float4* tv = (const float4*)tile;
+            float* dg = a.den + (size_t)s * P3;
+            float4* vg = a.vel + (size_t)s * P3;
+            for (int i = lane; i < P3; i += 32) {
+                const float4 o = tv[i];
+                dg[i] = o.w;
+                vg[i] = make_float4(o.x, o.y, o.z, 0.0f);
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
-    if (lane == 0) bulk_wait_all();
+    if (BULK && lane == 0) bulk_wait_all();
 }
 
 // ScatterDensity, race-free: own points only, into the own padded tile
@@ -487,7 +522,7 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     if (rc) return rc;
 
     const int P = g->P, P3 = P * P * P;
-    const size_t tile = (has_v ? (size_t)P3 * 16 : 0) + (has_d ? (size_t)P3 * 4 : 0);
+    const size_t tile = has_v ? (size_t)P3 * 16 : (size_t)P3 * 4;
     const size_t smem = tile * kFusedWarps;
     if (smem > 220 * 1024) {
         gvx_set_error("Splat: %d warps of %d^3 padded bricks need %zu bytes of shared memory", kFusedWarps, P, smem);

@@ -787,6 +787,13 @@ int orc_read_channel(const orc_grid* g, int chan, double* out, int64_t cap)
     memcpy(out, g->ch[chan], (size_t)n * sizeof(double));
     return ORC_OK;
 }
+int orc_write_channel(orc_grid* g, int chan, const double* in, int64_t count)
+{
+    int64_t n = orc_channel_size(g, chan);
+    if (n < 0 || count != n) return ORC_ERR_ARG;
+    memcpy(g->ch[chan], in, (size_t)n * sizeof(double));
+    return ORC_OK;
+}
 
 /* ------------------------------------------------------------------ */
 /* splats */

@@ -108,6 +108,7 @@ int orc_update_apron(orc_grid* g, int chan, double boundval);
  *   out[((s*P + lz)*P + ly)*P + lx)*ncomp + c],  P = brick + 2*apron */
 int64_t orc_channel_size(const orc_grid* g, int chan);   /* number of doubles */
 int orc_read_channel(const orc_grid* g, int chan, double* out, int64_t cap);
+int orc_write_channel(orc_grid* g, int chan, const double* in, int64_t count);
 
 /* host CPU topology (VG.cpp:2766-2855): ActivateSpace for every point, root
  * grows through Reparent.  Returns the number of leaves, or -1. */

@@ -56,7 +56,7 @@ def load():
         "orc_atlas_subdim": ([vp, vp], i), "orc_get_atlas_map": ([vp, vp, i], i),
         "orc_splat": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, i, i, i, i, i, f], i),
         "orc_update_apron": ([vp, i, d], i), "orc_channel_size": ([vp, i], i64),
-        "orc_read_channel": ([vp, i, vp, i64], i),
+        "orc_read_channel": ([vp, i, vp, i64], i), "orc_write_channel": ([vp, i, vp, i64], i),
         "orc_activate_space_cpu": ([i, vp, i, vp, i, vp, vp, i, vp], i),
         "orc_now_seconds": ([], d),
     }
@@ -177,6 +177,10 @@ class Oracle:
 
     def update_apron(self, chan, boundval=0.0):
         self._ck(self.lib.orc_update_apron(self.h, chan, float(boundval)), "update_apron")
+
+    def write_channel(self, chan, data):
+        data = np.ascontiguousarray(data, np.float64).ravel()
+        self._ck(self.lib.orc_write_channel(self.h, chan, _p(data), data.size), "write_channel")
 
     def read_channel(self, chan):
         n = self.lib.orc_channel_size(self.h, chan)
