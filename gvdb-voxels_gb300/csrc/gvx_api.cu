@@ -173,7 +173,8 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->own_r, &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
-                      &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->sc_tmp};
+                      &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->sc_tmp, &g->api_keys[0],
+                      &g->api_keys[1], &g->api_vals[0], &g->api_vals[1]};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -514,6 +515,38 @@ gvx_status gvx_update_apron_all(gvx_grid* g)
         gvx_status rc = update_apron_one(g, c, 0.0f);
         if (rc) return rc;
     }
+    return GVX_OK;
+}
+
+gvx_status gvx_radix_sort(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                          uint32_t* vals_out, uint32_t n, int bits)
+{
+    GVX_GUARD(g);
+    if (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out)) {
+        gvx_set_error("RadixSortByByte: null buffer");
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (bits < 1 || bits > 32) {
+        gvx_set_error("RadixSortByByte: bits must be 1..32, got %d", bits);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (n == 0) return GVX_OK;
+    for (int k = 0; k < 2; k++) {
+        GVX_CK(gvx_ensure(g->api_keys[k], (size_t)n * 4));
+        GVX_CK(gvx_ensure(g->api_vals[k], (size_t)n * 4));
+    }
+    GVX_CK(gvx_ensure(g->d_err, 64));
+    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));
+    GVX_CK(cudaMemcpyAsync(g->api_keys[0].p, keys_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, g->stream));
+    GVX_CK(cudaMemcpyAsync(g->api_vals[0].p, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, g->stream));
+    uint32_t* kk[2] = {g->api_keys[0].as<uint32_t>(), g->api_keys[1].as<uint32_t>()};
+    uint32_t* vv[2] = {g->api_vals[0].as<uint32_t>(), g->api_vals[1].as<uint32_t>()};
+    int res = 0;
+    gvx_status rc = gvx_sort_pairs(kk, vv, n, bits, g->sort, false, g->stream, g->d_err.as<uint32_t>(), &res,
+                                   &g->launches);
+    if (rc) return rc;
+    GVX_CK(cudaMemcpyAsync(keys_out, kk[res], (size_t)n * 4, cudaMemcpyDeviceToDevice, g->stream));
+    GVX_CK(cudaMemcpyAsync(vals_out, vv[res], (size_t)n * 4, cudaMemcpyDeviceToDevice, g->stream));
     return GVX_OK;
 }
 

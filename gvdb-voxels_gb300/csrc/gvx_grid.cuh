@@ -131,6 +131,9 @@ struct gvx_grid {
     // scratch of the gathers
     DevBuf sc_tmp;
 
+    // scratch of gvx_radix_sort (kept apart from the topology's grouping)
+    DevBuf api_keys[2], api_vals[2];
+
     int64_t launches = 0;
 };
 

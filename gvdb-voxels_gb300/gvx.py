@@ -86,6 +86,7 @@ def load(path=None):
         "gvx_channel_device_ptr": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(i64)], i),
         "gvx_retrieve_brick": ([vp, i, ip, vp, i64], i),
         "gvx_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
+        "gvx_radix_sort": ([vp, vp, vp, vp, vp, ctypes.c_uint32, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -300,3 +301,9 @@ class Grid:
         c = ctypes.c_int64()
         self._check(self.lib.gvx_kernel_launches(self.h, ctypes.byref(c)))
         return c.value
+
+
+def radix_sort(grid, keys_in, vals_in, keys_out, vals_out, n, bits):
+    """gvx_radix_sort on device buffers (torch tensors or raw pointers)"""
+    grid._check(grid.lib.gvx_radix_sort(grid.h, _ptr(keys_in), _ptr(vals_in), _ptr(keys_out), _ptr(vals_out),
+                                        int(n), int(bits)))

@@ -164,6 +164,14 @@ gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float tra
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
 gvx_status gvx_update_apron_all(gvx_grid* g);
 
+/* RadixSortByByte (VG.h:423, VG.cpp:904-928): stable ascending sort of n
+ * (key, value) pairs by the low `bits` (1..32) bits of 32-bit keys -- the
+ * onesweep radix sort the topology uses for brick keys.  Device pointers; the
+ * inputs are not modified; the grid owns the scratch memory (allocated on
+ * first use, kept for later calls).  Stream-ordered on the grid's stream. */
+gvx_status gvx_radix_sort(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                          uint32_t* vals_out, uint32_t n, int bits);
+
 /* queries: getNumTotalNodes/getNumUsedNodes (VG.h:637-643), getBoundMin/Max */
 gvx_status gvx_get_info(gvx_grid* g, gvx_info* out);
 /* node pool of one level as 64-byte Node records (host memory) */

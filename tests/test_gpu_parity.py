@@ -279,3 +279,21 @@ def test_apron_kernel_matches_fused_copies(gvx_mod, orc, c1):
     g.update_apron(0, 0.25)  # different boundary value: the apron kernel runs
     g.update_apron(0, 0.0)   # and back: must reproduce the splat's apron exactly
     assert g.read_channel(0).tobytes() == fused.tobytes()
+
+
+def test_radix_sort_entry_point(gvx_mod):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(13)
+    for n, bits in ((1, 8), (4095, 12), (200_003, 21), (65_536, 32)):
+        keys = rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+        vals = np.arange(n, dtype=np.uint32)
+        kd = torch.from_numpy(keys.view(np.int32)).cuda()
+        vd = torch.from_numpy(vals.view(np.int32)).cuda()
+        ko, vo = torch.empty_like(kd), torch.empty_like(vd)
+        g = gvx_mod.Grid(0)
+        gvx_mod.radix_sort(g, kd, vd, ko, vo, n, bits)
+        g.sync()
+        order = np.argsort(keys, kind="stable")
+        assert np.array_equal(ko.cpu().numpy().view(np.uint32), keys[order])
+        assert np.array_equal(vo.cpu().numpy().view(np.uint32), vals[order])
+        g.close()
