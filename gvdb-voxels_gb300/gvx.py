@@ -87,6 +87,7 @@ def load(path=None):
         "gvx_retrieve_brick": ([vp, i, ip, vp, i64], i),
         "gvx_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
         "gvx_radix_sort": ([vp, vp, vp, vp, vp, ctypes.c_uint32, i], i),
+        "gvx_radix_sort_noalloc": ([vp, vp, vp, vp, ctypes.c_uint32, i, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

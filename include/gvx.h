@@ -172,6 +172,21 @@ gvx_status gvx_update_apron_all(gvx_grid* g);
 gvx_status gvx_radix_sort(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                           uint32_t* vals_out, uint32_t n, int bits);
 
+/* gvx_radix_sort without any device allocation -- no counterpart in the
+ * reference.  For callers that must not allocate device memory (a host that
+ * hands the library a fixed memory budget, a plugin whose host owns all
+ * device allocations): same result as gvx_radix_sort, but the scratch lives in
+ * a static __device__ array inside libgvx, so the call allocates nothing.
+ * At most GVX_NOALLOC_SORT_MAX_KEYS pairs (larger n -> GVX_ERR_CAPACITY); the
+ * array (about 2.4 MB) stays resident on every GPU that loads the library;
+ * calls share it, so calls that overlap on the GPU race -- order them on one
+ * stream.  Runs on the current device and the given stream (NULL = legacy
+ * default stream); its first call on a device looks up the array's address,
+ * so make that first call before any stream capture. */
+#define GVX_NOALLOC_SORT_MAX_KEYS (1u << 18)
+gvx_status gvx_radix_sort_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                                  uint32_t* vals_out, uint32_t n, int bits, void* stream);
+
 /* queries: getNumTotalNodes/getNumUsedNodes (VG.h:637-643), getBoundMin/Max */
 gvx_status gvx_get_info(gvx_grid* g, gvx_info* out);
 /* node pool of one level as 64-byte Node records (host memory) */
