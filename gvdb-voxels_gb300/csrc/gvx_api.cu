@@ -174,7 +174,8 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
                       &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->sc_tmp, &g->api_keys[0],
-                      &g->api_keys[1], &g->api_vals[0], &g->api_vals[1]};
+                      &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
+                      &g->inc0, &g->inc_remap};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);

@@ -84,8 +84,8 @@ struct gvx_grid {
     // lookup of leaves by key for the current topology
     LeafLookup lookup{};
     bool lookup_valid = false;
-    DevBuf bm_a, bm_a_prefix, bm_b, bm_b_prefix;  // level-0 bitmaps backing `lookup`
-    DevBuf remap;
+    DevBuf bm_a, bm_a_prefix, bm_b, bm_b_prefix;  // active-leaf bitmap of UpdateAtlas
+    DevBuf lk_bits, lk_prefix, remap;             // active-leaf bitmap + rank -> pool index after an incremental build
 
     // per-leaf data
     DevBuf leaf_key;     // compact level-0 key per leaf (pool order)
@@ -125,6 +125,7 @@ struct gvx_grid {
 
     // scratch of the topology build
     DevBuf d0_bits, d0_prefix, x0_bits, x0_prefix, masks, upper, lists, tmp_scan, d_counts;
+    DevBuf inc0, inc_remap;  // incremental build: linked + new level-0 bitmaps, linked rank -> pool index
     DevBuf d_err, d_bbox;
     DevBuf host_stage;  // pinned staging of small readbacks
 

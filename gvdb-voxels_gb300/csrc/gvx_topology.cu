@@ -148,9 +148,10 @@ __global__ void k_mark_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint
 // dilation mask of every direct leaf: OR over its points of the leaves touched
 // by the box [int(p)-r, int(p)+2r] (cuda_gvdb_particles.cuh:481-482), encoded
 // as 27 bits (dz+1)*9 + (dy+1)*3 + (dx+1)
+// (hi_mul = 2 for the full rebuild's box, 1 for the incremental box [int(p)-r, int(p)+r], PT.cuh:433-434)
 __global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t n,
                               uint32_t invalid_key, BitRank d0, const char* pos, int off, int stride, float ox,
-                              float oy, float oz, float radius, int brick, uint32_t* masks)
+                              float oy, float oz, float radius, float hi_mul, int brick, uint32_t* masks)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
@@ -170,7 +171,7 @@ __global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t
         for (int a = 0; a < 3; a++) {
             const int ip = (int)w[a];
             const int bmin = (int)((float)ip - radius);
-            const int bmax = (int)((float)ip + 2.0f * radius);
+            const int bmax = (int)((float)ip + hi_mul * radius);
             const int cl = ip / brick;
             lo[a] = bmin / brick - cl;  // C truncation, as bmin/rres*rres
             hi[a] = bmax / brick - cl;
@@ -517,14 +518,21 @@ __global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uin
     if (last) leaf_range[leaf].y = (int)(i + 1);
 }
 
-// 27-neighbourhood of every leaf (leaf pool indices, -1 where no leaf)
+// 27-neighbourhood of every leaf (leaf pool indices, -1 where no leaf; all -1
+// for an inactive leaf, whose key is kNoKey)
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
 __global__ void k_neighbors(const uint32_t* __restrict__ leaf_key, uint32_t nleaves, LeafLookup L, int* nbr)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nleaves * 27u) return;
     const uint32_t leaf = t / 27u, d = t % 27u;
+    const uint32_t key = leaf_key[leaf];
+    if (key == kNoKey) {
+        nbr[t] = -1;
+        return;
+    }
     int c[3];
-    ks_unpack(L.ks, leaf_key[leaf], 0, c);
+    ks_unpack(L.ks, key, 0, c);
     nbr[t] = ll_find(L, c[0] + (int)(d % 3u) - 1, c[1] + (int)((d / 3u) % 3u) - 1, c[2] + (int)(d / 9u) - 1);
 }
 
@@ -577,6 +585,239 @@ __global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int
         atomicMin(&out[a], nodes[i].pos[a]);
         atomicMax(&out[3 + a], nodes[i].pos[a] + range);
     }
+}
+
+// ---------------------------------------------------------------------------
+// incremental rebuild: ActivateIncreBricksGPU (VG.cpp:1020-1156),
+// gvdbCalcIncreBrickId / gvdbCalcIncreExtraBrickId (PT.cuh:384-465),
+// gvdbLinkBricks (ND.cuh:470-505), gvdbDelinkLeafBricks / gvdbDelinkBricks
+// (ND.cuh:401-467).
+//
+// In the reference a node is reachable by a root descent exactly when its
+// parent reference is set: delinking clears the slot in the parent's child
+// list and writes ID_UNDEF64 into the node, and only reachable nodes gain
+// children.  The descents therefore become bitmap tests over one compact key
+// space: L_l = linked level-l nodes, T_l = nodes the points' boxes touch,
+// N_l = T_l & ~L_l = the nodes the reference allocates, in key order.
+
+enum { kSetLinked = 0, kSetActive = 1 };
+
+__device__ __forceinline__ bool node_key(const GvxNode& nd, const KeySpace& ks, int t, int range, uint32_t* key)
+{
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        c[a] = nd.pos[a] / range - (ks.lo[a] >> t);
+        if (c[a] < 0 || c[a] >= ks_extent(ks, a, t)) return false;
+    }
+    *key = ks_pack(ks, c[0], c[1], c[2], t);
+    return true;
+}
+
+__device__ __forceinline__ bool in_node_set(const GvxNode& nd, int set)
+{
+    return set == kSetActive ? nd.flags != 0 : nd.parent != ID_UNDEF64_U64;
+}
+
+// bitmap of a level's linked (or active) nodes; linked nodes outside the key
+// space cannot be touched and are left out, an active leaf outside it is an error
+__global__ void k_node_bits(const GvxNode* __restrict__ nodes, uint32_t n, KeySpace ks, int t, int range, int set,
+                            uint32_t* bits, uint32_t* err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GvxNode nd = nodes[i];
+    if (!in_node_set(nd, set)) return;
+    uint32_t key;
+    if (node_key(nd, ks, t, range, &key))
+        atomicOr(&bits[key >> 5], 1u << (key & 31));
+    else if (set == kSetActive)
+        atomicOr(err, GVX_DERR_DEGENERATE);
+}
+
+// rank in the set's bitmap -> pool index; with `leaf_key`, also the compact key
+// of every leaf (kNoKey where the leaf is not in the set)
+__global__ void k_node_remap(const GvxNode* __restrict__ nodes, uint32_t n, KeySpace ks, int t, int range, int set,
+                             BitRank br, int* remap, uint32_t* leaf_key)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GvxNode nd = nodes[i];
+    uint32_t key = kNoKey;
+    if (in_node_set(nd, set) && node_key(nd, ks, t, range, &key))
+        remap[br_rank(br, key)] = (int)i;
+    else
+        key = kNoKey;
+    if (leaf_key) leaf_key[i] = key;
+}
+
+// N = (D | A) & ~L: touched (by a point, or by a point's box) and not linked
+__global__ void k_new_bits(const uint32_t* __restrict__ D, const uint32_t* __restrict__ A,
+                           const uint32_t* __restrict__ L, uint32_t* N, uint32_t words)
+{
+    const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < words) N[w] = (D[w] | A[w]) & ~L[w];
+}
+
+// markers of the existing leaves (VG.cpp:1028-1043, 1078-1085): a linked leaf
+// inside some point's box gets 1, every other leaf keeps its flag
+// (AccumulateTopology) or gets 0
+__global__ void k_apply_markers(GvxNode* nodes, uint32_t n, KeySpace ks, int range, const uint32_t* __restrict__ d0,
+                                const uint32_t* __restrict__ x0, int accum)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GvxNode nd = nodes[i];
+    uint8_t m = accum ? nd.flags : 0;
+    uint32_t key;
+    if (nd.parent != ID_UNDEF64_U64 && node_key(nd, ks, 0, range, &key) &&
+        (((d0[key >> 5] | x0[key >> 5]) >> (key & 31)) & 1u))
+        m = 1;
+    nodes[i].flags = m;
+}
+
+struct IncNodeArgs {
+    int lev;
+    uint32_t count;        // new nodes of this level
+    uint32_t base;         // pool index of the first one (the old pool size)
+    const uint32_t* keys;  // their compact keys, sorted
+    KeySpace ks;
+    int tshift, range;
+    int lo[3];             // absolute level-l coordinates of compact (0,0,0)
+    GvxNode* nodes;
+    int parent_root;       // the parent level is the root's
+    int root_rel[3];       // root position in level-l node units
+    BitRank pl;            // linked parents, with their pool indices in premap
+    const int* premap;
+    BitRank pn;            // new parents (bits null when the parent level gets none)
+    uint32_t pbase;        // pool index of the first new parent
+    int logdim_parent, res_parent, tshift_parent;
+    uint64_t* pclist;
+    uint32_t* err;
+};
+
+// one new node per thread: SetupNode (VG.cpp:2512-2524) and its link
+// (gvdbLinkBricks); the parent is a linked node or a new one of this build
+__global__ void k_inc_write_nodes(IncNodeArgs a)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.count) return;
+    const uint32_t i = a.base + j;
+    int c[3];
+    ks_unpack(a.ks, a.keys[j], a.tshift, c);
+    GvxNode nd;
+    nd.lev = (uint8_t)a.lev;
+    nd.flags = 1;
+    nd.prio = 0;
+    nd.pad = 0;
+    for (int k = 0; k < 3; k++) {
+        nd.pos[k] = (a.lo[k] + c[k]) * a.range;
+        nd.value[k] = -1;
+        nd.vrange[k] = 0.f;
+    }
+    nd.mask = 0ull;
+    nd.childlist = a.lev > 0 ? (1ull | ((uint64_t)a.lev << 8) | ((uint64_t)i << 16)) : ID_UNDEFL_U64;
+    const int res = a.res_parent;
+    uint32_t pidx = 0u;
+    int rel[3];
+    bool ok = true;
+    if (a.parent_root) {
+        for (int k = 0; k < 3; k++) {
+            rel[k] = a.lo[k] + c[k] - a.root_rel[k];
+            if (rel[k] < 0 || rel[k] >= res) ok = false;
+        }
+    } else {
+        const int sh = a.logdim_parent;
+        const uint32_t pk = ks_pack(a.ks, c[0] >> sh, c[1] >> sh, c[2] >> sh, a.tshift_parent);
+        if (br_test(a.pl, pk))
+            pidx = (uint32_t)a.premap[br_rank(a.pl, pk)];
+        else if (a.pn.bits && br_test(a.pn, pk))
+            pidx = a.pbase + br_rank(a.pn, pk);
+        else
+            ok = false;
+        for (int k = 0; k < 3; k++) rel[k] = c[k] & (res - 1);
+    }
+    if (ok) {
+        nd.parent = ((uint64_t)pidx << 16) | ((uint64_t)(a.lev + 1) << 8);
+        const int bit = (rel[2] * res + rel[1]) * res + rel[0];
+        a.pclist[(size_t)pidx * res * res * res + bit] = ((uint64_t)i << 16) | ((uint64_t)a.lev << 8);
+    } else {
+        nd.parent = ID_UNDEFL_U64;  // no parent to link to: the reference's descent fails here
+        atomicOr(a.err, GVX_DERR_DEGENERATE);
+    }
+    a.nodes[i] = nd;
+}
+
+// clear node i's slot in its parent's child list and its parent reference
+__device__ void unlink_node(GvxNode* nodes, uint32_t i, const GvxNode& nd, const GvxNode* __restrict__ pnodes,
+                            uint32_t pcount, uint64_t* pclist, int res_p, int range, uint32_t* err)
+{
+    const uint64_t pid = nd.parent >> 16;
+    if (pid >= pcount) {
+        atomicOr(err, GVX_DERR_DEGENERATE);
+        return;
+    }
+    const GvxNode& pn = pnodes[pid];
+    int b[3];
+    for (int a = 0; a < 3; a++) {
+        const int d = nd.pos[a] - pn.pos[a];
+        b[a] = d / range;
+        if (d < 0 || b[a] >= res_p) {
+            atomicOr(err, GVX_DERR_DEGENERATE);
+            return;
+        }
+    }
+    const uint64_t cl = pn.childlist >> 16;  // == pid: lists are allocated in lockstep with the nodes
+    if (cl >= pcount) {
+        atomicOr(err, GVX_DERR_DEGENERATE);
+        return;
+    }
+    const size_t vc = (size_t)res_p * res_p * res_p;
+    pclist[(size_t)cl * vc + (b[2] * res_p + b[1]) * res_p + b[0]] = ID_UNDEF64_U64;
+    nodes[i].parent = ID_UNDEF64_U64;
+}
+
+// gvdbDelinkLeafBricks (ND.cuh:401-428): unmarked leaves leave the tree
+__global__ void k_delink_leaves(GvxNode* nodes, uint32_t n, const GvxNode* __restrict__ pnodes, uint32_t pcount,
+                                uint64_t* pclist, int res_p, int range, uint32_t* err)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GvxNode nd = nodes[i];
+    if (nd.flags || nd.parent == ID_UNDEF64_U64) return;
+    unlink_node(nodes, i, nd, pnodes, pcount, pclist, res_p, range, err);
+}
+
+// gvdbDelinkBricks (ND.cuh:430-467) for one level, one warp per node: a linked
+// node with any child stays active, a childless one leaves the tree
+__global__ void k_delink_upper(GvxNode* nodes, uint32_t n, const uint64_t* __restrict__ clist, uint32_t vc,
+                               const GvxNode* __restrict__ pnodes, uint32_t pcount, uint64_t* pclist, int res_p,
+                               int range, uint32_t* err)
+{
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;  // warp-uniform
+    const GvxNode nd = nodes[i];
+    if (nd.parent == ID_UNDEF64_U64) {
+        if (lane == 0) nodes[i].flags = 0;
+        return;
+    }
+    const uint64_t* cl = clist + (size_t)i * vc;
+    bool any = false;
+    for (uint32_t s0 = 0; s0 < vc; s0 += 32u) {
+        const uint32_t s = s0 + (uint32_t)lane;
+        if (__any_sync(0xFFFFFFFFu, s < vc && cl[s] != ID_UNDEF64_U64)) {
+            any = true;
+            break;
+        }
+    }
+    if (lane != 0) return;
+    if (any) {
+        nodes[i].flags = 1;
+        return;
+    }
+    nodes[i].flags = 0;
+    unlink_node(nodes, i, nd, pnodes, pcount, pclist, res_p, range, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -756,7 +997,7 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
         GVX_CK(cudaMemsetAsync(g->masks.p, 0, (size_t)n * 4, st));
         k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
                                                           g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
-                                                          radius, b, g->masks.as<uint32_t>());
+                                                          radius, 2.0f, b, g->masks.as<uint32_t>());
         k_dilate<<<blocks_for(n, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks,
                                                      g->masks.as<uint32_t>(), d0, x0.bits, g->d_err.as<uint32_t>());
         g->launches += 2;
@@ -903,6 +1144,350 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
     return GVX_OK;
 }
 
+// slots of d_counts read back by the incremental build
+enum { kCntNew = 0, kCntD0 = 20, kCntActive = 48 };
+
+// grows a pool buffer keeping its first `keep` bytes (PoolAlloc "preserve
+// existing on expand", VG.cpp:1096)
+static gvx_status grow_keep(gvx_grid* g, DevBuf& b, size_t bytes, size_t keep)
+{
+    if (b.p && bytes <= b.cap) return GVX_OK;
+    DevBuf nb;
+    GVX_CK(gvx_ensure(nb, bytes));
+    cudaError_t e = cudaSuccess;
+    if (b.p && keep) e = cudaMemcpyAsync(nb.p, b.p, keep, cudaMemcpyDeviceToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) {
+        gvx_free(nb);
+        return gvx_cuda_fail(e, "pool growth");
+    }
+    gvx_free(b);
+    b = nb;
+    return GVX_OK;
+}
+
+// leaf lookup over the ACTIVE leaves in key space `ks` (bitmap + rank -> pool
+// index), the per-leaf keys, the neighbour table and the point ranges of the
+// grouping made in `ks`; with read_used, the active count becomes used_leaves
+static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t words0, bool read_used)
+{
+    cudaStream_t st = g->stream;
+    const uint32_t L0 = (uint32_t)g->count[0];
+    GVX_CK(gvx_ensure(g->lk_bits, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->lk_prefix, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->remap, (size_t)L0 * 4 + 4));
+    GVX_CK(gvx_ensure(g->leaf_key, (size_t)L0 * 4 + 4));
+    GVX_CK(cudaMemsetAsync(g->lk_bits.p, 0, (size_t)words0 * 4, st));
+    uint32_t* counts = g->d_counts.as<uint32_t>();
+    if (L0) {
+        k_node_bits<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), L0, ks, 0, g->range[0],
+                                                         kSetActive, g->lk_bits.as<uint32_t>(),
+                                                         g->d_err.as<uint32_t>());
+        g->launches++;
+    }
+    gvx_status rc = gvx_bitmap_prefix(g->lk_bits.as<uint32_t>(), g->lk_prefix.as<uint32_t>(), words0,
+                                      counts + kCntActive, g->tmp_scan, st, &g->launches);
+    if (rc) return rc;
+    const BitRank lk{g->lk_bits.as<uint32_t>(), g->lk_prefix.as<uint32_t>(), words0};
+    if (L0) {
+        k_node_remap<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), L0, ks, 0, g->range[0],
+                                                          kSetActive, lk, g->remap.as<int>(),
+                                                          g->leaf_key.as<uint32_t>());
+        g->launches++;
+    }
+    g->lookup.ks = ks;
+    g->lookup.a = lk;
+    g->lookup.b = BitRank{nullptr, nullptr, 0u};
+    g->lookup.b_offset = 0u;
+    g->lookup.remap = g->remap.as<int>();
+    g->lookup_valid = true;
+    GVX_CK(gvx_ensure(g->nbr, (size_t)std::max<uint32_t>(L0, 1u) * 27 * sizeof(int)));
+    if (L0) {
+        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), L0, g->lookup,
+                                                                        g->nbr.as<int>());
+        g->launches++;
+    }
+    g->nbr_valid = true;
+    rc = fill_leaf_ranges(g, L0);
+    if (rc) return rc;
+    if (read_used) {
+        uint32_t used = 0;
+        GVX_CK(cudaMemcpyAsync(&used, counts + kCntActive, 4, cudaMemcpyDeviceToHost, st));
+        GVX_CK(cudaStreamSynchronize(st));
+        g->used_leaves = used;
+    }
+    return gvx_check_device_error(g, "RebuildTopology");
+}
+
+// Incremental rebuild (ActivateIncreBricksGPU, VG.cpp:1020-1156) of the tree
+// rooted at g->root_level over levels 0..depth-1; AccumulateTopology
+// (VG.cpp:1158-1178) may pass a depth below the root's level.  act[6] is the
+// box of the active leaves (voxels, max exclusive; empty when min > max).
+static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float o[3], int depth, bool accum,
+                                   const float mn[3], const float mx[3], const int act[6])
+{
+    cudaStream_t st = g->stream;
+    const int b = g->brick, R = g->root_level;
+    if (g->count[0] == 0) return GVX_OK;  // no leaf: the reference returns at once (VG.cpp:1022)
+    if (radius > (float)(b - 1)) {
+        gvx_set_error("RebuildTopology: incremental radius %g exceeds brick-1 = %d (box beyond the 26 neighbours)",
+                      radius, b - 1);
+        return GVX_ERR_UNSUPPORTED;
+    }
+    if (depth > R) {
+        gvx_set_error("AccumulateTopology: points need %d levels, the tree's root is at level %d", depth + 1, R);
+        return GVX_ERR_DEPTH;
+    }
+    const int top = depth < R ? depth : depth - 1;  // highest level whose linked set is needed
+    uint32_t old[GVX_MAXLEV] = {};
+    for (int l = 0; l <= R; l++) old[l] = (uint32_t)g->count[l];
+
+    // ---- key space: the points' boxes and the active leaves, inside the root
+    KeySpace ks;
+    const int root_span = g->range[R] / b;
+    const int align = 1 << g->tshift[top];
+    int64_t total_bits = 0;
+    for (int a = 0; a < 3; a++) {
+        const int rl = g->root_pos[a] / b;
+        const float lo_v = mn[a] > 0.f ? mn[a] : 0.f;
+        int lo = (int)floorf((lo_v - radius - 2.0f) / (float)b);
+        int hi = mx[a] < 0.f ? rl : (int)floorf((mx[a] + radius + 2.0f) / (float)b);
+        if (act[a] < act[3 + a]) {
+            lo = std::min(lo, act[a] / b);
+            hi = std::max(hi, act[3 + a] / b - 1);
+        }
+        lo = std::max(lo, rl);
+        hi = std::min(hi, rl + root_span - 1);
+        if (hi < lo) hi = lo;
+        lo = rl + ((lo - rl) / align) * align;
+        ks.lo[a] = lo;
+        ks.bits[a] = ceil_log2((int64_t)hi - lo + 1);
+        total_bits += ks.bits[a];
+    }
+    if (total_bits > 30) {
+        gvx_set_error("RebuildTopology: points and active bricks span 2^%lld leaf cells; the key space holds 2^30",
+                      (long long)total_bits);
+        return GVX_ERR_UNSUPPORTED;
+    }
+    ks.total_bits = (int)total_bits;
+    const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << total_bits) / 32ull));
+    const uint32_t invalid_key = 1u << ks.total_bits;
+
+    // ---- scratch: D0 / X0 (touched level-0 cells), L0 / N0 (linked / new), upper levels
+    GVX_CK(gvx_ensure(g->d0_bits, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->d0_prefix, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->x0_bits, (size_t)words0 * 4));
+    GVX_CK(gvx_ensure(g->inc0, (size_t)words0 * 16));
+    GVX_CK(gvx_ensure(g->masks, (size_t)std::max(n, 1) * 4));
+    GVX_CK(gvx_ensure(g->lists, (size_t)std::max(n, 1) * 4));
+    GVX_CK(cudaMemsetAsync(g->d0_bits.p, 0, (size_t)words0 * 4, st));
+    GVX_CK(cudaMemsetAsync(g->x0_bits.p, 0, (size_t)words0 * 4, st));
+    GVX_CK(cudaMemsetAsync(g->inc0.p, 0, (size_t)words0 * 16, st));
+    GVX_CK(cudaMemsetAsync(g->d_counts.p, 0, 64 * sizeof(uint32_t), st));
+    // per upper level: D (touched via direct leaves), A (via box leaves), L bits, L prefix, N bits, N prefix
+    UpperDesc ud;
+    memset(&ud, 0, sizeof(ud));
+    ud.nlev = depth - 1;
+    uint32_t upper_words = 0;
+    for (int l = 1; l <= top; l++) {
+        ud.tshift[l] = g->tshift[l];
+        ud.words[l] = std::max<uint32_t>(1u, (uint32_t)((1ull << ks_bits_at(ks, g->tshift[l])) / 32ull));
+        ud.off[l] = upper_words;
+        upper_words += 6u * ud.words[l];
+    }
+    GVX_CK(gvx_ensure(g->upper, (size_t)std::max<uint32_t>(upper_words, 1u) * 4));
+    if (upper_words) GVX_CK(cudaMemsetAsync(g->upper.p, 0, (size_t)upper_words * 4, st));
+    uint32_t* upper = g->upper.as<uint32_t>();
+    uint32_t* counts = g->d_counts.as<uint32_t>();
+    uint32_t* err = g->d_err.as<uint32_t>();
+
+    // ---- touched cells: the points' leaves (D0) and their boxes [int(p)-r, int(p)+r] (X0), PT.cuh:420-465
+    gvx_status rc = sort_points(g, n, o, ks, true);
+    if (rc) return rc;
+    const uint32_t* skeys = g->keys[g->sorted_buf].as<uint32_t>();
+    const uint32_t* svals = g->vals[g->sorted_buf].as<uint32_t>();
+    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, invalid_key, g->d0_bits.as<uint32_t>());
+    g->launches++;
+    rc = gvx_bitmap_prefix(g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0, counts + kCntD0,
+                           g->tmp_scan, st, &g->launches);
+    if (rc) return rc;
+    const BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
+    uint32_t* dlist = g->lists.as<uint32_t>();
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, dlist);
+    g->launches++;
+    if (radius > 0.f) {
+        GVX_CK(cudaMemsetAsync(g->masks.p, 0, (size_t)n * 4, st));
+        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
+                                                          g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
+                                                          radius, 1.0f, b, g->masks.as<uint32_t>());
+        k_dilate<<<blocks_for(n, 256), 256, 0, st>>>(dlist, counts + kCntD0, ks, g->masks.as<uint32_t>(), d0,
+                                                     g->x0_bits.as<uint32_t>(), err);
+        g->launches += 2;
+    }
+    if (ud.nlev > 0) {
+        k_upper_direct<<<blocks_for(n, 256), 256, 0, st>>>(dlist, counts + kCntD0, ks, ud, upper);
+        k_upper_extra<<<blocks_for(words0, 256), 256, 0, st>>>(g->x0_bits.as<uint32_t>(), words0, ks, ud, upper);
+        g->launches += 2;
+    }
+
+    // ---- linked sets L_l with rank -> pool index, levels 0..top
+    size_t roff[GVX_MAXLEV] = {}, rtotal = 0;
+    for (int l = 0; l <= top; l++) {
+        roff[l] = rtotal;
+        rtotal += old[l];
+    }
+    GVX_CK(gvx_ensure(g->inc_remap, rtotal * 4 + 4));
+    BitRank Lb[GVX_MAXLEV] = {}, Nb[GVX_MAXLEV] = {};
+    for (int l = 0; l <= top; l++) {
+        uint32_t* base = l == 0 ? g->inc0.as<uint32_t>() : upper + ud.off[l] + 2u * ud.words[l];
+        const uint32_t w = l == 0 ? words0 : ud.words[l];
+        Lb[l] = BitRank{base, base + w, w};
+        Nb[l] = BitRank{base + 2u * w, base + 3u * w, w};
+        if (old[l]) {
+            k_node_bits<<<blocks_for(old[l], 256), 256, 0, st>>>(g->nodes[l].as<GvxNode>(), old[l], ks,
+                                                                 g->tshift[l], g->range[l], kSetLinked, Lb[l].bits,
+                                                                 err);
+            g->launches++;
+        }
+        rc = gvx_bitmap_prefix(Lb[l].bits, Lb[l].prefix, w, nullptr, g->tmp_scan, st, &g->launches);
+        if (rc) return rc;
+        if (old[l]) {
+            k_node_remap<<<blocks_for(old[l], 256), 256, 0, st>>>(g->nodes[l].as<GvxNode>(), old[l], ks,
+                                                                  g->tshift[l], g->range[l], kSetLinked, Lb[l],
+                                                                  g->inc_remap.as<int>() + roff[l], nullptr);
+            g->launches++;
+        }
+    }
+    // ---- new nodes N_l = T_l & ~L_l, levels 0..depth-1
+    for (int l = 0; l < depth; l++) {
+        const uint32_t* D = l == 0 ? d0.bits : upper + ud.off[l];
+        const uint32_t* A = l == 0 ? g->x0_bits.as<uint32_t>() : upper + ud.off[l] + ud.words[l];
+        k_new_bits<<<blocks_for(Nb[l].words, 256), 256, 0, st>>>(D, A, Lb[l].bits, Nb[l].bits, Nb[l].words);
+        g->launches++;
+        rc = gvx_bitmap_prefix(Nb[l].bits, Nb[l].prefix, Nb[l].words, counts + kCntNew + l, g->tmp_scan, st,
+                               &g->launches);
+        if (rc) return rc;
+    }
+    GVX_CK(cudaGetLastError());
+
+    // ---- new-node counts to the host
+    uint32_t hc[64];
+    GVX_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    GVX_CK(cudaStreamSynchronize(st));
+    rc = gvx_check_device_error(g, "RebuildTopology");
+    if (rc) return rc;
+    uint32_t nnew[GVX_MAXLEV] = {};
+    uint64_t total_new = 0;
+    for (int l = 0; l < depth; l++) {
+        nnew[l] = hc[kCntNew + l];
+        total_new += nnew[l];
+    }
+    g->group_valid = false;  // the grouping now follows `ks`
+    if (total_new == 0) {
+        // no new node: the reference returns before it applies the markers (VG.cpp:1066)
+        rc = build_active_lookup(g, ks, words0, false);
+        if (rc) return rc;
+        g->last_rebuild = 0;
+    } else {
+        k_apply_markers<<<blocks_for(old[0], 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), old[0], ks, g->range[0],
+                                                                 d0.bits, g->x0_bits.as<uint32_t>(), accum ? 1 : 0);
+        g->launches++;
+        // ---- pools grow, keeping their nodes and child lists; new lists start empty
+        for (int l = 0; l < depth; l++) {
+            if (!nnew[l]) continue;
+            const size_t cnt = (size_t)old[l] + nnew[l];
+            rc = grow_keep(g, g->nodes[l], cnt * sizeof(GvxNode), (size_t)old[l] * sizeof(GvxNode));
+            if (rc) return rc;
+            if (l > 0) {
+                const size_t vb = (size_t)g->res[l] * g->res[l] * g->res[l] * sizeof(uint64_t);
+                rc = grow_keep(g, g->clist[l], cnt * vb, (size_t)old[l] * vb);
+                if (rc) return rc;
+                GVX_CK(cudaMemsetAsync((char*)g->clist[l].p + (size_t)old[l] * vb, 0xFF, (size_t)nnew[l] * vb, st));
+            }
+        }
+        // ---- sorted keys of the new nodes
+        GVX_CK(gvx_ensure(g->lists, (size_t)(total_new + 1) * 4));
+        const uint32_t* nl[GVX_MAXLEV] = {};
+        uint32_t* lp = g->lists.as<uint32_t>();
+        for (int l = 0; l < depth; l++) {
+            if (!nnew[l]) continue;
+            k_select<<<blocks_for(Nb[l].words, 256), 256, 0, st>>>(Nb[l].bits, Nb[l].prefix, Nb[l].words, lp);
+            g->launches++;
+            nl[l] = lp;
+            lp += nnew[l];
+        }
+        // ---- new nodes and their links (gvdbLinkBricks top-down, VG.cpp:1121-1129)
+        for (int l = depth - 1; l >= 0; l--) {
+            if (!nnew[l]) continue;
+            IncNodeArgs a;
+            memset(&a, 0, sizeof(a));
+            a.lev = l;
+            a.count = nnew[l];
+            a.base = old[l];
+            a.keys = nl[l];
+            a.ks = ks;
+            a.tshift = g->tshift[l];
+            a.range = g->range[l];
+            for (int k = 0; k < 3; k++) {
+                a.lo[k] = ks.lo[k] >> g->tshift[l];
+                a.root_rel[k] = g->root_pos[k] / g->range[l];
+            }
+            a.nodes = g->nodes[l].as<GvxNode>();
+            a.parent_root = l + 1 == R;
+            if (!a.parent_root) {
+                a.pl = Lb[l + 1];
+                a.premap = g->inc_remap.as<int>() + roff[l + 1];
+                if (l + 1 < depth && nnew[l + 1]) a.pn = Nb[l + 1];
+                a.pbase = old[l + 1];
+            }
+            a.logdim_parent = g->logdim[l + 1];
+            a.res_parent = g->res[l + 1];
+            a.tshift_parent = g->tshift[l + 1];
+            a.pclist = g->clist[l + 1].as<uint64_t>();
+            a.err = err;
+            k_inc_write_nodes<<<blocks_for(nnew[l], 256), 256, 0, st>>>(a);
+            g->launches++;
+        }
+        for (int l = 0; l < depth; l++) g->count[l] = (int64_t)old[l] + nnew[l];
+        // ---- delink, bottom-up (VG.cpp:1131-1140)
+        const uint32_t L0 = (uint32_t)g->count[0];
+        k_delink_leaves<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), L0,
+                                                             g->nodes[1].as<GvxNode>(), (uint32_t)g->count[1],
+                                                             g->clist[1].as<uint64_t>(), g->res[1], g->range[0], err);
+        g->launches++;
+        for (int l = 1; l < depth; l++) {
+            const uint32_t cnt = (uint32_t)g->count[l];
+            const uint32_t vc = (uint32_t)(g->res[l] * g->res[l] * g->res[l]);
+            k_delink_upper<<<blocks_for((uint64_t)cnt * 32u, 256), 256, 0, st>>>(
+                g->nodes[l].as<GvxNode>(), cnt, g->clist[l].as<uint64_t>(), vc, g->nodes[l + 1].as<GvxNode>(),
+                (uint32_t)g->count[l + 1], g->clist[l + 1].as<uint64_t>(), g->res[l + 1], g->range[l], err);
+            g->launches++;
+        }
+        GVX_CK(cudaGetLastError());
+        rc = build_active_lookup(g, ks, words0, true);
+        if (rc) return rc;
+        g->atlas_valid = false;
+        g->last_rebuild = 2;
+    }
+    g->group_valid = true;
+    g->group_pos = g->pts.pos;
+    g->group_n = n;
+    for (int a = 0; a < 3; a++) g->group_trans[a] = o[a];
+    return GVX_OK;
+}
+
+// the incremental build checks its limits (UNSUPPORTED, DEPTH) before it
+// touches anything; any later failure leaves no usable tree
+static gvx_status incremental_status(gvx_grid* g, gvx_status rc)
+{
+    if (rc == GVX_OK || rc == GVX_ERR_UNSUPPORTED || rc == GVX_ERR_DEPTH) return rc;
+    g->rebuild_topo = true;
+    g->root_level = -1;
+    g->lookup_valid = false;
+    g->group_valid = false;
+    return rc;
+}
+
 gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
 {
     if (!g->configured) {
@@ -930,7 +1515,17 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     k_bbox<<<bb, 256, 0, st>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, o[0], o[1], o[2],
                                g->d_bbox.as<uint32_t>(), g->d_err.as<uint32_t>());
     g->launches++;
-    uint32_t hb[6];
+    // an incremental build also needs the box of the active leaves: same readback
+    const bool maybe_incremental = g->root_level >= 0 && !g->rebuild_topo && mode != GVX_TOPO_FULL;
+    int* act_dev = g->d_bbox.as<int>() + 8;
+    k_bounds_init<<<1, 32, 0, st>>>(act_dev);
+    g->launches++;
+    if (maybe_incremental && g->count[0] > 0) {
+        k_leaf_bounds<<<blocks_for(g->count[0], 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(),
+                                                                     (uint32_t)g->count[0], g->range[0], act_dev);
+        g->launches++;
+    }
+    uint32_t hb[14];
     GVX_CK(cudaMemcpyAsync(hb, g->d_bbox.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
     GVX_CK(cudaStreamSynchronize(st));
     rc = gvx_check_device_error(g, "GetBoundingBox");
@@ -958,9 +1553,17 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
             break;
         }
     }
+    int act[6];
+    memcpy(act, hb + 8, sizeof(act));
     if (mode == GVX_TOPO_ACCUMULATE && !g->rebuild_topo) {
-        gvx_set_error("AccumulateTopology on an existing topology: incremental rebuild is not available yet");
-        return GVX_ERR_UNSUPPORTED;
+        // AccumulateTopology (VG.cpp:1158-1178): depth raised to min_depth, no depth-change check
+        int d = depth;
+        if (d >= 0 && d < min_depth) d = min_depth;
+        if (d <= 0 || d >= g->levels) {
+            gvx_set_error("AccumulateTopology: depth %d outside 1..%d", d, g->levels - 1);
+            return GVX_ERR_DEPTH;
+        }
+        return incremental_status(g, topo_incremental(g, n, radius, o, d, true, mn, mx, act));
     }
     if (depth <= 0) {
         gvx_set_error(depth == 0 ? "RebuildTopology: point extents smaller than 1 brick"
@@ -977,10 +1580,7 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
         g->rebuild_topo = true;  // "Depth change in rebuild": Clear + full rebuild
         g->curr_depth = depth;
     }
-    if (!g->rebuild_topo) {
-        gvx_set_error("RebuildTopology: incremental rebuild is not available yet (use GVX_TOPO_FULL)");
-        return GVX_ERR_UNSUPPORTED;
-    }
+    if (!g->rebuild_topo) return incremental_status(g, topo_incremental(g, n, radius, o, depth, false, mn, mx, act));
     rc = topo_full(g, n, radius, o, depth, rootpos, mn, mx);
     if (rc) {
         g->root_level = -1;

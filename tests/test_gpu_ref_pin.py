@@ -81,10 +81,13 @@ def test_full_topology_other_configs(orc, logdim):
 
 
 @pytest.mark.parametrize("accumulate", [False, True])
-def test_incremental_frames_match_reference_kernels(orc, accumulate):
+def test_incremental_frames_match_reference_kernels(orc, gvx_mod, accumulate):
     pos = slab(30_000, 3)
     vel = np.random.default_rng(4).normal(0, 1, pos.shape).astype(np.float32)
     r, o = pair(orc)
+    g = gvx_mod.Grid(0)
+    g.configure((3, 3, 3, 3, 5))
+    g.add_channel(0, gvx_mod.T_FLOAT, 1)
     mode = 2 if accumulate else 0
     for frame in range(6):
         p = (pos + np.float32(2.0 * frame) * vel).astype(np.float32)
@@ -97,6 +100,11 @@ def test_incremental_frames_match_reference_kernels(orc, accumulate):
         r.update_atlas()
         o.update_atlas()
         same_pools(r, o, o.root_level() + 1)
+        g.commit_points_host(p)
+        g.rebuild_topology(len(p), 1.0, mode=mode)
+        g.update_atlas()
+        assert g.info()["last_rebuild"] == o.last_mode()
+        compare_topology(g, o)
 
 
 @pytest.mark.parametrize("typ", [3, 4])
