@@ -173,9 +173,10 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->own_r, &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
-                      &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->sc_tmp, &g->api_keys[0],
+                      &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->api_keys[0],
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
-                      &g->inc0, &g->inc_remap};
+                      &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
+                      &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -452,35 +453,22 @@ gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, cons
     return gvx_scatter_ref(g, n, radius, trans, expand);
 }
 
-gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
-                                     int* sc_len)
+gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int sc_len,
+                              int chan_density, int chan_clr, int accum)
 {
     GVX_GUARD(g);
-    (void)subcell;
-    (void)radius;
-    (void)sc_len;
-    gvx_status rc = gvx_topo_group_points(g, n, trans);
-    if (rc) return rc;
-    gvx_set_error("InsertPointsSubcell: not available yet");
-    return GVX_ERR_UNSUPPORTED;
+    (void)n;      // the lists of InsertPointsSubcell hold the points, as in the reference
+    (void)trans;  // (VG.cpp:5318-5344 passes neither to the kernel)
+    return gvx_gather_run(g, 0, subcell, radius, sc_len, chan_density, chan_clr, accum);
 }
 
-gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
-                              int chan_density, int accum)
+gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int sc_len,
+                               int chan_levelset, int chan_clr, int accum)
 {
     GVX_GUARD(g);
-    (void)subcell; (void)n; (void)radius; (void)trans; (void)chan_density; (void)accum;
-    gvx_set_error("GatherDensity: not available yet");
-    return GVX_ERR_UNSUPPORTED;
-}
-
-gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
-                               int chan_levelset, int accum)
-{
-    GVX_GUARD(g);
-    (void)subcell; (void)n; (void)radius; (void)trans; (void)chan_levelset; (void)accum;
-    gvx_set_error("GatherLevelSet: not available yet");
-    return GVX_ERR_UNSUPPORTED;
+    (void)n;
+    (void)trans;
+    return gvx_gather_run(g, 1, subcell, radius, sc_len, chan_levelset, chan_clr, accum);
 }
 
 gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_density,

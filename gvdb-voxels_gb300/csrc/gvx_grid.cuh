@@ -129,8 +129,16 @@ struct gvx_grid {
     DevBuf d_err, d_bbox;
     DevBuf host_stage;  // pinned staging of small readbacks
 
-    // scratch of the gathers
-    DevBuf sc_tmp;
+    // subcell lists of InsertPointsSubcell: entries sorted by subcell index
+    // (atlas slot * (b/s)^3 + local subcell), point order within a subcell
+    DevBuf sc_cnt, sc_off;          // per point: entry count, then its offset
+    DevBuf sc_keys[2], sc_vals[2];  // entries: subcell index, point index
+    DevBuf sc_pts;                  // float4 per entry: translated position, colour bits in .w
+    DevBuf sc_beg, sc_end;          // per subcell: [beg, end) in the entry arrays
+    int sc_size = 0;
+    uint32_t sc_len = 0, sc_nsub = 0;
+    bool sc_has_clr = false;
+    bool sc_valid = false;  // the lists match the current topology and atlas
 
     // scratch of gvx_radix_sort (kept apart from the topology's grouping)
     DevBuf api_keys[2], api_vals[2];
@@ -148,12 +156,12 @@ gvx_status gvx_topo_read_bounds(gvx_grid* g);
 gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel);
 gvx_status gvx_check_device_error(gvx_grid* g, const char* stage);
 
-// splats (gvx_splat.cu)
+// splats (gvx_splat.cu) and gathers (gvx_gather.cu)
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
                          int chan_v, int accum);
 gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand);
-gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, int n, float radius, float radius_ins,
-                          const float trans[3], int chan, int accum);
+gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, int sc_len, int chan, int chan_clr,
+                          int accum);
 
 // apron (gvx_apron.cu)
 gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval);

@@ -132,3 +132,6 @@ __device__ inline void gvx_sort_count_key(uint32_t* sh, uint32_t key, int passes
 // ---- generic exclusive scan of popcounts of a bitmap (gvx_topology.cu) -----
 gvx_status gvx_bitmap_prefix(const uint32_t* bits, uint32_t* prefix, uint32_t words, uint32_t* total,
                              DevBuf& tmp, cudaStream_t st, int64_t* launches);
+// exclusive scan of n uint32 values (in -> out, may not alias), total -> *total if non-null
+gvx_status gvx_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, DevBuf& tmp,
+                        cudaStream_t st, int64_t* launches);

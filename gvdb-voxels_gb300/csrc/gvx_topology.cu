@@ -314,13 +314,21 @@ constexpr int kPfxPerThread = 16;
 constexpr uint32_t kPfxChunk = kPfxThreads * kPfxPerThread;
 }  // namespace
 
+// POPC: the scanned values are the popcounts of bitmap words, else the words themselves
+template <bool POPC>
+__device__ __forceinline__ uint32_t pfx_value(uint32_t v)
+{
+    return POPC ? (uint32_t)__popc(v) : v;
+}
+
+template <bool POPC>
 __global__ void k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words, uint32_t* block_sums)
 {
     const uint32_t base = blockIdx.x * kPfxChunk;
     uint32_t s = 0u;
     for (uint32_t i = threadIdx.x; i < kPfxChunk; i += kPfxThreads) {
         const uint32_t w = base + i;
-        if (w < words) s += __popc(bits[w]);
+        if (w < words) s += pfx_value<POPC>(bits[w]);
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     __shared__ uint32_t ws[kPfxThreads / 32];
@@ -363,6 +371,7 @@ __global__ void k_pfx_top(uint32_t* block_sums, uint32_t nblocks, uint32_t* tota
     if (threadIdx.x == 0 && total) *total = s_carry;
 }
 
+template <bool POPC>
 __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, const uint32_t* __restrict__ block_off,
                             uint32_t* prefix)
 {
@@ -372,7 +381,7 @@ __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, c
 #pragma unroll
     for (int k = 0; k < kPfxPerThread; k++) {
         const uint32_t w = base + k;
-        cnt[k] = w < words ? __popc(bits[w]) : 0u;
+        cnt[k] = w < words ? pfx_value<POPC>(bits[w]) : 0u;
         s += cnt[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -394,17 +403,30 @@ __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, c
     }
 }
 
-gvx_status gvx_bitmap_prefix(const uint32_t* bits, uint32_t* prefix, uint32_t words, uint32_t* total, DevBuf& tmp,
-                             cudaStream_t st, int64_t* launches)
+template <bool POPC>
+static gvx_status pfx_run(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, DevBuf& tmp, cudaStream_t st,
+                          int64_t* launches)
 {
-    const uint32_t nb = (words + kPfxChunk - 1) / kPfxChunk;
+    const uint32_t nb = std::max<uint32_t>(1u, (n + kPfxChunk - 1) / kPfxChunk);
     GVX_CK(gvx_ensure(tmp, (size_t)(nb + 1) * sizeof(uint32_t)));
-    k_pfx_reduce<<<nb, kPfxThreads, 0, st>>>(bits, words, tmp.as<uint32_t>());
+    k_pfx_reduce<POPC><<<nb, kPfxThreads, 0, st>>>(in, n, tmp.as<uint32_t>());
     k_pfx_top<<<1, 1024, 0, st>>>(tmp.as<uint32_t>(), nb, total);
-    k_pfx_apply<<<nb, kPfxThreads, 0, st>>>(bits, words, tmp.as<uint32_t>(), prefix);
+    k_pfx_apply<POPC><<<nb, kPfxThreads, 0, st>>>(in, n, tmp.as<uint32_t>(), out);
     *launches += 3;
     GVX_CK(cudaGetLastError());
     return GVX_OK;
+}
+
+gvx_status gvx_bitmap_prefix(const uint32_t* bits, uint32_t* prefix, uint32_t words, uint32_t* total, DevBuf& tmp,
+                             cudaStream_t st, int64_t* launches)
+{
+    return pfx_run<true>(bits, prefix, words, total, tmp, st, launches);
+}
+
+gvx_status gvx_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total, DevBuf& tmp, cudaStream_t st,
+                        int64_t* launches)
+{
+    return pfx_run<false>(in, out, n, total, tmp, st, launches);
 }
 
 // set bits -> sorted key list (select)
@@ -1504,6 +1526,7 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     }
     gvx_status rc = ensure_grid_scratch(g);
     if (rc) return rc;
+    g->sc_valid = false;
     const float o[3] = {orig ? orig[0] : 0.f, orig ? orig[1] : 0.f, orig ? orig[2] : 0.f};
     cudaStream_t st = g->stream;
     GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, st));
@@ -1631,6 +1654,7 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     GVX_CK(cudaGetLastError());
     g->atlas_used = used;
     g->atlas_valid = true;
+    g->sc_valid = false;  // subcell indices follow the atlas slots
     for (int c = 0; c < GVX_MAXCH; c++) g->ch[c].apron_valid = false;  // bricks moved to new slots
     return GVX_OK;
 }

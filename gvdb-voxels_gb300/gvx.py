@@ -75,8 +75,8 @@ def load(path=None):
         "gvx_insert_points": ([vp, i, fp, vp], i),
         "gvx_scatter_density": ([vp, i, f, f, fp, i], i),
         "gvx_insert_points_subcell": ([vp, i, i, f, fp, ip], i),
-        "gvx_gather_density": ([vp, i, i, f, fp, i, i], i),
-        "gvx_gather_levelset": ([vp, i, i, f, fp, i, i], i),
+        "gvx_gather_density": ([vp, i, i, f, fp, i, i, i, i], i),
+        "gvx_gather_levelset": ([vp, i, i, f, fp, i, i, i, i], i),
         "gvx_splat": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
@@ -169,9 +169,10 @@ class Grid:
         self._check(self.lib.gvx_sync(self.h))
 
     # --- points
-    def set_points(self, n, pos, pos_offset=0, pos_stride=12, vel=None, vel_offset=0, vel_stride=12):
+    def set_points(self, n, pos, pos_offset=0, pos_stride=12, vel=None, vel_offset=0, vel_stride=12, clr=None,
+                   clr_offset=0, clr_stride=4):
         self._check(self.lib.gvx_set_points(self.h, n, _ptr(pos), pos_offset, pos_stride, _ptr(vel), vel_offset,
-                                            vel_stride, None, 0, 0))
+                                            vel_stride, _ptr(clr), clr_offset, clr_stride))
 
     def set_point_attribs(self, weight=None, radius=None):
         self._check(self.lib.gvx_set_point_attribs(self.h, _ptr(weight), _ptr(radius)))
@@ -222,11 +223,13 @@ class Grid:
                                                        ctypes.byref(ln)))
         return ln.value
 
-    def gather_density(self, subcell, n, radius, trans=None, chan=0, accum=False):
-        self._check(self.lib.gvx_gather_density(self.h, subcell, n, float(radius), _f3(trans), chan, int(accum)))
+    def gather_density(self, subcell, n, radius, sc_len, trans=None, chan=0, chan_clr=-1, accum=False):
+        self._check(self.lib.gvx_gather_density(self.h, subcell, n, float(radius), _f3(trans), sc_len, chan,
+                                                chan_clr, int(accum)))
 
-    def gather_levelset(self, subcell, n, radius, trans=None, chan=0, accum=False):
-        self._check(self.lib.gvx_gather_levelset(self.h, subcell, n, float(radius), _f3(trans), chan, int(accum)))
+    def gather_levelset(self, subcell, n, radius, sc_len, trans=None, chan=0, chan_clr=-1, accum=False):
+        self._check(self.lib.gvx_gather_levelset(self.h, subcell, n, float(radius), _f3(trans), sc_len, chan,
+                                                 chan_clr, int(accum)))
 
     def update_apron(self, chan=None, boundval=0.0):
         if chan is None:

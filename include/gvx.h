@@ -140,15 +140,25 @@ gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* 
  * without the reference's racy read-modify-write. */
 gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3],
                                int expand);
-/* InsertPointsSubcell (VG.h:551, VG.cpp:4971-5092): sc_len receives the number
- * of (point, subcell) entries, as pSCPntsLength */
+/* InsertPointsSubcell (VG.h:551, VG.cpp:4971-5092): every point joins each
+ * subcell (size `subcell`, dividing the brick size) of an active brick that
+ * its box [(int(p-r)/s)s, (int(p+1+r)/s)s] touches.  sc_len receives the
+ * number of (point, subcell) entries, as pSCPntsLength.  Needs UpdateAtlas
+ * after the topology build.  Points with z == NOHIT (1e10) are skipped. */
 gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius,
                                      const float trans[3], int* sc_len);
-/* GatherDensity / GatherLevelSet (VG.h:556-557, VG.cpp:5318-5373) */
+/* GatherDensity / GatherLevelSet (VG.h:556-557, VG.cpp:5318-5373): every
+ * interior voxel v of every active brick takes max(R - |p - v|) (density,
+ * start 0) or min(|p - v| - R) (level set, start 3) over the points listed in
+ * its subcell by the last InsertPointsSubcell (same subcell size), starting
+ * from the old value with accum.  chan is a T_FLOAT channel; chan_clr a
+ * T_UCHAR4 channel or -1: it receives the mean colour of the listed points
+ * when SetPoints bound colours.  GatherDensity does nothing when sc_len is 0,
+ * as in the reference; n and trans are unused, as in the reference. */
 gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
-                              int chan_density, int accum);
+                              int sc_len, int chan_density, int chan_clr, int accum);
 gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
-                               int chan_levelset, int accum);
+                               int sc_len, int chan_levelset, int chan_clr, int accum);
 /* TRILINEAR / CUBIC splat of weight (and velocity*weight into a FLOAT3/FLOAT4
  * channel) of the points that lie in active bricks; chan_vel may be -1.
  * Every voxel of each active brick, apron included, receives the sum of the

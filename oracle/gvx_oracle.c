@@ -675,7 +675,7 @@ int orc_add_channel(orc_grid* g, int chan, int type)
     int nc;
     switch (type) {
     case ORC_T_FLOAT: case ORC_T_UCHAR: nc = 1; break;
-    case ORC_T_FLOAT3: case ORC_T_FLOAT4: nc = 4; break;
+    case ORC_T_FLOAT3: case ORC_T_FLOAT4: case ORC_T_UCHAR4: nc = 4; break;
     default: return ORC_ERR_ARG;
     }
     if (!g->have_atlas) {
@@ -1013,11 +1013,14 @@ static int splat_ref_scatter(orc_grid* g, int n, const float* pos, int ps, float
 
 /* InsertPointsSubcell (VG.cpp:4971-5092; PT.cuh:109-118, 218-315, 677-694) and
  * GatherDensity / GatherLevelSet (VG.cpp:5318-5373; PT.cuh:696-773) */
-static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int ps, float radius,
-                        float rins, const float* tr, int sc, int chan, int accum)
+static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int ps, const uint8_t* clr,
+                        float radius, float rins, const float* tr, int sc, int chan, int chan_clr, int accum,
+                        int64_t* sc_len)
 {
     pool* p0 = &g->pools[0];
     if (!g->ch[chan]) return ORC_ERR_STATE;
+    if (chan_clr >= 0 && (chan_clr >= MAXCH || !g->ch[chan_clr] || g->ncomp[chan_clr] != 4)) return ORC_ERR_ARG;
+    if (!clr) chan_clr = -1; /* no point colours: the colour channel is not written */
     int b = g->brick;
     if (sc <= 0 || b % sc) return ORC_ERR_ARG;
     int scdim = b / sc, spb = scdim * scdim * scdim;
@@ -1073,8 +1076,10 @@ static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int 
     int* list = (int*)malloc((size_t)(lcnt + 1) * sizeof(int));
     int64_t* fill = (int64_t*)calloc((size_t)(nsc + 1), sizeof(int64_t));
     for (int64_t k = 0; k < lcnt; k++) list[off[lsc[k]] + fill[lsc[k]]++] = lpt[k];
+    if (sc_len) *sc_len = lcnt;
+    const int skip = !levelset && lcnt == 0; /* GatherDensity returns when pSCPntsLength is 0 (VG.cpp:5321) */
     /* gather per subcell voxel */
-    for (int i = 0; i < total; i++) {
+    for (int i = 0; i < total && !skip; i++) {
         orc_node* nd = &p0->nodes[i];
         if (nd->parent == ID_UNDEF64) continue;
         if (nd->value[0] < 0) continue;
@@ -1098,6 +1103,20 @@ static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int 
                             else { double t = radius - c; if (t > val) val = t; }
                         }
                         *out = val;
+                        if (chan_clr < 0) continue;
+                        /* colour: mean of the listed points' colours and, with accum, the old one */
+                        double* co = vox_ptr(g, chan_clr, nd->value, lx, ly, lz);
+                        double c4[4] = {0.0, 0.0, 0.0, 1.0};
+                        if (accum)
+                            for (int k = 0; k < 4; k++) c4[k] = co[k] / 255.0;
+                        for (int64_t j = off[idx]; j < off[idx + 1]; j++)
+                            for (int k = 0; k < 4; k++) c4[k] += clr[(int64_t)list[j] * 4 + k] / 255.0;
+                        double den = (double)(off[idx + 1] - off[idx]) + (accum ? 1.0 : 0.0);
+                        for (int k = 0; k < 4; k++) {
+                            double v = c4[k] / den * 255.0;
+                            v = v != v ? 0.0 : (v < 0.0 ? 0.0 : (v > 255.0 ? 255.0 : v));
+                            co[k] = floor(v);
+                        }
                     }
         }
     }
@@ -1125,10 +1144,23 @@ int orc_splat(orc_grid* g, int mode, int n, const float* pos, int pos_stride, co
         return splat_ref_scatter(g, n, pos, pos_stride, radius, tr, expand);
     case ORC_SPLAT_GATHER_DENSITY:
     case ORC_SPLAT_GATHER_LEVELSET:
-        return splat_gather(g, mode == ORC_SPLAT_GATHER_LEVELSET, n, pos, pos_stride, radius, radius_ins, tr,
-                            subcell, chan_density, accum);
+        return splat_gather(g, mode == ORC_SPLAT_GATHER_LEVELSET, n, pos, pos_stride, NULL, radius, radius_ins, tr,
+                            subcell, chan_density, -1, accum, NULL);
     }
     return ORC_ERR_ARG;
+}
+
+int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_stride, const uint8_t* clr,
+               float radius, float radius_ins, const float trans[3], int subcell, int chan, int chan_clr,
+               int accum, int64_t* sc_len)
+{
+    if (!g || n < 0 || (n > 0 && !pos) || pos_stride < 3) return ORC_ERR_ARG;
+    if (g->root_level < 0) return ORC_ERR_STATE;
+    if (chan < 0 || chan >= MAXCH || !g->ch[chan]) return ORC_ERR_ARG;
+    float tr[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    g->degenerate = 0;
+    return splat_gather(g, levelset, n, pos, pos_stride, clr, radius, radius_ins, tr, subcell, chan, chan_clr,
+                        accum, sc_len);
 }
 
 /* ------------------------------------------------------------------ */

@@ -53,7 +53,7 @@ enum {
 };
 
 /* channel types, same numbering as gvdb_types.h:70-78 */
-enum { ORC_T_UCHAR = 0, ORC_T_FLOAT = 3, ORC_T_FLOAT3 = 4, ORC_T_FLOAT4 = 5 };
+enum { ORC_T_UCHAR = 0, ORC_T_UCHAR4 = 2, ORC_T_FLOAT = 3, ORC_T_FLOAT3 = 4, ORC_T_FLOAT4 = 5 };
 
 /* 64-byte node record, same layout as VDBNode (cuda_gvdb_nodes.cuh:24-35) */
 typedef struct orc_node {
@@ -100,6 +100,16 @@ int orc_splat(orc_grid* g, int mode, int n, const float* pos, int pos_stride,
               const float* weight, const float* radius_pp, const float* vel, int vel_stride,
               float radius, const float trans[3], int chan_density, int chan_vel,
               int accum, int expand, int subcell, float radius_ins);
+
+/* InsertPointsSubcell + GatherDensity / GatherLevelSet with the optional
+ * colour average (PT.cuh:696-773): clr holds one uchar4 per point (or NULL),
+ * chan_clr a T_UCHAR4 channel (or -1).  *sc_len receives the number of
+ * (point, subcell) entries (pSCPntsLength).  The colour is stored as
+ * uchar(c * 255) saturated to [0, 255] (the reference's conversion of values
+ * outside that range is undefined). */
+int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_stride, const uint8_t* clr,
+               float radius, float radius_ins, const float trans[3], int subcell, int chan, int chan_clr,
+               int accum, int64_t* sc_len);
 
 int orc_update_apron(orc_grid* g, int chan, double boundval);
 

@@ -17,7 +17,7 @@ SRC = os.path.join(HERE, "gvx_oracle.c")
 OK, ERR_ARG, ERR_DEPTH, ERR_DEGENERATE, ERR_STATE, ERR_NOMEM = 0, 1, 2, 3, 4, 5
 TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
 SPLAT_TRILINEAR, SPLAT_CUBIC, SPLAT_REF_SCATTER, SPLAT_GATHER_DENSITY, SPLAT_GATHER_LEVELSET = 0, 1, 2, 3, 4
-T_UCHAR, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 3, 4, 5
+T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
 
 NODE_DTYPE = np.dtype([("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "u1"),
                        ("pos", "<i4", (3,)), ("value", "<i4", (3,)), ("vrange", "<f4", (3,)),
@@ -55,6 +55,7 @@ def load():
         "orc_get_nodes": ([vp, i, vp, i], i), "orc_get_childlist": ([vp, i, vp, i64], i),
         "orc_atlas_subdim": ([vp, vp], i), "orc_get_atlas_map": ([vp, vp, i], i),
         "orc_splat": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, i, i, i, i, i, f], i),
+        "orc_gather": ([vp, i, i, vp, i, vp, f, f, vp, i, i, i, i, vp], i),
         "orc_update_apron": ([vp, i, d], i), "orc_channel_size": ([vp, i], i64),
         "orc_read_channel": ([vp, i, vp, i64], i), "orc_write_channel": ([vp, i, vp, i64], i),
         "orc_activate_space_cpu": ([i, vp, i, vp, i, vp, vp, i, vp], i),
@@ -109,7 +110,7 @@ class Oracle:
 
     def add_channel(self, chan, typ):
         self._ck(self.lib.orc_add_channel(self.h, chan, typ), "add_channel")
-        self.ncomp[chan] = 4 if typ in (T_FLOAT3, T_FLOAT4) else 1
+        self.ncomp[chan] = 4 if typ in (T_FLOAT3, T_FLOAT4, T_UCHAR4) else 1
 
     def clear_channel(self, chan):
         self._ck(self.lib.orc_clear_channel(self.h, chan), "clear_channel")
@@ -174,6 +175,19 @@ class Oracle:
         st = self.lib.orc_splat(self.h, mode, pos.shape[0], _p(pos), 3, _p(w), _p(r), _p(v), 3, float(radius),
                                 _p(t), chan_density, chan_vel, int(accum), int(expand), subcell, float(radius_ins))
         return self._ck(st, "splat", allow_degenerate)
+
+    def gather(self, levelset, pos, radius, radius_ins, subcell=4, chan=0, chan_clr=-1, clr=None,
+               trans=(0, 0, 0), accum=False, allow_degenerate=False):
+        """InsertPointsSubcell + GatherDensity / GatherLevelSet; returns the
+        number of (point, subcell) entries"""
+        pos = np.ascontiguousarray(pos, np.float32)
+        c = None if clr is None else np.ascontiguousarray(clr, np.uint8).reshape(-1, 4)
+        t = np.ascontiguousarray(trans, np.float32)
+        n = ctypes.c_int64(0)
+        st = self.lib.orc_gather(self.h, int(levelset), pos.shape[0], _p(pos), 3, _p(c), float(radius),
+                                 float(radius_ins), _p(t), subcell, chan, chan_clr, int(accum), ctypes.byref(n))
+        self._ck(st, "gather", allow_degenerate)
+        return n.value
 
     def update_apron(self, chan, boundval=0.0):
         self._ck(self.lib.orc_update_apron(self.h, chan, float(boundval)), "update_apron")

@@ -153,7 +153,7 @@ def test_scatter_matches_reference_kernels(orc):
 
 
 @pytest.mark.parametrize("levelset", [False, True])
-def test_gathers_match_reference_kernels(orc, levelset):
+def test_gathers_match_reference_kernels(orc, gvx_mod, levelset):
     pos = slab(15_000, 9, box=(100.0, 80.0, 120.0))
     r, o = pair(orc)
     r.set_points(pos)
@@ -168,3 +168,17 @@ def test_gathers_match_reference_kernels(orc, levelset):
     ref = o.read_channel(0)[:used, 1:-1, 1:-1, 1:-1]
     # the reference takes sqrtf with --use_fast_math: absolute error <= 1e-5 of the radius scale
     assert np.abs(got - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
+    # libgvx against the reference kernels directly
+    g = gvx_mod.Grid(0)
+    g.configure((3, 3, 3, 3, 5))
+    g.add_channel(0, gvx_mod.T_FLOAT, 1)
+    g.commit_points_host(pos)
+    g.rebuild_topology(len(pos), 2.0, mode=gvx_mod.TOPO_FULL)
+    g.update_atlas()
+    n = g.insert_points_subcell(4, len(pos), 2.0)
+    if levelset:
+        g.gather_levelset(4, len(pos), 1.0, n, chan=0)
+    else:
+        g.gather_density(4, len(pos), 1.0, n, chan=0)
+    mine = g.read_channel(0)[:used, 1:-1, 1:-1, 1:-1].astype(np.float64)
+    assert np.abs(mine - got).max() <= 1e-5 * max(1.0, np.abs(got).max())

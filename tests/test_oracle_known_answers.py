@@ -137,6 +137,25 @@ def test_gather_known_values(orc):
     assert math.isclose(blk[100 - 96 + 1, 1, 300 - 296 + 1], math.sqrt(0.75) - 1.0, rel_tol=1e-9)
 
 
+def test_gather_colour_and_entry_count(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    o.add_channel(1, orc.T_UCHAR4)
+    pts = np.array([[10.5, 10.5, 10.5], [100.5, 100.5, 100.5]], np.float32)
+    clr = np.array([[200, 100, 50, 0], [10, 20, 30, 40]], np.uint8)
+    o.rebuild_topology(pts, 0.0)
+    o.update_atlas()
+    # insertion radius 0: each point joins the one subcell [(int(p)/4)*4, (int(p+1)/4)*4] = [8, 8]
+    n = o.gather(False, pts, 1.0, 0.0, subcell=4, chan=0, chan_clr=1, clr=clr)
+    assert n == 2
+    leaves = o.nodes(0)["pos"].tolist()
+    c = o.read_channel(1)[leaves.index([8, 8, 8])]
+    # (0,0,0,1) + clr/255 over one point, times 255, truncated and saturated (PT.cuh:724-732)
+    assert c[1 + 2, 1 + 2, 1 + 2].tolist() == [200.0, 100.0, 50.0, 255.0]
+    # a subcell with no point: 0/0 -> 0 for r,g,b and 1/0 -> 255 for alpha
+    assert c[1 + 5, 1 + 5, 1 + 5].tolist() == [0.0, 0.0, 0.0, 255.0]
+
+
 def test_apron_copies_neighbours_and_boundary(orc):
     o = orc.Oracle()
     o.add_channel(0, orc.T_FLOAT)
