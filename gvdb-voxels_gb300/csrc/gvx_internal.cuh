@@ -20,6 +20,7 @@
 #define GVX_DERR_CAPACITY 2u     // a kernel found more items than its buffer holds
 #define GVX_DERR_DEGENERATE 4u   // a node lies outside the root / a level-0 key domain
 #define GVX_DERR_BADPOINT 8u     // NaN position
+#define GVX_DERR_RADIUS 16u      // a per-point splat radius reaches past the 26 neighbouring bricks
 
 // 64-byte node record, layout of VDBNode (cuda_gvdb_nodes.cuh:24-35) / Node (gvdb_node.h:27-40)
 struct __align__(16) GvxNode {

@@ -1,17 +1,17 @@
 // gvx_splat.cu -- point -> brick-atlas splats.
 //
 // Modes
-//   TRILINEAR, CUBIC (no reference counterpart): one warp per active brick
-//     PULLS the points of its 27-brick neighbourhood (points are grouped by
-//     brick by the topology sort), keeps those whose footprint reaches the
-//     PADDED brick, and adds them into a shared-memory copy of the whole padded
-//     brick in their global sorted order, one point at a time across the
+//   TRILINEAR, CUBIC (no reference counterpart): one warp per z-slab of an
+//     active PADDED brick PULLS the points of the brick's 27-neighbourhood
+//     (points are grouped by brick by the topology sort), keeps those whose
+//     footprint reaches its slab, and adds them into a shared-memory copy of
+//     the slab in their global sorted order, one point at a time across the
 //     warp's lanes.  Every voxel is therefore the same sum, added in the same
 //     order, in the brick that owns it and in the bricks that hold it as an
 //     apron voxel: the splat writes interior and apron together, the apron
 //     bit-identical to the neighbours' interior (UpdateApron's copy
 //     semantics), with no atomics, deterministically, and one bulk (TMA) store
-//     per channel and brick.
+//     per channel and slab.
 //   REF_SCATTER: ScatterDensity semantics (gvdb_volume_gvdb.cpp:5624-5660,
 //     cuda_gvdb_particles.cuh:516-573): (1 - d^2/r^2)^3 at the point's voxel
 //     and its 6 face neighbours, inside the point's own padded brick, summed
@@ -26,7 +26,9 @@
 
 namespace {
 constexpr int kSplatThreads = 256;
-constexpr int kFusedWarps = 4;
+constexpr int kSlabWarps = 4;        // warps (brick slabs) per block of the splat
+constexpr int kSlabMinBlocks = 6;    // resident blocks per SM the register budget is sized for
+constexpr size_t kSlabTileMax = 48 * 1024;  // shared tile bytes of one warp at most
 constexpr float kInvPi = 0.318309886183790671538f;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 }  // namespace
@@ -94,6 +96,9 @@ struct SplatArgs {
     float radius;
     float* den;          // channel data (slot-major, P^3 per slot) or nullptr
     float4* vel;         // or nullptr
+    int slabs, slab_layers;  // z-slabs per padded brick, layers per slab
+    int reach;           // voxels a point's footprint reaches beyond its brick (neighbour pruning)
+    float max_radius;    // per-point radii above this reach past the 26 neighbours
     bool accum;
     float boundval;
     uint32_t* err;
@@ -129,18 +134,24 @@ struct Tile {
     }
 };
 
+// One warp per (brick, z-slab): the padded brick's layers are split into
+// slabs of a.slab_layers layers, each with its own shared tile, so a warp's
+// tile is a fraction of the brick and twice as many warps stay resident.
+// Every slab sees the same candidate points in the same order, so a voxel's
+// sum does not depend on the split.
 template <bool HAS_DEN, bool HAS_VEL, int MODE>
-__global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
+__global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(SplatArgs a)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
-    const int P = a.P, P3 = P * P * P, ap = a.apron;
+    const int P = a.P, P2 = P * P, P3 = P2 * P, ap = a.apron, b = a.brick;
+    const int L = a.slab_layers, S = a.slabs;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char* tile = smem + (size_t)wid * T::bytes(P3);
-    __shared__ __align__(8) uint64_t s_bar[kFusedWarps];
-    __shared__ int s_rs[kFusedWarps][28];
-    __shared__ int s_ro[kFusedWarps][28];
-    // single-channel tiles go to HBM in one bulk (TMA) store; the combined
+    unsigned char* tile = smem + (size_t)wid * T::bytes(L * P2);
+    __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
+    __shared__ int s_rs[kSlabWarps][28];
+    __shared__ int s_ro[kSlabWarps][28];
+    // single-channel tiles go to HBM in one bulk (TMA) copy; the combined
     // density+velocity tile is split into the two channels by vector stores
     constexpr bool BULK = !(HAS_DEN && HAS_VEL);
 
@@ -150,20 +161,28 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
     }
     __syncwarp();
     uint32_t phase = 0;
-    const uint32_t nw = gridDim.x * kFusedWarps;
-    for (uint32_t s = blockIdx.x * kFusedWarps + wid; s < a.nslots; s += nw) {
+    const uint32_t units = a.nslots * (uint32_t)S;
+    const uint32_t nw = gridDim.x * kSlabWarps;
+    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw) {
+        const uint32_t s = u / (uint32_t)S;
+        const int z0 = (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
+        const int nl = min(L, P - z0);
+        const int nvox = nl * P2;
+        const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel
         const int leaf = a.slot_leaf[s];
         const GvxNode* nd = a.nodes0 + leaf;
         const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
+        const int Zlo = Oz + z0, Zhi = Oz + z0 + nl - 1;                          // world z of the slab
 
-        // ---- the 27 neighbour ranges, ordered by their place in the sorted points
+        // ---- the 27 neighbour ranges that can reach the slab, ordered by their place in the sorted points
         int2 rg = make_int2(0, 0);
         bool has_nb = false;
         if (lane < 27) {
-            const int nl = a.nbr[(size_t)leaf * 27 + lane];
-            if (nl >= 0) {
-                rg = a.leaf_range[nl];
-                has_nb = a.leaf_slot[nl] >= 0;
+            const int nl_ = a.nbr[(size_t)leaf * 27 + lane];
+            if (nl_ >= 0) {
+                has_nb = a.leaf_slot[nl_] >= 0;
+                const int bz = nd->pos[2] + (lane / 9 - 1) * b;  // the neighbour's world z range [bz, bz + b)
+                if (bz - a.reach <= Zhi && bz + b - 1 + a.reach >= Zlo) rg = a.leaf_range[nl_];
             }
         }
         const uint32_t nbmask = __ballot_sync(kFull, has_nb);
@@ -190,22 +209,22 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
         if (a.accum) {
             if (BULK) {
                 if (lane == 0) {
-                    const uint32_t nb = (uint32_t)T::bytes(P3);
+                    const uint32_t nb = (uint32_t)T::bytes(nvox);
                     mbar_expect_tx(&s_bar[wid], nb);
-                    if (HAS_DEN) bulk_g2s(tile, a.den + (size_t)s * P3, nb, &s_bar[wid]);
-                    else bulk_g2s(tile, a.vel + (size_t)s * P3, nb, &s_bar[wid]);
+                    if (HAS_DEN) bulk_g2s(tile, a.den + gofs, nb, &s_bar[wid]);
+                    else bulk_g2s(tile, a.vel + gofs, nb, &s_bar[wid]);
                 }
                 if (!mbar_wait_bounded(&s_bar[wid], phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
                 phase ^= 1u;
             } else {
                 float4* tv = (float4*)tile;
-                for (int i = lane; i < P3; i += 32) {
-                    const float4 v = a.vel[(size_t)s * P3 + i];
-                    tv[i] = make_float4(v.x, v.y, v.z, a.den[(size_t)s * P3 + i]);
+                for (int i = lane; i < nvox; i += 32) {
+                    const float4 v = a.vel[gofs + i];
+                    tv[i] = make_float4(v.x, v.y, v.z, a.den[gofs + i]);
                 }
             }
         } else {
-            for (int i = lane; i < P3; i += 32) T::set(tile, i, 0.0f);
+            for (int i = lane; i < nvox; i += 32) T::set(tile, i, 0.0f);
         }
         __syncwarp();
 
@@ -224,20 +243,21 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                 }
                 idx = s_rs[wid][lo] + (v - s_ro[wid][lo]);
             }
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f), u = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
             bool hit = false;
             if (idx >= 0) {
                 p = a.spos[idx];
-                if (HAS_VEL || a.per_point_radius) u = a.svel[idx];
+                if (HAS_VEL || a.per_point_radius) uv = a.svel[idx];
                 if (MODE == GVX_SPLAT_TRILINEAR) {
-                    const int x0 = (int)floorf(p.x), y0 = (int)floorf(p.y), z0 = (int)floorf(p.z);
-                    hit = x0 + 1 >= Ox && x0 < Ox + P && y0 + 1 >= Oy && y0 < Oy + P && z0 + 1 >= Oz && z0 < Oz + P;
+                    const int x0 = (int)floorf(p.x), y0 = (int)floorf(p.y), z0p = (int)floorf(p.z);
+                    hit = x0 + 1 >= Ox && x0 < Ox + P && y0 + 1 >= Oy && y0 < Oy + P && z0p + 1 >= Zlo && z0p <= Zhi;
                 } else {
                     // voxels strictly inside (p - R, p + R) on every axis
-                    const float R = a.per_point_radius ? u.w : a.radius;
+                    const float R = a.per_point_radius ? uv.w : a.radius;
+                    if (R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
                     hit = (int)ceilf(p.x + R) - 1 >= Ox && (int)floorf(p.x - R) + 1 < Ox + P &&
                           (int)ceilf(p.y + R) - 1 >= Oy && (int)floorf(p.y - R) + 1 < Oy + P &&
-                          (int)ceilf(p.z + R) - 1 >= Oz && (int)floorf(p.z - R) + 1 < Oz + P;
+                          (int)ceilf(p.z + R) - 1 >= Zlo && (int)floorf(p.z - R) + 1 <= Zhi;
                 }
             }
             uint32_t hm = __ballot_sync(kFull, hit);
@@ -248,16 +268,16 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                 const float pz = __shfl_sync(kFull, p.z, src), pw = __shfl_sync(kFull, p.w, src);
                 float ux = 0.f, uy = 0.f, uz = 0.f;
                 if (HAS_VEL) {
-                    ux = __shfl_sync(kFull, u.x, src);
-                    uy = __shfl_sync(kFull, u.y, src);
-                    uz = __shfl_sync(kFull, u.z, src);
+                    ux = __shfl_sync(kFull, uv.x, src);
+                    uy = __shfl_sync(kFull, uv.y, src);
+                    uz = __shfl_sync(kFull, uv.z, src);
                 }
                 if (MODE == GVX_SPLAT_TRILINEAR) {
                     if (lane < 8) {
                         const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
                         const int dx = lane & 1, dy = (lane >> 1) & 1, dz = lane >> 2;
-                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Oz;
-                        if (lx >= 0 && ly >= 0 && lz >= 0 && lx < P && ly < P && lz < P) {
+                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Oz - z0;
+                        if (lx >= 0 && ly >= 0 && lz >= 0 && lx < P && ly < P && lz < nl) {
                             const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
                             const float wgt =
                                 pw * (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
@@ -266,20 +286,27 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                     }
                 } else {
                     // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
-                    // support R = 2h.  Rows (y, z) over the lanes; along a row R^2 - d^2 is
-                    // formed from an error-free c = R^2 - dy^2 - dz^2 (two-product, two-sum)
-                    // so that the outer branch 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3
-                    // keeps FP32 relative accuracy up to the edge of the support.
-                    const float R = a.per_point_radius ? __shfl_sync(kFull, u.w, src) : a.radius;
+                    // support R = 2h.  The lanes take (row, x pair) cells of the support box;
+                    // along a row R^2 - d^2 is formed from an error-free c = R^2 - dy^2 - dz^2
+                    // (two-product, two-sum) so that the outer branch
+                    // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
+                    // accuracy up to the edge of the support.
+                    const float R = a.per_point_radius ? __shfl_sync(kFull, uv.w, src) : a.radius;
                     const float h = 0.5f * R, inv_h = 1.0f / h;
                     const float norm = kInvPi * inv_h * inv_h * inv_h * pw;
                     const float r2h = R * R, r2l = fmaf(R, R, -r2h);
                     const int xl = max((int)floorf(px - R) + 1, Ox), xh = min((int)ceilf(px + R) - 1, Ox + P - 1);
                     const int yl = max((int)floorf(py - R) + 1, Oy), yh = min((int)ceilf(py + R) - 1, Oy + P - 1);
-                    const int zl = max((int)floorf(pz - R) + 1, Oz), zh = min((int)ceilf(pz + R) - 1, Oz + P - 1);
-                    const int ny = yh - yl + 1, nz = zh - zl + 1;
-                    for (int r = lane; r < ny * nz; r += 32) {
-                        const int y = yl + r % ny, z = zl + r / ny;
+                    const int zl = max((int)floorf(pz - R) + 1, Zlo), zh = min((int)ceilf(pz + R) - 1, Zhi);
+                    const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1, nz = zh - zl + 1;
+                    const int ncell = nxp * ny * nz;
+                    const float inv_nxp = 1.0f / (float)nxp, inv_ny = 1.0f / (float)ny;
+                    for (int c = lane; c < ncell; c += 32) {
+                        // c -> (x pair, y, z): exact for these small integers
+                        const int r = (int)(((float)c + 0.5f) * inv_nxp);
+                        const int xp = c - r * nxp;
+                        const int zz = (int)(((float)r + 0.5f) * inv_ny);
+                        const int y = yl + (r - zz * ny), z = zl + zz, x = xl + 2 * xp;
                         const float dy = (float)y - py, dz = (float)z - pz;
                         const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
                         const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
@@ -291,9 +318,12 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                         const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
                         const float cl = e2 + r2l - ((ey + ez) + e1);
                         if (c1 + cl <= 0.0f) continue;
-                        const int t0 = ((z - Oz) * P + (y - Oy)) * P - Ox;
-                        for (int x = xl; x <= xh; x++) {
-                            const float dx = (float)x - px;
+                        const int t0 = ((z - Zlo) * P + (y - Oy)) * P - Ox;
+#pragma unroll
+                        for (int k = 0; k < 2; k++) {
+                            const int xx = x + k;
+                            if (xx > xh) break;
+                            const float dx = (float)xx - px;
                             const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
                             if (t <= 0.0f) continue;
                             const float d = sqrtf(fmaf(dx, dx, syz));
@@ -305,7 +335,7 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
                                 const float uu = t / (h * (R + d));  // 2 - q
                                 wm = 0.25f * uu * uu * uu;
                             }
-                            T::add(tile, t0 + x, norm * wm, ux, uy, uz);
+                            T::add(tile, t0 + xx, norm * wm, ux, uy, uz);
                         }
                     }
                 }
@@ -315,15 +345,14 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
 
         // ---- apron voxels with no neighbouring brick take the boundary value (0)
         if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
-            const int napron = 6 * P * P - 12 * P + 8;
-            for (int e = lane; e < napron; e += 32) {
-                int x, y, z;
-                apron_voxel_coords(e, P, x, y, z);
+            for (int i = lane; i < nvox; i += 32) {
+                const int z = z0 + i / P2, r = i % P2, y = r / P, x = r % P;
                 const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
                 const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
                 const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
+                if (!(dx | dy | dz)) continue;  // interior voxel
                 if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
-                T::set(tile, (z * P + y) * P + x, a.boundval);
+                T::set(tile, i, a.boundval);
             }
             __syncwarp();
         }
@@ -333,17 +362,17 @@ __global__ void __launch_bounds__(kFusedWarps * 32) k_splat_fused(SplatArgs a)
             fence_async_smem();
             __syncwarp();
             if (lane == 0) {
-                if (HAS_DEN) bulk_s2g(a.den + (size_t)s * P3, tile, (uint32_t)T::bytes(P3));
-                else bulk_s2g(a.vel + (size_t)s * P3, tile, (uint32_t)T::bytes(P3));
+                if (HAS_DEN) bulk_s2g(a.den + gofs, tile, (uint32_t)T::bytes(nvox));
+                else bulk_s2g(a.vel + gofs, tile, (uint32_t)T::bytes(nvox));
                 bulk_commit();
                 bulk_wait_read_all();
             }
             __syncwarp();
         } else {
             const float4* tv = (const float4*)tile;
-            float* dg = a.den + (size_t)s * P3;
-            float4* vg = a.vel + (size_t)s * P3;
-            for (int i = lane; i < P3; i += 32) {
+            float* dg = a.den + gofs;
+            float4* vg = a.vel + gofs;
+            for (int i = lane; i < nvox; i += 32) {
                 const float4 o = tv[i];
                 dg[i] = o.w;
                 vg[i] = make_float4(o.x, o.y, o.z, 0.0f);
@@ -480,10 +509,10 @@ static int sm_count(gvx_grid* g)
 }
 
 template <bool D, bool V>
-static void* fused_kernel(int mode)
+static void* slab_kernel(int mode)
 {
-    return mode == GVX_SPLAT_TRILINEAR ? (void*)k_splat_fused<D, V, GVX_SPLAT_TRILINEAR>
-                                       : (void*)k_splat_fused<D, V, GVX_SPLAT_CUBIC>;
+    return mode == GVX_SPLAT_TRILINEAR ? (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR>
+                                       : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC>;
 }
 
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
@@ -521,13 +550,15 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     rc = gvx_prepare_points(g, n, trans, need_svel);
     if (rc) return rc;
 
-    const int P = g->P, P3 = P * P * P;
-    const size_t tile = has_v ? (size_t)P3 * 16 : (size_t)P3 * 4;
-    const size_t smem = tile * kFusedWarps;
-    if (smem > 220 * 1024) {
-        gvx_set_error("Splat: %d warps of %d^3 padded bricks need %zu bytes of shared memory", kFusedWarps, P, smem);
+    const int P = g->P, P2 = P * P;
+    const size_t eb = has_v ? 16 : 4;
+    // slab height: half the padded brick, fewer layers where a half does not fit the tile budget
+    const int layers = std::min((P + 1) / 2, (int)(kSlabTileMax / ((size_t)P2 * eb)));
+    if (layers < 1) {
+        gvx_set_error("Splat: a %d^2 layer of the padded brick exceeds the shared tile budget", P);
         return GVX_ERR_UNSUPPORTED;
     }
+    const size_t smem = (size_t)layers * P2 * eb * kSlabWarps;
     SplatArgs a;
     a.brick = g->brick;
     a.P = P;
@@ -544,6 +575,10 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     a.radius = radius;
     a.den = has_d ? g->ch[chan_d].data.as<float>() : nullptr;
     a.vel = has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
+    a.slab_layers = layers;
+    a.slabs = (P + layers - 1) / layers;
+    a.max_radius = (float)(g->brick - 1);
+    a.reach = mode == GVX_SPLAT_TRILINEAR ? 1 : (ppr ? g->brick - 1 : (int)ceilf(radius));
     a.accum = accum != 0;
     a.boundval = 0.0f;
     a.err = g->d_err.as<uint32_t>();
@@ -555,15 +590,16 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         if (has_v) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
     }
     if (a.nslots == 0) return GVX_OK;
-    void* kern = has_d ? (has_v ? fused_kernel<true, true>(mode) : fused_kernel<true, false>(mode))
-                       : fused_kernel<false, true>(mode);
+    void* kern = has_d ? (has_v ? slab_kernel<true, true>(mode) : slab_kernel<true, false>(mode))
+                       : slab_kernel<false, true>(mode);
     GVX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedWarps * 32, smem));
-    const uint64_t ctas_needed = (a.nslots + kFusedWarps - 1) / kFusedWarps;
+    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSlabWarps * 32, smem));
+    const uint64_t units = (uint64_t)a.nslots * a.slabs;
+    const uint64_t ctas_needed = (units + kSlabWarps - 1) / kSlabWarps;
     const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g) * std::max(per_sm, 1));
     void* args[] = {&a};
-    GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kFusedWarps * 32), args, smem, g->stream));
+    GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kSlabWarps * 32), args, smem, g->stream));
     g->launches++;
     if (has_d) {
         g->ch[chan_d].apron_valid = valid_after;

@@ -864,6 +864,10 @@ gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
         gvx_set_error("%s: NaN point position", stage);
         return GVX_ERR_INVALID_ARG;
     }
+    if (e & GVX_DERR_RADIUS) {
+        gvx_set_error("%s: a per-point radius exceeds brick-1 (footprint beyond the 26 neighbouring bricks)", stage);
+        return GVX_ERR_UNSUPPORTED;
+    }
     return GVX_OK;
 }
 
