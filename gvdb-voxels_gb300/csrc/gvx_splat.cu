@@ -139,10 +139,14 @@ struct Tile {
 // tile is a fraction of the brick and twice as many warps stay resident.
 // Every slab sees the same candidate points in the same order, so a voxel's
 // sum does not depend on the split.
-template <bool HAS_DEN, bool HAS_VEL, int MODE>
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
 __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(SplatArgs a)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
+    constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
+    // cubic constants of a uniform radius (per point with PPR)
+    const float R0 = a.radius, h0 = 0.5f * R0, inv_h0 = CUBIC && !PPR ? 1.0f / h0 : 0.0f;
+    const float norm0 = kInvPi * inv_h0 * inv_h0 * inv_h0, r2h0 = R0 * R0, r2l0 = fmaf(R0, R0, -r2h0);
     extern __shared__ __align__(128) unsigned char smem[];
     const int P = a.P, P2 = P * P, P3 = P2 * P, ap = a.apron, b = a.brick;
     const int L = a.slab_layers, S = a.slabs;
@@ -245,19 +249,23 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
             }
             float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
             bool hit = false;
+            uint32_t box0 = 0u, box1 = 0u;  // cubic: the support box in slab-tile coordinates, 8 bits a bound
             if (idx >= 0) {
                 p = a.spos[idx];
-                if (HAS_VEL || a.per_point_radius) uv = a.svel[idx];
-                if (MODE == GVX_SPLAT_TRILINEAR) {
-                    const int x0 = (int)floorf(p.x), y0 = (int)floorf(p.y), z0p = (int)floorf(p.z);
-                    hit = x0 + 1 >= Ox && x0 < Ox + P && y0 + 1 >= Oy && y0 < Oy + P && z0p + 1 >= Zlo && z0p <= Zhi;
+                if (HAS_VEL || PPR) uv = a.svel[idx];
+                if (!CUBIC) {
+                    const int x0 = (int)floorf(p.x) - Ox, y0 = (int)floorf(p.y) - Oy, zb = (int)floorf(p.z) - Zlo;
+                    hit = x0 >= -1 && x0 < P && y0 >= -1 && y0 < P && zb >= -1 && zb < nl;
                 } else {
-                    // voxels strictly inside (p - R, p + R) on every axis
-                    const float R = a.per_point_radius ? uv.w : a.radius;
-                    if (R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
-                    hit = (int)ceilf(p.x + R) - 1 >= Ox && (int)floorf(p.x - R) + 1 < Ox + P &&
-                          (int)ceilf(p.y + R) - 1 >= Oy && (int)floorf(p.y - R) + 1 < Oy + P &&
-                          (int)ceilf(p.z + R) - 1 >= Zlo && (int)floorf(p.z - R) + 1 <= Zhi;
+                    // voxels strictly inside (p - R, p + R) on every axis, clipped to the slab tile
+                    const float R = PPR ? uv.w : R0;
+                    if (PPR && R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
+                    const int xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
+                    const int yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
+                    const int zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
+                    hit = xl <= xh && yl <= yh && zl <= zh;
+                    box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
+                    box1 = (uint32_t)zl | ((uint32_t)zh << 8);
                 }
             }
             uint32_t hm = __ballot_sync(kFull, hit);
@@ -272,11 +280,11 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
                     uy = __shfl_sync(kFull, uv.y, src);
                     uz = __shfl_sync(kFull, uv.z, src);
                 }
-                if (MODE == GVX_SPLAT_TRILINEAR) {
+                if (!CUBIC) {
                     if (lane < 8) {
                         const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
                         const int dx = lane & 1, dy = (lane >> 1) & 1, dz = lane >> 2;
-                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Oz - z0;
+                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Zlo;
                         if (lx >= 0 && ly >= 0 && lz >= 0 && lx < P && ly < P && lz < nl) {
                             const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
                             const float wgt =
@@ -286,28 +294,34 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
                     }
                 } else {
                     // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
-                    // support R = 2h.  The lanes take (row, x pair) cells of the support box;
+                    // support R = 2h.  The lanes take (x pair, row) cells of the support box;
                     // along a row R^2 - d^2 is formed from an error-free c = R^2 - dy^2 - dz^2
                     // (two-product, two-sum) so that the outer branch
                     // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
                     // accuracy up to the edge of the support.
-                    const float R = a.per_point_radius ? __shfl_sync(kFull, uv.w, src) : a.radius;
-                    const float h = 0.5f * R, inv_h = 1.0f / h;
-                    const float norm = kInvPi * inv_h * inv_h * inv_h * pw;
-                    const float r2h = R * R, r2l = fmaf(R, R, -r2h);
-                    const int xl = max((int)floorf(px - R) + 1, Ox), xh = min((int)ceilf(px + R) - 1, Ox + P - 1);
-                    const int yl = max((int)floorf(py - R) + 1, Oy), yh = min((int)ceilf(py + R) - 1, Oy + P - 1);
-                    const int zl = max((int)floorf(pz - R) + 1, Zlo), zh = min((int)ceilf(pz + R) - 1, Zhi);
+                    const uint32_t b0 = __shfl_sync(kFull, box0, src), b1 = __shfl_sync(kFull, box1, src);
+                    float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
+                    if (PPR) {
+                        R = __shfl_sync(kFull, uv.w, src);
+                        h = 0.5f * R;
+                        inv_h = 1.0f / h;
+                        norm = kInvPi * inv_h * inv_h * inv_h;
+                        r2h = R * R;
+                        r2l = fmaf(R, R, -r2h);
+                    }
+                    norm *= pw;
+                    const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u);
+                    const int yl = (int)((b0 >> 16) & 255u), yh = (int)(b0 >> 24);
+                    const int zl = (int)(b1 & 255u), zh = (int)(b1 >> 8);
                     const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1, nz = zh - zl + 1;
-                    const int ncell = nxp * ny * nz;
-                    const float inv_nxp = 1.0f / (float)nxp, inv_ny = 1.0f / (float)ny;
+                    // cells on a power-of-two grid: decoded by shifts, the padding masked off
+                    const int bx = 32 - __clz(nxp - 1), by = 32 - __clz(ny - 1), bz = 32 - __clz(nz - 1);
+                    const int ncell = 1 << (bx + by + bz);
                     for (int c = lane; c < ncell; c += 32) {
-                        // c -> (x pair, y, z): exact for these small integers
-                        const int r = (int)(((float)c + 0.5f) * inv_nxp);
-                        const int xp = c - r * nxp;
-                        const int zz = (int)(((float)r + 0.5f) * inv_ny);
-                        const int y = yl + (r - zz * ny), z = zl + zz, x = xl + 2 * xp;
-                        const float dy = (float)y - py, dz = (float)z - pz;
+                        const int xp = c & ((1 << bx) - 1), yy = (c >> bx) & ((1 << by) - 1), zz = c >> (bx + by);
+                        if (xp >= nxp || yy >= ny || zz >= nz) continue;
+                        const int lx = xl + 2 * xp, ly = yl + yy, lz = zl + zz;
+                        const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
                         const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
                         const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
                         const float syz = qy + qz;
@@ -318,23 +332,20 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
                         const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
                         const float cl = e2 + r2l - ((ey + ez) + e1);
                         if (c1 + cl <= 0.0f) continue;
-                        const int t0 = ((z - Zlo) * P + (y - Oy)) * P - Ox;
+                        const int t0 = (lz * P + ly) * P;
 #pragma unroll
                         for (int k = 0; k < 2; k++) {
-                            const int xx = x + k;
+                            const int xx = lx + k;
                             if (xx > xh) break;
-                            const float dx = (float)xx - px;
+                            const float dx = (float)(xx + Ox) - px;
                             const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
                             if (t <= 0.0f) continue;
-                            const float d = sqrtf(fmaf(dx, dx, syz));
+                            const float d2 = fmaf(dx, dx, syz);
+                            const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
                             const float q = d * inv_h;
-                            float wm;
-                            if (q < 1.0f) {
-                                wm = 1.0f - 1.5f * q * q + 0.75f * q * q * q;
-                            } else {
-                                const float uu = t / (h * (R + d));  // 2 - q
-                                wm = 0.25f * uu * uu * uu;
-                            }
+                            const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
+                            const float uu = __fdividef(t, h * (R + d));               // 2 - q
+                            const float wm = q < 1.0f ? wi : 0.25f * uu * uu * uu;
                             T::add(tile, t0 + xx, norm * wm, ux, uy, uz);
                         }
                     }
@@ -509,10 +520,10 @@ static int sm_count(gvx_grid* g)
 }
 
 template <bool D, bool V>
-static void* slab_kernel(int mode)
+static void* slab_kernel(int mode, bool ppr)
 {
-    return mode == GVX_SPLAT_TRILINEAR ? (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR>
-                                       : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC>;
+    if (mode == GVX_SPLAT_TRILINEAR) return (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR, false>;
+    return ppr ? (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, true> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false>;
 }
 
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
@@ -590,8 +601,8 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         if (has_v) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
     }
     if (a.nslots == 0) return GVX_OK;
-    void* kern = has_d ? (has_v ? slab_kernel<true, true>(mode) : slab_kernel<true, false>(mode))
-                       : slab_kernel<false, true>(mode);
+    void* kern = has_d ? (has_v ? slab_kernel<true, true>(mode, ppr) : slab_kernel<true, false>(mode, ppr))
+                       : slab_kernel<false, true>(mode, ppr);
     GVX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSlabWarps * 32, smem));
