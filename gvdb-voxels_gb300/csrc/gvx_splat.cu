@@ -232,7 +232,12 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
         }
         __syncwarp();
 
-        // ---- candidates, 32 at a time, in sorted order
+        // ---- candidates, 32 at a time, in sorted order.  Each lane tests one
+        // candidate and sizes the cells of its footprint in the slab (a cell = an
+        // x pair of a (y, z) row); the cells of all hits are then dealt to the
+        // lanes 32 at a time, and updates are applied point by point in sorted
+        // order, so every voxel sums its contributions in the same order in every
+        // brick that holds it.
         for (int base = 0; base < total; base += 32) {
             const int v = base + lane;
             int idx = -1;
@@ -248,79 +253,107 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
                 idx = s_rs[wid][lo] + (v - s_ro[wid][lo]);
             }
             float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
-            bool hit = false;
-            uint32_t box0 = 0u, box1 = 0u;  // cubic: the support box in slab-tile coordinates, 8 bits a bound
+            uint32_t box0 = 0u, box1 = 0u, magic = 0u;  // footprint in slab-tile coordinates, 8 bits a bound
+            int ncell = 0;
             if (idx >= 0) {
                 p = a.spos[idx];
                 if (HAS_VEL || PPR) uv = a.svel[idx];
+                int xl, xh, yl, yh, zl, zh;
                 if (!CUBIC) {
                     const int x0 = (int)floorf(p.x) - Ox, y0 = (int)floorf(p.y) - Oy, zb = (int)floorf(p.z) - Zlo;
-                    hit = x0 >= -1 && x0 < P && y0 >= -1 && y0 < P && zb >= -1 && zb < nl;
+                    xl = max(x0, 0), xh = min(x0 + 1, P - 1);
+                    yl = max(y0, 0), yh = min(y0 + 1, P - 1);
+                    zl = max(zb, 0), zh = min(zb + 1, nl - 1);
                 } else {
-                    // voxels strictly inside (p - R, p + R) on every axis, clipped to the slab tile
+                    // voxels strictly inside (p - R, p + R) on every axis
                     const float R = PPR ? uv.w : R0;
                     if (PPR && R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
-                    const int xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
-                    const int yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
-                    const int zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
-                    hit = xl <= xh && yl <= yh && zl <= zh;
+                    xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
+                    yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
+                    zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
+                }
+                if (xl <= xh && yl <= yh && zl <= zh) {
+                    const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1;
+                    ncell = nxp * ny * (zh - zl + 1);
                     box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
                     box1 = (uint32_t)zl | ((uint32_t)zh << 8);
+                    // ceil(2^15 / n): (c * magic) >> 15 == c / n for c <= 2^15 / n (cells <= 7*14*14 here)
+                    magic = ((32767u + (uint32_t)nxp) / (uint32_t)nxp) | (((32767u + (uint32_t)ny) / (uint32_t)ny) << 16);
                 }
             }
-            uint32_t hm = __ballot_sync(kFull, hit);
-            while (hm) {
-                const int src = __ffs(hm) - 1;
-                hm &= hm - 1u;
-                const float px = __shfl_sync(kFull, p.x, src), py = __shfl_sync(kFull, p.y, src);
-                const float pz = __shfl_sync(kFull, p.z, src), pw = __shfl_sync(kFull, p.w, src);
+            // inclusive scan of the cell counts over the lanes
+            int cend = ncell;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, cend, o);
+                if (lane >= o) cend += t;
+            }
+            const int ctot = __shfl_sync(kFull, cend, 31);
+            const int cstart = cend - ncell;
+            for (int g0 = 0; g0 < ctot; g0 += 32) {
+                const int g = g0 + lane;
+                const bool act = g < ctot;
+                // the point dealing this cell: the first lane whose cells end after g
+                int lo = 0, hi = 31;
+#pragma unroll
+                for (int it = 0; it < 5; it++) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__shfl_sync(kFull, cend, mid) > g)
+                        hi = mid;
+                    else
+                        lo = mid + 1;
+                }
+                const int j = lo;
+                const float px = __shfl_sync(kFull, p.x, j), py = __shfl_sync(kFull, p.y, j);
+                const float pz = __shfl_sync(kFull, p.z, j), pw = __shfl_sync(kFull, p.w, j);
                 float ux = 0.f, uy = 0.f, uz = 0.f;
                 if (HAS_VEL) {
-                    ux = __shfl_sync(kFull, uv.x, src);
-                    uy = __shfl_sync(kFull, uv.y, src);
-                    uz = __shfl_sync(kFull, uv.z, src);
+                    ux = __shfl_sync(kFull, uv.x, j);
+                    uy = __shfl_sync(kFull, uv.y, j);
+                    uz = __shfl_sync(kFull, uv.z, j);
                 }
-                if (!CUBIC) {
-                    if (lane < 8) {
+                const uint32_t b0 = __shfl_sync(kFull, box0, j), b1 = __shfl_sync(kFull, box1, j);
+                const uint32_t mg = __shfl_sync(kFull, magic, j);
+                const int cell = g - __shfl_sync(kFull, cstart, j);
+                const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
+                const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
+                const int zl = (int)(b1 & 255u);
+                const int nxp = (xh - xl + 2) >> 1, ny = (int)(b0 >> 24) - yl + 1;
+                const int r = (int)(((uint32_t)cell * (mg & 0xFFFFu)) >> 15);
+                const int zz = (int)(((uint32_t)r * (mg >> 16)) >> 15);
+                const int lx = xl + 2 * (cell - r * nxp), ly = yl + (r - zz * ny), lz = zl + zz;
+                // the lane's two voxels (lx, lx + 1) of row (ly, lz): index and value
+                int vi0 = -1, vi1 = -1;
+                float w0 = 0.f, w1 = 0.f;
+                if (act) {
+                    const int t0 = (lz * P + ly) * P + lx;
+                    if (!CUBIC) {
                         const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
-                        const int dx = lane & 1, dy = (lane >> 1) & 1, dz = lane >> 2;
-                        const int lx = (int)fx0 + dx - Ox, ly = (int)fy0 + dy - Oy, lz = (int)fz0 + dz - Zlo;
-                        if (lx >= 0 && ly >= 0 && lz >= 0 && lx < P && ly < P && lz < nl) {
-                            const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
-                            const float wgt =
-                                pw * (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
-                            T::add(tile, (lz * P + ly) * P + lx, wgt, ux, uy, uz);
+                        const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
+                        const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
+                        const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
+                        w0 = pw * wxa * wyz;
+                        vi0 = t0;
+                        if (lx + 1 <= xh) {
+                            w1 = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
+                            vi1 = t0 + 1;
                         }
-                    }
-                } else {
-                    // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
-                    // support R = 2h.  The lanes take (x pair, row) cells of the support box;
-                    // along a row R^2 - d^2 is formed from an error-free c = R^2 - dy^2 - dz^2
-                    // (two-product, two-sum) so that the outer branch
-                    // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
-                    // accuracy up to the edge of the support.
-                    const uint32_t b0 = __shfl_sync(kFull, box0, src), b1 = __shfl_sync(kFull, box1, src);
-                    float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
-                    if (PPR) {
-                        R = __shfl_sync(kFull, uv.w, src);
-                        h = 0.5f * R;
-                        inv_h = 1.0f / h;
-                        norm = kInvPi * inv_h * inv_h * inv_h;
-                        r2h = R * R;
-                        r2l = fmaf(R, R, -r2h);
-                    }
-                    norm *= pw;
-                    const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u);
-                    const int yl = (int)((b0 >> 16) & 255u), yh = (int)(b0 >> 24);
-                    const int zl = (int)(b1 & 255u), zh = (int)(b1 >> 8);
-                    const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1, nz = zh - zl + 1;
-                    // cells on a power-of-two grid: decoded by shifts, the padding masked off
-                    const int bx = 32 - __clz(nxp - 1), by = 32 - __clz(ny - 1), bz = 32 - __clz(nz - 1);
-                    const int ncell = 1 << (bx + by + bz);
-                    for (int c = lane; c < ncell; c += 32) {
-                        const int xp = c & ((1 << bx) - 1), yy = (c >> bx) & ((1 << by) - 1), zz = c >> (bx + by);
-                        if (xp >= nxp || yy >= ny || zz >= nz) continue;
-                        const int lx = xl + 2 * xp, ly = yl + yy, lz = zl + zz;
+                    } else {
+                        // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
+                        // support R = 2h.  Along the row R^2 - d^2 is formed from an error-free
+                        // c = R^2 - dy^2 - dz^2 (two-product, two-sum) so that the outer branch
+                        // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
+                        // accuracy up to the edge of the support.
+                        float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
+                        if (PPR) {
+                            R = pR;
+                            h = 0.5f * R;
+                            inv_h = 1.0f / h;
+                            norm = kInvPi * inv_h * inv_h * inv_h;
+                            r2h = R * R;
+                            r2l = fmaf(R, R, -r2h);
+                        }
+                        norm *= pw;
                         const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
                         const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
                         const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
@@ -331,26 +364,42 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
                         bv = c1 - r2h;
                         const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
                         const float cl = e2 + r2l - ((ey + ez) + e1);
-                        if (c1 + cl <= 0.0f) continue;
-                        const int t0 = (lz * P + ly) * P;
+                        if (c1 + cl > 0.0f) {
 #pragma unroll
-                        for (int k = 0; k < 2; k++) {
-                            const int xx = lx + k;
-                            if (xx > xh) break;
-                            const float dx = (float)(xx + Ox) - px;
-                            const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
-                            if (t <= 0.0f) continue;
-                            const float d2 = fmaf(dx, dx, syz);
-                            const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                            const float q = d * inv_h;
-                            const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
-                            const float uu = __fdividef(t, h * (R + d));               // 2 - q
-                            const float wm = q < 1.0f ? wi : 0.25f * uu * uu * uu;
-                            T::add(tile, t0 + xx, norm * wm, ux, uy, uz);
+                            for (int k = 0; k < 2; k++) {
+                                if (lx + k > xh) break;
+                                const float dx = (float)(lx + k + Ox) - px;
+                                const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
+                                if (t <= 0.0f) continue;
+                                const float d2 = fmaf(dx, dx, syz);
+                                const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                                const float q = d * inv_h;
+                                const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
+                                const float uu = __fdividef(t, h * (R + d));               // 2 - q
+                                const float wv = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
+                                if (k == 0) {
+                                    w0 = wv;
+                                    vi0 = t0;
+                                } else {
+                                    w1 = wv;
+                                    vi1 = t0 + 1;
+                                }
+                            }
                         }
                     }
                 }
-                __syncwarp();
+                // apply point by point: the lanes of one point touch distinct voxels
+                const int jprev = __shfl_up_sync(kFull, j, 1);
+                const uint32_t first = __ballot_sync(kFull, act && (lane == 0 || jprev != j));
+                const int npts = __popc(first);
+                const int pr = __popc(first & (0xFFFFFFFFu >> (31 - lane))) - 1;
+                for (int ph = 0; ph < npts; ph++) {
+                    if (act && pr == ph) {
+                        if (vi0 >= 0) T::add(tile, vi0, w0, ux, uy, uz);
+                        if (vi1 >= 0) T::add(tile, vi1, w1, ux, uy, uz);
+                    }
+                    __syncwarp();
+                }
             }
         }
 
