@@ -156,9 +156,9 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 
 def algorithmic_bytes(n, nb, P):
-    """per frame: positions read by the topology, point attributes
-    read by the splat, every active padded brick written once per channel, and
-    the apron source voxels read once per channel"""
+    """algorithmic bytes per frame: positions read by the topology, point
+    attributes read by the splat, every active padded brick written once per
+    channel, and the apron source voxels read once per channel"""
     ch_bytes = 4 + 16  # density float + velocity float3 stored as float4
     b_topo = 12 * n
     b_splat_pts = (12 + 12) * n
@@ -351,6 +351,69 @@ def run_ours(args, rank, world, pool):
     return out
 
 
+def run_differentiable(dev, iters=5):
+    """Differentiable workload: 1M points U[8,504)^3, w ~ U(0,1), per-point R ~ U(1,3),
+    cubic density splat (forward) and its adjoint gvx_splat_backward (backward) with
+    G = rho - rho*, rho* the splat of p + N(0, 0.5).  CUDA-event times of both
+    kernels' calls on the grid's stream, after warm-up."""
+    import numpy as np
+    import torch
+
+    import gvx
+    import workloads
+
+    pos, w, r = workloads.differentiable(n=1_000_000, seed=1)
+    tgt = np.clip(pos + np.random.default_rng(2).normal(0, 0.5, pos.shape), 8.0, 504.0).astype(np.float32)
+    n = len(pos)
+    stream = torch.cuda.Stream(device=dev)
+    g = gvx.Grid(dev.index)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx.T_FLOAT, 1)
+    g.set_stream(stream.cuda_stream)
+    both = torch.from_numpy(np.vstack([pos, tgt])).to(dev)
+    pd, td = both[:n], both[n:]
+    wd, rd = torch.from_numpy(w).to(dev), torch.from_numpy(r).to(dev)
+    with torch.cuda.stream(stream):
+        g.set_points(2 * n, both)
+        g.rebuild_topology(2 * n, 3.0, mode=gvx.TOPO_FULL)
+        g.update_atlas()
+        g.set_points(n, td)
+        g.set_point_attribs(weight=wd, radius=rd)
+        g.splat(gvx.SPLAT_CUBIC, n, 1.0, chan_density=0)
+        ptr, nbytes = g.channel_device_ptr(0)
+        rho_t = torch.empty(nbytes // 4, dtype=torch.float32, device=dev)
+        g.sync()
+        rho_t.copy_(torch.from_numpy(g.read_channel(0).reshape(-1)))
+        g.set_points(n, pd)
+        g.set_point_attribs(weight=wd, radius=rd)
+        gp = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        gw = torch.empty(n, dtype=torch.float32, device=dev)
+        gr = torch.empty(n, dtype=torch.float32, device=dev)
+        G = torch.empty_like(rho_t)
+        fwd, bwd = [], []
+        for k in range(iters + 3):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(stream)
+            g.splat(gvx.SPLAT_CUBIC, n, 1.0, chan_density=0)
+            e[1].record(stream)
+            if k == 0:
+                g.sync()
+                G.copy_(torch.from_numpy(g.read_channel(0).reshape(-1)) - rho_t.cpu())
+            g.splat_backward(gvx.SPLAT_CUBIC, n, 1.0, G, gp, gw, gr)
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            if k >= 3:
+                fwd.append(e[0].elapsed_time(e[1]))
+                bwd.append(e[1].elapsed_time(e[2]))
+        bricks = g.info()["used_leaves"]
+    g.close()
+    f, b = sum(fwd) / len(fwd), sum(bwd) / len(bwd)
+    return {"workload": "differentiable: 1M points U[8,504)^3 in 512^3, w~U(0,1), R~U(1,3), cubic density; "
+                        "G = rho - rho*, rho* = splat of p + N(0,0.5)",
+            "points": n, "active_bricks": bricks, "fwd_ms": round(f, 4), "bwd_ms": round(b, 4),
+            "fwd_plus_bwd_ms": round(f + b, 4), "bwd_over_fwd": round(b / f, 4)}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -386,6 +449,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=0, help="smaller runs for profiling (same density)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the differentiable-workload timing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
@@ -399,6 +463,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         pool = cpu_pool(1)  # spawned before the first CUDA call
     out = run_ours(args, rank, world, pool)
+    if rank == 0 and world == 1 and not args.no_extras:
+        import torch
+
+        out["differentiable"] = run_differentiable(torch.device("cuda", 0))
     if rank == 0:
         if pool is not None:
             out["cpu_baseline"] = cpu_baseline(pool)

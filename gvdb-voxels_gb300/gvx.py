@@ -78,6 +78,7 @@ def load(path=None):
         "gvx_gather_density": ([vp, i, i, f, fp, i, i, i, i], i),
         "gvx_gather_levelset": ([vp, i, i, f, fp, i, i, i, i], i),
         "gvx_splat": ([vp, i, i, f, fp, i, i, i], i),
+        "gvx_splat_backward": ([vp, i, i, f, fp, vp, vp, vp, vp], i),
         "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
         "gvx_read_nodes": ([vp, i, vp, i64], i), "gvx_read_childlist": ([vp, i, vp, i64], i),
@@ -216,6 +217,12 @@ class Grid:
     def splat(self, mode, n, radius, trans=None, chan_density=0, chan_vel=-1, accum=False):
         self._check(self.lib.gvx_splat(self.h, mode, n, float(radius), _f3(trans), chan_density, chan_vel,
                                        int(accum)))
+
+    def splat_backward(self, mode, n, radius, dl_drho, grad_pos, grad_w, grad_r=None, trans=None):
+        """device buffers (torch tensors or raw pointers): dL/drho in the density
+        channel layout in, dL/dp (n x 3), dL/dw (n) and dL/dR (n) out"""
+        self._check(self.lib.gvx_splat_backward(self.h, mode, n, float(radius), _f3(trans), _ptr(dl_drho),
+                                                _ptr(grad_pos), _ptr(grad_w), _ptr(grad_r)))
 
     def insert_points_subcell(self, subcell, n, radius, trans=None):
         ln = ctypes.c_int(0)

@@ -170,6 +170,15 @@ gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, co
  * formed in the points' sorted order: results are deterministic. */
 gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float trans[3],
                      int chan_density, int chan_vel, int accum);
+/* Adjoint of gvx_splat's density (no counterpart in the reference).  dL_drho
+ * holds dL/drho in the density channel's brick-major layout (device memory;
+ * only interior voxels are read, an apron voxel being a copy).  Writes, in the
+ * points' original order and to device memory, dL/dp (3 floats per point),
+ * dL/dw and, when grad_r is not NULL, dL/dR per point (the CUBIC radius;
+ * the bound per-point radii if any).  Points outside the active bricks get 0.
+ * Uses the grouping of the forward splat, re-sorting if the points changed. */
+gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const float trans[3],
+                              const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r);
 /* UpdateApron(chan, boundval) / UpdateApron() (VG.h:407-408, VG.cpp:4411-4457) */
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
 gvx_status gvx_update_apron_all(gvx_grid* g);
