@@ -20,6 +20,13 @@
 // Sample convention of all modes: voxel v of the index space is sampled at the
 // integer coordinate v (as gvdbGatherDensity, cuda_gvdb_particles.cuh:705).
 #include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "gvx_grid.cuh"
 #include "gvx_ptx.cuh"
@@ -29,6 +36,7 @@ constexpr int kSplatThreads = 256;
 constexpr int kSlabWarps = 4;        // warps (brick slabs) per block of the splat
 constexpr int kSlabMinBlocks = 6;    // resident blocks per SM the register budget is sized for
 constexpr size_t kSlabTileMax = 48 * 1024;  // shared tile bytes of one warp at most
+constexpr int kBatchMaxGrids = 256;         // grids of one batched launch
 constexpr float kInvPi = 0.318309886183790671538f;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 }  // namespace
@@ -136,311 +144,356 @@ struct Tile {
 
 // One warp per (brick, z-slab): the padded brick's layers are split into
 // slabs of a.slab_layers layers, each with its own shared tile, so a warp's
-// tile is a fraction of the brick and twice as many warps stay resident.
-// Every slab sees the same candidate points in the same order, so a voxel's
-// sum does not depend on the split.
+// tile is a fraction of the brick and more warps stay resident.  Every slab
+// sees the same candidate points in the same order, so a voxel's sum does not
+// depend on the split.  splat_unit processes work unit u = slot * slabs + slab.
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
+__device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u, unsigned char* tile, uint64_t* bar,
+                                           int* s_rs_w, int* s_ro_w, uint32_t& phase, const int lane)
+{
+    using T = Tile<HAS_DEN, HAS_VEL>;
+    constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
+    // single-channel tiles go to HBM in one bulk (TMA) copy; the combined
+    // density+velocity tile is split into the two channels by vector stores
+    constexpr bool BULK = !(HAS_DEN && HAS_VEL);
+    // cubic constants of a uniform radius (per point with PPR)
+    const float R0 = a.radius, h0 = 0.5f * R0, inv_h0 = CUBIC && !PPR ? 1.0f / h0 : 0.0f;
+    const float norm0 = kInvPi * inv_h0 * inv_h0 * inv_h0, r2h0 = R0 * R0, r2l0 = fmaf(R0, R0, -r2h0);
+    const int P = a.P, P2 = P * P, P3 = P2 * P, ap = a.apron, b = a.brick;
+    const int L = a.slab_layers, S = a.slabs;
+    const uint32_t s = u / (uint32_t)S;
+    const int z0 = (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
+    const int nl = min(L, P - z0);
+    const int nvox = nl * P2;
+    const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel
+    const int leaf = a.slot_leaf[s];
+    const GvxNode* nd = a.nodes0 + leaf;
+    const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
+    const int Zlo = Oz + z0, Zhi = Oz + z0 + nl - 1;                          // world z of the slab
+
+    // ---- the 27 neighbour ranges that can reach the slab, ordered by their place in the sorted points
+    int2 rg = make_int2(0, 0);
+    bool has_nb = false;
+    if (lane < 27) {
+        const int nl_ = a.nbr[(size_t)leaf * 27 + lane];
+        if (nl_ >= 0) {
+            has_nb = a.leaf_slot[nl_] >= 0;
+            const int bz = nd->pos[2] + (lane / 9 - 1) * b;  // the neighbour's world z range [bz, bz + b)
+            if (bz - a.reach <= Zhi && bz + b - 1 + a.reach >= Zlo) rg = a.leaf_range[nl_];
+        }
+    }
+    const uint32_t nbmask = __ballot_sync(kFull, has_nb);
+    const int len = max(0, rg.y - rg.x);
+    int rank = 0, off = 0, total = 0, m = 0;
+    for (int k = 0; k < 27; k++) {
+        const int sk = __shfl_sync(kFull, rg.x, k), lk = __shfl_sync(kFull, len, k);
+        if (lk > 0) {
+            m++;
+            total += lk;
+            if (sk < rg.x) {
+                rank++;
+                off += lk;
+            }
+        }
+    }
+    if (lane < 27 && len > 0) {
+        s_rs_w[rank] = rg.x;
+        s_ro_w[rank] = off;
+    }
+    if (lane == 0) s_ro_w[m] = total;
+
+    // ---- tile: previous values (accumulate) or zeros
+    if (a.accum) {
+        if (BULK) {
+            if (lane == 0) {
+                const uint32_t nb = (uint32_t)T::bytes(nvox);
+                mbar_expect_tx(bar, nb);
+                if (HAS_DEN) bulk_g2s(tile, a.den + gofs, nb, bar);
+                else bulk_g2s(tile, a.vel + gofs, nb, bar);
+            }
+            if (!mbar_wait_bounded(bar, phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
+            phase ^= 1u;
+        } else {
+            float4* tv = (float4*)tile;
+            for (int i = lane; i < nvox; i += 32) {
+                const float4 v = a.vel[gofs + i];
+                tv[i] = make_float4(v.x, v.y, v.z, a.den[gofs + i]);
+            }
+        }
+    } else {
+        for (int i = lane; i < nvox; i += 32) T::set(tile, i, 0.0f);
+    }
+    __syncwarp();
+
+    // ---- candidates, 32 at a time, in sorted order.  Each lane tests one
+    // candidate and sizes the cells of its footprint in the slab (a cell = an
+    // x pair of a (y, z) row); the cells of all hits are then dealt to the
+    // lanes 32 at a time, and updates are applied point by point in sorted
+    // order, so every voxel sums its contributions in the same order in every
+    // brick that holds it.
+    for (int base = 0; base < total; base += 32) {
+        const int v = base + lane;
+        int idx = -1;
+        if (v < total) {
+            int lo = 0, hi = m - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_ro_w[mid] <= v)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            idx = s_rs_w[lo] + (v - s_ro_w[lo]);
+        }
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t box0 = 0u, box1 = 0u, magic = 0u;  // footprint in slab-tile coordinates, 8 bits a bound
+        int ncell = 0;
+        if (idx >= 0) {
+            p = a.spos[idx];
+            if (HAS_VEL || PPR) uv = a.svel[idx];
+            int xl, xh, yl, yh, zl, zh;
+            if (!CUBIC) {
+                const int x0 = (int)floorf(p.x) - Ox, y0 = (int)floorf(p.y) - Oy, zb = (int)floorf(p.z) - Zlo;
+                xl = max(x0, 0), xh = min(x0 + 1, P - 1);
+                yl = max(y0, 0), yh = min(y0 + 1, P - 1);
+                zl = max(zb, 0), zh = min(zb + 1, nl - 1);
+            } else {
+                // voxels strictly inside (p - R, p + R) on every axis
+                const float R = PPR ? uv.w : R0;
+                if (PPR && R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
+                xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
+                yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
+                zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
+            }
+            if (xl <= xh && yl <= yh && zl <= zh) {
+                const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1;
+                ncell = nxp * ny * (zh - zl + 1);
+                box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
+                box1 = (uint32_t)zl | ((uint32_t)zh << 8);
+                // ceil(2^15 / n): (c * magic) >> 15 == c / n for c <= 2^15 / n (cells <= 7*14*14 here)
+                magic = ((32767u + (uint32_t)nxp) / (uint32_t)nxp) | (((32767u + (uint32_t)ny) / (uint32_t)ny) << 16);
+            }
+        }
+        // inclusive scan of the cell counts over the lanes
+        int cend = ncell;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, cend, o);
+            if (lane >= o) cend += t;
+        }
+        const int ctot = __shfl_sync(kFull, cend, 31);
+        const int cstart = cend - ncell;
+        for (int g0 = 0; g0 < ctot; g0 += 32) {
+            const int g = g0 + lane;
+            const bool act = g < ctot;
+            // the point dealing this cell: the first lane whose cells end after g
+            int lo = 0, hi = 31;
+#pragma unroll
+            for (int it = 0; it < 5; it++) {
+                const int mid = (lo + hi) >> 1;
+                if (__shfl_sync(kFull, cend, mid) > g)
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            const int j = lo;
+            const float px = __shfl_sync(kFull, p.x, j), py = __shfl_sync(kFull, p.y, j);
+            const float pz = __shfl_sync(kFull, p.z, j), pw = __shfl_sync(kFull, p.w, j);
+            float ux = 0.f, uy = 0.f, uz = 0.f;
+            if (HAS_VEL) {
+                ux = __shfl_sync(kFull, uv.x, j);
+                uy = __shfl_sync(kFull, uv.y, j);
+                uz = __shfl_sync(kFull, uv.z, j);
+            }
+            const uint32_t b0 = __shfl_sync(kFull, box0, j), b1 = __shfl_sync(kFull, box1, j);
+            const uint32_t mg = __shfl_sync(kFull, magic, j);
+            const int cell = g - __shfl_sync(kFull, cstart, j);
+            const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
+            const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
+            const int zl = (int)(b1 & 255u);
+            const int nxp = (xh - xl + 2) >> 1, ny = (int)(b0 >> 24) - yl + 1;
+            const int r = (int)(((uint32_t)cell * (mg & 0xFFFFu)) >> 15);
+            const int zz = (int)(((uint32_t)r * (mg >> 16)) >> 15);
+            const int lx = xl + 2 * (cell - r * nxp), ly = yl + (r - zz * ny), lz = zl + zz;
+            // the lane's two voxels (lx, lx + 1) of row (ly, lz): index and value
+            int vi0 = -1, vi1 = -1;
+            float w0 = 0.f, w1 = 0.f;
+            if (act) {
+                const int t0 = (lz * P + ly) * P + lx;
+                if (!CUBIC) {
+                    const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
+                    const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
+                    const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
+                    const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
+                    w0 = pw * wxa * wyz;
+                    vi0 = t0;
+                    if (lx + 1 <= xh) {
+                        w1 = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
+                        vi1 = t0 + 1;
+                    }
+                } else {
+                    // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
+                    // support R = 2h.  Along the row R^2 - d^2 is formed from an error-free
+                    // c = R^2 - dy^2 - dz^2 (two-product, two-sum) so that the outer branch
+                    // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
+                    // accuracy up to the edge of the support.
+                    float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
+                    if (PPR) {
+                        R = pR;
+                        h = 0.5f * R;
+                        inv_h = 1.0f / h;
+                        norm = kInvPi * inv_h * inv_h * inv_h;
+                        r2h = R * R;
+                        r2l = fmaf(R, R, -r2h);
+                    }
+                    norm *= pw;
+                    const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
+                    const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
+                    const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
+                    const float syz = qy + qz;
+                    float bv = syz - qy;
+                    const float e1 = (qy - (syz - bv)) + (qz - bv);
+                    const float c1 = r2h - syz;
+                    bv = c1 - r2h;
+                    const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
+                    const float cl = e2 + r2l - ((ey + ez) + e1);
+                    if (c1 + cl > 0.0f) {
+#pragma unroll
+                        for (int k = 0; k < 2; k++) {
+                            if (lx + k > xh) break;
+                            const float dx = (float)(lx + k + Ox) - px;
+                            const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
+                            if (t <= 0.0f) continue;
+                            const float d2 = fmaf(dx, dx, syz);
+                            const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                            const float q = d * inv_h;
+                            const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
+                            const float uu = __fdividef(t, h * (R + d));               // 2 - q
+                            const float wv = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
+                            if (k == 0) {
+                                w0 = wv;
+                                vi0 = t0;
+                            } else {
+                                w1 = wv;
+                                vi1 = t0 + 1;
+                            }
+                        }
+                    }
+                }
+            }
+            // apply point by point: the lanes of one point touch distinct voxels
+            const int jprev = __shfl_up_sync(kFull, j, 1);
+            const uint32_t first = __ballot_sync(kFull, act && (lane == 0 || jprev != j));
+            const int npts = __popc(first);
+            const int pr = __popc(first & (0xFFFFFFFFu >> (31 - lane))) - 1;
+            for (int ph = 0; ph < npts; ph++) {
+                if (act && pr == ph) {
+                    if (vi0 >= 0) T::add(tile, vi0, w0, ux, uy, uz);
+                    if (vi1 >= 0) T::add(tile, vi1, w1, ux, uy, uz);
+                }
+                __syncwarp();
+            }
+        }
+    }
+
+    // ---- apron voxels with no neighbouring brick take the boundary value (0)
+    if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
+        for (int i = lane; i < nvox; i += 32) {
+            const int z = z0 + i / P2, r = i % P2, y = r / P, x = r % P;
+            const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
+            const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
+            const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
+            if (!(dx | dy | dz)) continue;  // interior voxel
+            if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
+            T::set(tile, i, a.boundval);
+        }
+        __syncwarp();
+    }
+
+    // ---- out to HBM
+    if (BULK) {
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            if (HAS_DEN) bulk_s2g(a.den + gofs, tile, (uint32_t)T::bytes(nvox));
+            else bulk_s2g(a.vel + gofs, tile, (uint32_t)T::bytes(nvox));
+            bulk_commit();
+            bulk_wait_read_all();
+        }
+        __syncwarp();
+    } else {
+        const float4* tv = (const float4*)tile;
+        float* dg = a.den + gofs;
+        float4* vg = a.vel + gofs;
+        for (int i = lane; i < nvox; i += 32) {
+            const float4 o = tv[i];
+            dg[i] = o.w;
+            vg[i] = make_float4(o.x, o.y, o.z, 0.0f);
+        }
+        __syncwarp();
+    }
+}
+
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
 __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(SplatArgs a)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
-    constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
-    // cubic constants of a uniform radius (per point with PPR)
-    const float R0 = a.radius, h0 = 0.5f * R0, inv_h0 = CUBIC && !PPR ? 1.0f / h0 : 0.0f;
-    const float norm0 = kInvPi * inv_h0 * inv_h0 * inv_h0, r2h0 = R0 * R0, r2l0 = fmaf(R0, R0, -r2h0);
     extern __shared__ __align__(128) unsigned char smem[];
-    const int P = a.P, P2 = P * P, P3 = P2 * P, ap = a.apron, b = a.brick;
-    const int L = a.slab_layers, S = a.slabs;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char* tile = smem + (size_t)wid * T::bytes(L * P2);
+    unsigned char* tile = smem + (size_t)wid * T::bytes(a.slab_layers * a.P * a.P);
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
     __shared__ int s_rs[kSlabWarps][28];
     __shared__ int s_ro[kSlabWarps][28];
-    // single-channel tiles go to HBM in one bulk (TMA) copy; the combined
-    // density+velocity tile is split into the two channels by vector stores
-    constexpr bool BULK = !(HAS_DEN && HAS_VEL);
-
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
     }
     __syncwarp();
     uint32_t phase = 0;
-    const uint32_t units = a.nslots * (uint32_t)S;
+    const uint32_t units = a.nslots * (uint32_t)a.slabs;
     const uint32_t nw = gridDim.x * kSlabWarps;
-    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw) {
-        const uint32_t s = u / (uint32_t)S;
-        const int z0 = (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
-        const int nl = min(L, P - z0);
-        const int nvox = nl * P2;
-        const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel
-        const int leaf = a.slot_leaf[s];
-        const GvxNode* nd = a.nodes0 + leaf;
-        const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
-        const int Zlo = Oz + z0, Zhi = Oz + z0 + nl - 1;                          // world z of the slab
+    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw)
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], phase, lane);
+    if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
+}
 
-        // ---- the 27 neighbour ranges that can reach the slab, ordered by their place in the sorted points
-        int2 rg = make_int2(0, 0);
-        bool has_nb = false;
-        if (lane < 27) {
-            const int nl_ = a.nbr[(size_t)leaf * 27 + lane];
-            if (nl_ >= 0) {
-                has_nb = a.leaf_slot[nl_] >= 0;
-                const int bz = nd->pos[2] + (lane / 9 - 1) * b;  // the neighbour's world z range [bz, bz + b)
-                if (bz - a.reach <= Zhi && bz + b - 1 + a.reach >= Zlo) rg = a.leaf_range[nl_];
-            }
-        }
-        const uint32_t nbmask = __ballot_sync(kFull, has_nb);
-        const int len = max(0, rg.y - rg.x);
-        int rank = 0, off = 0, total = 0, m = 0;
-        for (int k = 0; k < 27; k++) {
-            const int sk = __shfl_sync(kFull, rg.x, k), lk = __shfl_sync(kFull, len, k);
-            if (lk > 0) {
-                m++;
-                total += lk;
-                if (sk < rg.x) {
-                    rank++;
-                    off += lk;
-                }
-            }
-        }
-        if (lane < 27 && len > 0) {
-            s_rs[wid][rank] = rg.x;
-            s_ro[wid][rank] = off;
-        }
-        if (lane == 0) s_ro[wid][m] = total;
-
-        // ---- tile: previous values (accumulate) or zeros
-        if (a.accum) {
-            if (BULK) {
-                if (lane == 0) {
-                    const uint32_t nb = (uint32_t)T::bytes(nvox);
-                    mbar_expect_tx(&s_bar[wid], nb);
-                    if (HAS_DEN) bulk_g2s(tile, a.den + gofs, nb, &s_bar[wid]);
-                    else bulk_g2s(tile, a.vel + gofs, nb, &s_bar[wid]);
-                }
-                if (!mbar_wait_bounded(&s_bar[wid], phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
-                phase ^= 1u;
-            } else {
-                float4* tv = (float4*)tile;
-                for (int i = lane; i < nvox; i += 32) {
-                    const float4 v = a.vel[gofs + i];
-                    tv[i] = make_float4(v.x, v.y, v.z, a.den[gofs + i]);
-                }
-            }
-        } else {
-            for (int i = lane; i < nvox; i += 32) T::set(tile, i, 0.0f);
-        }
-        __syncwarp();
-
-        // ---- candidates, 32 at a time, in sorted order.  Each lane tests one
-        // candidate and sizes the cells of its footprint in the slab (a cell = an
-        // x pair of a (y, z) row); the cells of all hits are then dealt to the
-        // lanes 32 at a time, and updates are applied point by point in sorted
-        // order, so every voxel sums its contributions in the same order in every
-        // brick that holds it.
-        for (int base = 0; base < total; base += 32) {
-            const int v = base + lane;
-            int idx = -1;
-            if (v < total) {
-                int lo = 0, hi = m - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (s_ro[wid][mid] <= v)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                idx = s_rs[wid][lo] + (v - s_ro[wid][lo]);
-            }
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
-            uint32_t box0 = 0u, box1 = 0u, magic = 0u;  // footprint in slab-tile coordinates, 8 bits a bound
-            int ncell = 0;
-            if (idx >= 0) {
-                p = a.spos[idx];
-                if (HAS_VEL || PPR) uv = a.svel[idx];
-                int xl, xh, yl, yh, zl, zh;
-                if (!CUBIC) {
-                    const int x0 = (int)floorf(p.x) - Ox, y0 = (int)floorf(p.y) - Oy, zb = (int)floorf(p.z) - Zlo;
-                    xl = max(x0, 0), xh = min(x0 + 1, P - 1);
-                    yl = max(y0, 0), yh = min(y0 + 1, P - 1);
-                    zl = max(zb, 0), zh = min(zb + 1, nl - 1);
-                } else {
-                    // voxels strictly inside (p - R, p + R) on every axis
-                    const float R = PPR ? uv.w : R0;
-                    if (PPR && R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
-                    xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
-                    yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
-                    zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
-                }
-                if (xl <= xh && yl <= yh && zl <= zh) {
-                    const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1;
-                    ncell = nxp * ny * (zh - zl + 1);
-                    box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
-                    box1 = (uint32_t)zl | ((uint32_t)zh << 8);
-                    // ceil(2^15 / n): (c * magic) >> 15 == c / n for c <= 2^15 / n (cells <= 7*14*14 here)
-                    magic = ((32767u + (uint32_t)nxp) / (uint32_t)nxp) | (((32767u + (uint32_t)ny) / (uint32_t)ny) << 16);
-                }
-            }
-            // inclusive scan of the cell counts over the lanes
-            int cend = ncell;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(kFull, cend, o);
-                if (lane >= o) cend += t;
-            }
-            const int ctot = __shfl_sync(kFull, cend, 31);
-            const int cstart = cend - ncell;
-            for (int g0 = 0; g0 < ctot; g0 += 32) {
-                const int g = g0 + lane;
-                const bool act = g < ctot;
-                // the point dealing this cell: the first lane whose cells end after g
-                int lo = 0, hi = 31;
-#pragma unroll
-                for (int it = 0; it < 5; it++) {
-                    const int mid = (lo + hi) >> 1;
-                    if (__shfl_sync(kFull, cend, mid) > g)
-                        hi = mid;
-                    else
-                        lo = mid + 1;
-                }
-                const int j = lo;
-                const float px = __shfl_sync(kFull, p.x, j), py = __shfl_sync(kFull, p.y, j);
-                const float pz = __shfl_sync(kFull, p.z, j), pw = __shfl_sync(kFull, p.w, j);
-                float ux = 0.f, uy = 0.f, uz = 0.f;
-                if (HAS_VEL) {
-                    ux = __shfl_sync(kFull, uv.x, j);
-                    uy = __shfl_sync(kFull, uv.y, j);
-                    uz = __shfl_sync(kFull, uv.z, j);
-                }
-                const uint32_t b0 = __shfl_sync(kFull, box0, j), b1 = __shfl_sync(kFull, box1, j);
-                const uint32_t mg = __shfl_sync(kFull, magic, j);
-                const int cell = g - __shfl_sync(kFull, cstart, j);
-                const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
-                const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
-                const int zl = (int)(b1 & 255u);
-                const int nxp = (xh - xl + 2) >> 1, ny = (int)(b0 >> 24) - yl + 1;
-                const int r = (int)(((uint32_t)cell * (mg & 0xFFFFu)) >> 15);
-                const int zz = (int)(((uint32_t)r * (mg >> 16)) >> 15);
-                const int lx = xl + 2 * (cell - r * nxp), ly = yl + (r - zz * ny), lz = zl + zz;
-                // the lane's two voxels (lx, lx + 1) of row (ly, lz): index and value
-                int vi0 = -1, vi1 = -1;
-                float w0 = 0.f, w1 = 0.f;
-                if (act) {
-                    const int t0 = (lz * P + ly) * P + lx;
-                    if (!CUBIC) {
-                        const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
-                        const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
-                        const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
-                        const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
-                        w0 = pw * wxa * wyz;
-                        vi0 = t0;
-                        if (lx + 1 <= xh) {
-                            w1 = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
-                            vi1 = t0 + 1;
-                        }
-                    } else {
-                        // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
-                        // support R = 2h.  Along the row R^2 - d^2 is formed from an error-free
-                        // c = R^2 - dy^2 - dz^2 (two-product, two-sum) so that the outer branch
-                        // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
-                        // accuracy up to the edge of the support.
-                        float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
-                        if (PPR) {
-                            R = pR;
-                            h = 0.5f * R;
-                            inv_h = 1.0f / h;
-                            norm = kInvPi * inv_h * inv_h * inv_h;
-                            r2h = R * R;
-                            r2l = fmaf(R, R, -r2h);
-                        }
-                        norm *= pw;
-                        const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
-                        const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
-                        const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
-                        const float syz = qy + qz;
-                        float bv = syz - qy;
-                        const float e1 = (qy - (syz - bv)) + (qz - bv);
-                        const float c1 = r2h - syz;
-                        bv = c1 - r2h;
-                        const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
-                        const float cl = e2 + r2l - ((ey + ez) + e1);
-                        if (c1 + cl > 0.0f) {
-#pragma unroll
-                            for (int k = 0; k < 2; k++) {
-                                if (lx + k > xh) break;
-                                const float dx = (float)(lx + k + Ox) - px;
-                                const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
-                                if (t <= 0.0f) continue;
-                                const float d2 = fmaf(dx, dx, syz);
-                                const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                                const float q = d * inv_h;
-                                const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
-                                const float uu = __fdividef(t, h * (R + d));               // 2 - q
-                                const float wv = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
-                                if (k == 0) {
-                                    w0 = wv;
-                                    vi0 = t0;
-                                } else {
-                                    w1 = wv;
-                                    vi1 = t0 + 1;
-                                }
-                            }
-                        }
-                    }
-                }
-                // apply point by point: the lanes of one point touch distinct voxels
-                const int jprev = __shfl_up_sync(kFull, j, 1);
-                const uint32_t first = __ballot_sync(kFull, act && (lane == 0 || jprev != j));
-                const int npts = __popc(first);
-                const int pr = __popc(first & (0xFFFFFFFFu >> (31 - lane))) - 1;
-                for (int ph = 0; ph < npts; ph++) {
-                    if (act && pr == ph) {
-                        if (vi0 >= 0) T::add(tile, vi0, w0, ux, uy, uz);
-                        if (vi1 >= 0) T::add(tile, vi1, w1, ux, uy, uz);
-                    }
-                    __syncwarp();
-                }
-            }
-        }
-
-        // ---- apron voxels with no neighbouring brick take the boundary value (0)
-        if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
-            for (int i = lane; i < nvox; i += 32) {
-                const int z = z0 + i / P2, r = i % P2, y = r / P, x = r % P;
-                const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
-                const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
-                const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
-                if (!(dx | dy | dz)) continue;  // interior voxel
-                if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
-                T::set(tile, i, a.boundval);
-            }
-            __syncwarp();
-        }
-
-        // ---- out to HBM
-        if (BULK) {
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) {
-                if (HAS_DEN) bulk_s2g(a.den + gofs, tile, (uint32_t)T::bytes(nvox));
-                else bulk_s2g(a.vel + gofs, tile, (uint32_t)T::bytes(nvox));
-                bulk_commit();
-                bulk_wait_read_all();
-            }
-            __syncwarp();
-        } else {
-            const float4* tv = (const float4*)tile;
-            float* dg = a.den + gofs;
-            float4* vg = a.vel + gofs;
-            for (int i = lane; i < nvox; i += 32) {
-                const float4 o = tv[i];
-                dg[i] = o.w;
-                vg[i] = make_float4(o.x, o.y, o.z, 0.0f);
-            }
-            __syncwarp();
-        }
+// The same work over many grids in one persistent launch: the units of grid
+// k are [ustart[k], ustart[k+1]) of one global range, dealt to the warps in
+// stride; every grid has the same brick and tile shape (slab_layers, P).
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
+__global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
+    k_splat_batch(const SplatArgs* __restrict__ args, const uint32_t* __restrict__ ustart, int ngrids)
+{
+    using T = Tile<HAS_DEN, HAS_VEL>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned char* tile = smem + (size_t)wid * T::bytes(args[0].slab_layers * args[0].P * args[0].P);
+    __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
+    __shared__ int s_rs[kSlabWarps][28];
+    __shared__ int s_ro[kSlabWarps][28];
+    __shared__ uint32_t s_us[kBatchMaxGrids + 1];
+    for (int i = threadIdx.x; i <= ngrids; i += blockDim.x) s_us[i] = ustart[i];
+    if (lane == 0) {
+        mbar_init(&s_bar[wid], 1);
+        mbar_fence_init();
     }
-    if (BULK && lane == 0) bulk_wait_all();
+    __syncthreads();
+    uint32_t phase = 0;
+    const uint32_t total = s_us[ngrids];
+    const uint32_t nw = gridDim.x * kSlabWarps;
+    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < total; u += nw) {
+        int lo = 0, hi = ngrids - 1;  // the grid k with ustart[k] <= u < ustart[k+1]
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_us[mid] <= u)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid], s_ro[wid],
+                                                phase, lane);
+    }
+    if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
 
 // ScatterDensity, race-free: own points only, into the own padded tile
@@ -561,22 +614,51 @@ static gvx_status check_splat_state(gvx_grid* g, const char* what)
     return GVX_OK;
 }
 
-static int sm_count(gvx_grid* g)
+static int sm_count(int device)
 {
     int v = 0;
-    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, g->device);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
     return v > 0 ? v : 152;
 }
 
+// kernel variant: channel set x mode x per-point radius
+struct SplatKind {
+    bool has_d, has_v, ppr;
+    int mode;
+    bool operator==(const SplatKind& o) const
+    {
+        return has_d == o.has_d && has_v == o.has_v && ppr == o.ppr && mode == o.mode;
+    }
+};
+
 template <bool D, bool V>
-static void* slab_kernel(int mode, bool ppr)
+static void* pick_kernel(const SplatKind& k, bool batch)
 {
-    if (mode == GVX_SPLAT_TRILINEAR) return (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR, false>;
-    return ppr ? (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, true> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false>;
+    if (k.mode == GVX_SPLAT_TRILINEAR)
+        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_TRILINEAR, false>
+                     : (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR, false>;
+    if (k.ppr)
+        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, true> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, true>;
+    return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, false> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false>;
 }
 
-gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
-                         int accum)
+static void* splat_kernel(const SplatKind& k, bool batch)
+{
+    return k.has_d ? (k.has_v ? pick_kernel<true, true>(k, batch) : pick_kernel<true, false>(k, batch))
+                   : pick_kernel<false, true>(k, batch);
+}
+
+// the largest slab (in layers) whose tile fits the per-warp budget, at most `want`
+static int clamp_layers(int P, size_t eb, int want)
+{
+    const int fit = (int)(kSlabTileMax / ((size_t)P * P * eb));
+    return std::min(std::min(want, P), fit);
+}
+
+// validation, InsertPoints grouping and the kernel arguments of one grid's splat;
+// layers <= 0 picks the default slab height (half the padded brick)
+static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
+                                int chan_v, int accum, int layers, SplatArgs* out, SplatKind* kind)
 {
     gvx_status rc = check_splat_state(g, "Splat");
     if (rc) return rc;
@@ -609,17 +691,15 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     const bool need_svel = has_v || ppr;
     rc = gvx_prepare_points(g, n, trans, need_svel);
     if (rc) return rc;
-
-    const int P = g->P, P2 = P * P;
+    const int P = g->P;
     const size_t eb = has_v ? 16 : 4;
-    // slab height: half the padded brick, fewer layers where a half does not fit the tile budget
-    const int layers = std::min((P + 1) / 2, (int)(kSlabTileMax / ((size_t)P2 * eb)));
+    layers = clamp_layers(P, eb, layers > 0 ? layers : (P + 1) / 2);
     if (layers < 1) {
         gvx_set_error("Splat: a %d^2 layer of the padded brick exceeds the shared tile budget", P);
         return GVX_ERR_UNSUPPORTED;
     }
-    const size_t smem = (size_t)layers * P2 * eb * kSlabWarps;
-    SplatArgs a;
+    SplatArgs& a = *out;
+    memset(&a, 0, sizeof(a));
     a.brick = g->brick;
     a.P = P;
     a.apron = g->apron;
@@ -642,35 +722,417 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
     a.accum = accum != 0;
     a.boundval = 0.0f;
     a.err = g->d_err.as<uint32_t>();
-    // apron state after the splat: exact copies with boundary value 0, unless an
-    // accumulating splat started from an apron that was not a valid copy
+    kind->has_d = has_d;
+    kind->has_v = has_v;
+    kind->ppr = ppr;
+    kind->mode = mode;
+    return GVX_OK;
+}
+
+// apron state after the splat: exact copies with boundary value 0, unless an
+// accumulating splat started from an apron that was not a valid copy
+static void splat_finish(gvx_grid* g, int chan_d, int chan_v, int accum)
+{
     bool valid_after = true;
-    if (a.accum) {
-        if (has_d) valid_after &= g->ch[chan_d].apron_valid && g->ch[chan_d].apron_bv == 0.0f;
-        if (has_v) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
+    if (accum) {
+        if (chan_d >= 0) valid_after &= g->ch[chan_d].apron_valid && g->ch[chan_d].apron_bv == 0.0f;
+        if (chan_v >= 0) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
     }
-    if (a.nslots == 0) return GVX_OK;
-    void* kern = has_d ? (has_v ? slab_kernel<true, true>(mode, ppr) : slab_kernel<true, false>(mode, ppr))
-                       : slab_kernel<false, true>(mode, ppr);
+    for (int c : {chan_d, chan_v}) {
+        if (c < 0) continue;
+        g->ch[c].apron_valid = valid_after;
+        g->ch[c].apron_bv = 0.0f;
+    }
+}
+
+static size_t splat_smem(const SplatArgs& a, const SplatKind& k)
+{
+    return (size_t)a.slab_layers * a.P * a.P * (k.has_v ? 16 : 4) * kSlabWarps;
+}
+
+gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
+                         int accum)
+{
+    SplatArgs a;
+    SplatKind kind;
+    gvx_status rc = splat_prepare(g, mode, n, radius, trans, chan_d, chan_v, accum, 0, &a, &kind);
+    if (rc) return rc;
+    if (a.nslots) {
+        const size_t smem = splat_smem(a, kind);
+        void* kern = splat_kernel(kind, false);
+        GVX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSlabWarps * 32, smem));
+        const uint64_t units = (uint64_t)a.nslots * a.slabs;
+        const uint64_t ctas_needed = (units + kSlabWarps - 1) / kSlabWarps;
+        const uint32_t grid =
+            (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g->device) * std::max(per_sm, 1));
+        void* args[] = {&a};
+        GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kSlabWarps * 32), args, smem, g->stream));
+        g->launches++;
+    }
+    splat_finish(g, chan_d, chan_v, accum);
+    return GVX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched multi-grid splat: the splats of many grids (same brick shape and
+// channel kinds) in ONE persistent launch, optionally captured in a CUDA graph
+// and replayed while the grids' buffers stay where they are, with an
+// autotuner over the slab height and the CTAs per SM (cached per GPU).
+
+struct BatchTuning {
+    int layers = 0, blocks_per_sm = 0;
+    float ms = 0.f;
+};
+
+static std::mutex g_tune_mu;
+static std::map<std::string, BatchTuning> g_tune_cache;
+
+struct gvx_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<gvx_grid*> grids;
+    DevBuf d_args, d_ustart;
+    std::vector<SplatArgs> cap_args;   // arguments of the captured graph
+    std::vector<uint32_t> cap_ustart;
+    SplatKind cap_kind{};
+    int cap_blocks = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev = nullptr;
+    BatchTuning tuning;
+    int64_t launches = 0;
+};
+
+static void batch_drop_graph(gvx_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->cap_args.clear();
+}
+
+static std::string tune_key(int device, const SplatArgs& a, const SplatKind& k)
+{
+    cudaDeviceProp prop;
+    memset(&prop, 0, sizeof(prop));
+    cudaGetDeviceProperties(&prop, device);
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s|%d|P%d|m%d|d%d|v%d|r%d", prop.name, device, a.P, k.mode, (int)k.has_d,
+             (int)k.has_v, (int)k.ppr);
+    return buf;
+}
+
+// one launch of the batch kernel over args/ustart already on the device
+static gvx_status batch_launch(gvx_batch* b, const SplatKind& k, const SplatArgs& a0, int ngrids, int blocks)
+{
+    const size_t smem = splat_smem(a0, k);
+    void* kern = splat_kernel(k, true);
+    const SplatArgs* dargs = b->d_args.as<SplatArgs>();
+    const uint32_t* dus = b->d_ustart.as<uint32_t>();
+    void* args[] = {(void*)&dargs, (void*)&dus, (void*)&ngrids};
+    GVX_CK(cudaLaunchKernel(kern, dim3(blocks), dim3(kSlabWarps * 32), args, smem, b->stream));
+    b->launches++;
+    return GVX_OK;
+}
+
+// argument table of every grid for a slab height, and the unit ranges
+static gvx_status batch_tables(gvx_batch* b, int mode, float radius, int chan_d, int chan_v, int accum, int layers,
+                               std::vector<SplatArgs>& args, std::vector<uint32_t>& ustart, SplatKind& kind)
+{
+    args.resize(b->grids.size());
+    ustart.assign(b->grids.size() + 1, 0u);
+    uint64_t tot = 0;
+    for (size_t i = 0; i < b->grids.size(); i++) {
+        gvx_grid* g = b->grids[i];
+        const int n = g->group_valid ? g->group_n : g->pts.n;
+        const float* t = g->group_valid ? g->group_trans : nullptr;
+        SplatKind k;
+        gvx_status rc = splat_prepare(g, mode, n, radius, t, chan_d, chan_v, accum, layers, &args[i], &k);
+        if (rc) return rc;
+        if (i == 0) {
+            kind = k;
+        } else if (!(k == kind) || args[i].P != args[0].P || args[i].slab_layers != args[0].slab_layers) {
+            gvx_set_error("BatchSplat: grid %zu differs from grid 0 in brick shape, channels or radius kind", i);
+            return GVX_ERR_INVALID_ARG;
+        }
+        ustart[i] = (uint32_t)tot;
+        tot += (uint64_t)args[i].nslots * args[i].slabs;
+        if (tot >= (1ull << 32)) {
+            gvx_set_error("BatchSplat: more than 2^32 work units");
+            return GVX_ERR_CAPACITY;
+        }
+    }
+    ustart[b->grids.size()] = (uint32_t)tot;
+    return GVX_OK;
+}
+
+static gvx_status batch_upload(gvx_batch* b, const std::vector<SplatArgs>& args, const std::vector<uint32_t>& ustart)
+{
+    GVX_CK(gvx_ensure(b->d_args, args.size() * sizeof(SplatArgs)));
+    GVX_CK(gvx_ensure(b->d_ustart, ustart.size() * sizeof(uint32_t)));
+    GVX_CK(cudaMemcpyAsync(b->d_args.p, args.data(), args.size() * sizeof(SplatArgs), cudaMemcpyHostToDevice,
+                           b->stream));
+    GVX_CK(cudaMemcpyAsync(b->d_ustart.p, ustart.data(), ustart.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           b->stream));
+    return GVX_OK;
+}
+
+static gvx_status batch_max_blocks(gvx_batch* b, const SplatKind& k, const SplatArgs& a0, int* per_sm)
+{
+    void* kern = splat_kernel(k, true);
+    const size_t smem = splat_smem(a0, k);
     GVX_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSlabWarps * 32, smem));
-    const uint64_t units = (uint64_t)a.nslots * a.slabs;
-    const uint64_t ctas_needed = (units + kSlabWarps - 1) / kSlabWarps;
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g) * std::max(per_sm, 1));
-    void* args[] = {&a};
-    GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kSlabWarps * 32), args, smem, g->stream));
-    g->launches++;
-    if (has_d) {
-        g->ch[chan_d].apron_valid = valid_after;
-        g->ch[chan_d].apron_bv = 0.0f;
+    GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, kSlabWarps * 32, smem));
+    *per_sm = std::max(*per_sm, 1);
+    return GVX_OK;
+}
+
+// tries the candidate (slab height, CTAs per SM) pairs on the live batch and
+// keeps the fastest; each candidate: one warm-up, then the mean of two timed runs
+static gvx_status batch_tune(gvx_batch* b, int mode, float radius, int chan_d, int chan_v, BatchTuning* best)
+{
+    const int P = b->grids[0]->P;
+    const int cand_layers[3] = {(P + 1) / 2, P, (P + 2) / 3};
+    cudaEvent_t e0, e1;
+    GVX_CK(cudaEventCreate(&e0));
+    GVX_CK(cudaEventCreate(&e1));
+    best->ms = 1e30f;
+    gvx_status rc = GVX_OK;
+    for (int li = 0; li < 3 && rc == GVX_OK; li++) {
+        std::vector<SplatArgs> args;
+        std::vector<uint32_t> us;
+        SplatKind k;
+        rc = batch_tables(b, mode, radius, chan_d, chan_v, 0, cand_layers[li], args, us, k);
+        if (rc) break;
+        if (li > 0 && args[0].slab_layers == best->layers) continue;  // clamped to a height already tried
+        rc = batch_upload(b, args, us);
+        if (rc) break;
+        int per_sm = 1;
+        rc = batch_max_blocks(b, k, args[0], &per_sm);
+        if (rc) break;
+        const int sms = sm_count(b->device);
+        for (int bp : {per_sm, std::max(1, (per_sm + 1) / 2)}) {
+            const int blocks = sms * bp;
+            float ms = 0.f;
+            for (int it = 0; it < 3 && rc == GVX_OK; it++) {
+                if (it == 1) cudaEventRecord(e0, b->stream);
+                rc = batch_launch(b, k, args[0], (int)args.size(), blocks);
+            }
+            if (rc) break;
+            cudaEventRecord(e1, b->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = gvx_cuda_fail(cudaGetLastError(), "autotune");
+                break;
+            }
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms *= 0.5f;
+            if (ms < best->ms) {
+                best->ms = ms;
+                best->layers = args[0].slab_layers;
+                best->blocks_per_sm = bp;
+            }
+            if (bp == 1) break;
+        }
     }
-    if (has_v) {
-        g->ch[chan_v].apron_valid = valid_after;
-        g->ch[chan_v].apron_bv = 0.0f;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" {
+
+gvx_status gvx_batch_create(int device, gvx_batch** out)
+{
+    if (!out) {
+        gvx_set_error("gvx_batch_create: null output");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    GVX_CK(cudaSetDevice(device));
+    gvx_batch* b = new gvx_batch();
+    b->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        delete b;
+        return gvx_cuda_fail(e, "gvx_batch_create");
+    }
+    b->own_stream = true;
+    *out = b;
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_destroy(gvx_batch* b)
+{
+    if (!b) return GVX_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graph(b);
+    gvx_free(b->d_args);
+    gvx_free(b->d_ustart);
+    if (b->ev) cudaEventDestroy(b->ev);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_set_stream(gvx_batch* b, void* stream)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaSetDevice(b->device));
+    GVX_CK(cudaStreamSynchronize(b->stream));
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    b->stream = (cudaStream_t)stream;
+    b->own_stream = false;
+    batch_drop_graph(b);
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count)
+{
+    if (!b || (count > 0 && !grids) || count < 0 || count > kBatchMaxGrids) {
+        gvx_set_error("BatchSetGrids: need 0..%d grids", kBatchMaxGrids);
+        return GVX_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < count; i++) {
+        if (!grids[i] || grids[i]->device != b->device) {
+            gvx_set_error("BatchSetGrids: grid %d is null or on another device", i);
+            return GVX_ERR_INVALID_ARG;
+        }
+    }
+    b->grids.assign(grids, grids + count);
+    batch_drop_graph(b);
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_splat(gvx_batch* b, int mode, float radius, int chan_density, int chan_vel, int accum, int flags)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaSetDevice(b->device));
+    if (b->grids.empty()) return GVX_OK;
+    // the grids' own streams first (their InsertPoints work), then the batch
+    for (gvx_grid* g : b->grids) {
+        if (g->stream == b->stream) continue;
+        GVX_CK(cudaEventRecord(b->ev, g->stream));
+        GVX_CK(cudaStreamWaitEvent(b->stream, b->ev, 0));
+    }
+    int layers = 0, bps = 0;
+    std::vector<SplatArgs> args;
+    std::vector<uint32_t> us;
+    SplatKind kind;
+    gvx_status rc = batch_tables(b, mode, radius, chan_density, chan_vel, accum, 0, args, us, kind);
+    if (rc) return rc;
+    const std::string key = tune_key(b->device, args[0], kind);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) b->tuning = it->second;
+    }
+    if ((flags & GVX_BATCH_TUNE) && !accum && b->tuning.layers == 0) {
+        // the grids' streams must not run during the timing
+        for (gvx_grid* g : b->grids) GVX_CK(cudaStreamSynchronize(g->stream));
+        batch_drop_graph(b);
+        rc = batch_tune(b, mode, radius, chan_density, chan_vel, &b->tuning);
+        if (rc) return rc;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = b->tuning;
+    }
+    layers = b->tuning.layers;
+    bps = b->tuning.blocks_per_sm;
+    if (layers > 0 && layers != args[0].slab_layers) {
+        rc = batch_tables(b, mode, radius, chan_density, chan_vel, accum, layers, args, us, kind);
+        if (rc) return rc;
+    }
+    int per_sm = 1;
+    rc = batch_max_blocks(b, kind, args[0], &per_sm);
+    if (rc) return rc;
+    if (bps <= 0 || bps > per_sm) bps = per_sm;
+    const uint64_t ctas_needed = ((uint64_t)us.back() + kSlabWarps - 1) / kSlabWarps;
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(b->device) * bps));
+    const bool same = b->exec && b->cap_args.size() == args.size() && b->cap_kind == kind &&
+                      b->cap_blocks == blocks &&
+                      memcmp(b->cap_args.data(), args.data(), args.size() * sizeof(SplatArgs)) == 0 &&
+                      b->cap_ustart == us;
+    if (us.back() > 0) {
+        if (flags & GVX_BATCH_GRAPH) {
+            if (!same) {
+                batch_drop_graph(b);
+                rc = batch_upload(b, args, us);
+                if (rc) return rc;
+                GVX_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+                rc = batch_launch(b, kind, args[0], (int)args.size(), blocks);
+                cudaGraph_t graph = nullptr;
+                cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+                if (rc) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return rc;
+                }
+                if (e != cudaSuccess) return gvx_cuda_fail(e, "cudaStreamEndCapture");
+                b->graph = graph;
+                e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+                if (e != cudaSuccess) {
+                    batch_drop_graph(b);
+                    return gvx_cuda_fail(e, "cudaGraphInstantiate");
+                }
+                b->cap_args = args;
+                b->cap_ustart = us;
+                b->cap_kind = kind;
+                b->cap_blocks = blocks;
+                b->launches--;  // the captured launch runs with the graph below
+            }
+            GVX_CK(cudaGraphLaunch(b->exec, b->stream));
+            b->launches++;
+        } else {
+            rc = batch_upload(b, args, us);
+            if (rc) return rc;
+            rc = batch_launch(b, kind, args[0], (int)args.size(), blocks);
+            if (rc) return rc;
+        }
+    }
+    // the grids' streams see the splat before their next work
+    GVX_CK(cudaEventRecord(b->ev, b->stream));
+    for (gvx_grid* g : b->grids) {
+        if (g->stream != b->stream) GVX_CK(cudaStreamWaitEvent(g->stream, b->ev, 0));
+        g->launches++;
+        splat_finish(g, chan_density, chan_vel, accum);
     }
     return GVX_OK;
 }
+
+gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_sm, float* ms)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (slab_layers) *slab_layers = b->tuning.layers;
+    if (blocks_per_sm) *blocks_per_sm = b->tuning.blocks_per_sm;
+    if (ms) *ms = b->tuning.ms;
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* out)
+{
+    if (!b || !out) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *out = b->launches;
+    return GVX_OK;
+}
+
+}  // extern "C"
 
 gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand)
 {
@@ -706,7 +1168,7 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
     GVX_CK(cudaFuncSetAttribute(k_scatter_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     GVX_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scatter_ref, kSplatThreads, smem));
-    const uint32_t grid = std::min<uint32_t>(a.nslots, (uint32_t)(sm_count(g) * std::max(per_sm, 1)));
+    const uint32_t grid = std::min<uint32_t>(a.nslots, (uint32_t)(sm_count(g->device) * std::max(per_sm, 1)));
     k_scatter_ref<<<grid, kSplatThreads, smem, g->stream>>>(a);
     g->launches++;
     GVX_CK(cudaGetLastError());

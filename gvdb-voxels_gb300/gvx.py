@@ -89,6 +89,11 @@ def load(path=None):
         "gvx_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
         "gvx_radix_sort": ([vp, vp, vp, vp, vp, ctypes.c_uint32, i], i),
         "gvx_radix_sort_noalloc": ([vp, vp, vp, vp, ctypes.c_uint32, i, vp], i),
+        "gvx_batch_create": ([i, ctypes.POINTER(vp)], i), "gvx_batch_destroy": ([vp], i),
+        "gvx_batch_set_stream": ([vp, vp], i), "gvx_batch_set_grids": ([vp, ctypes.POINTER(vp), i], i),
+        "gvx_batch_splat": ([vp, i, f, i, i, i, i], i),
+        "gvx_batch_get_tuning": ([vp, ip, ip, fp], i),
+        "gvx_batch_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -318,3 +323,56 @@ def radix_sort(grid, keys_in, vals_in, keys_out, vals_out, n, bits):
     """gvx_radix_sort on device buffers (torch tensors or raw pointers)"""
     grid._check(grid.lib.gvx_radix_sort(grid.h, _ptr(keys_in), _ptr(vals_in), _ptr(keys_out), _ptr(vals_out),
                                         int(n), int(bits)))
+
+
+BATCH_GRAPH, BATCH_TUNE = 1, 2
+
+
+class Batch:
+    """One gvx_batch handle: the splats of many grids in one persistent launch."""
+
+    def __init__(self, device=0, lib=None):
+        self.lib = lib or load()
+        h = ctypes.c_void_p()
+        st = self.lib.gvx_batch_create(device, ctypes.byref(h))
+        if st:
+            raise GvxError(st, self.lib.gvx_last_error().decode())
+        self.h = h
+        self._grids = []
+
+    def _check(self, st):
+        if st:
+            raise GvxError(st, self.lib.gvx_last_error().decode())
+
+    def close(self):
+        if self.h:
+            self.lib.gvx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        self._check(self.lib.gvx_batch_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def set_grids(self, grids):
+        self._grids = list(grids)
+        arr = (ctypes.c_void_p * len(grids))(*[g.h.value for g in grids])
+        self._check(self.lib.gvx_batch_set_grids(self.h, arr, len(grids)))
+
+    def splat(self, mode, radius, chan_density=0, chan_vel=-1, accum=False, graph=True, tune=False):
+        flags = (BATCH_GRAPH if graph else 0) | (BATCH_TUNE if tune else 0)
+        self._check(self.lib.gvx_batch_splat(self.h, mode, float(radius), chan_density, chan_vel, int(accum), flags))
+
+    def tuning(self):
+        la, bp, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0)
+        self._check(self.lib.gvx_batch_get_tuning(self.h, ctypes.byref(la), ctypes.byref(bp), ctypes.byref(ms)))
+        return {"slab_layers": la.value, "blocks_per_sm": bp.value, "ms": ms.value}
+
+    def kernel_launches(self):
+        c = ctypes.c_int64()
+        self._check(self.lib.gvx_batch_kernel_launches(self.h, ctypes.byref(c)))
+        return c.value

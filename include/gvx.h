@@ -228,6 +228,27 @@ gvx_status gvx_retrieve_brick(gvx_grid* g, int chan, const int corner[3], void* 
 /* number of kernels the library has launched on this grid (instrumentation) */
 gvx_status gvx_kernel_launches(gvx_grid* g, int64_t* count);
 
+/* ---- batched multi-grid splat (no counterpart in the reference, where each
+ * VolumeGVDB splats on its own).  A batch splats many grids -- one per point
+ * cloud, all configured with the same brick shape and channel kinds, each
+ * with its topology, atlas and InsertPoints grouping done -- in ONE persistent
+ * launch.  With GVX_BATCH_GRAPH the launch is captured in a CUDA graph and
+ * replayed while no grid's buffers move (a change re-captures it); with
+ * GVX_BATCH_TUNE the first call of a (GPU, brick shape, kind) times a few slab
+ * heights and CTAs per SM on the live batch and caches the fastest for the
+ * process.  Results are those of gvx_splat on each grid, bit for bit. */
+typedef struct gvx_batch gvx_batch;
+#define GVX_BATCH_GRAPH 1
+#define GVX_BATCH_TUNE 2
+gvx_status gvx_batch_create(int device, gvx_batch** out);
+gvx_status gvx_batch_destroy(gvx_batch* b);
+gvx_status gvx_batch_set_stream(gvx_batch* b, void* stream);
+gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count);
+gvx_status gvx_batch_splat(gvx_batch* b, int mode, float radius, int chan_density, int chan_vel, int accum,
+                           int flags);
+gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_sm, float* ms);
+gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* count);
+
 #ifdef __cplusplus
 }
 #endif
