@@ -414,6 +414,69 @@ def run_differentiable(dev, iters=5):
             "fwd_plus_bwd_ms": round(f + b, 4), "bwd_over_fwd": round(b / f, 4)}
 
 
+def run_batched(dev, iters=5):
+    """Batched workload: 64 uneven clouds (N_i = floor(exp(U(ln 1e4, ln 2e6))), seed 7, Gaussian
+    mixtures in 1024^3, w ~ U(0.5, 1.5)), one grid each, TRILINEAR density.  Times, on one stream,
+    the per-cloud loop of gvx_splat calls against one gvx_batch_splat replaying its captured graph
+    (autotuned on its first call); the topologies, atlases and groupings are built beforehand."""
+    import numpy as np
+    import torch
+
+    import gvx
+    import workloads
+
+    cl = workloads.batched_clouds(count=64, seed=7)
+    stream = torch.cuda.Stream(device=dev)
+    grids, keep = [], []
+    with torch.cuda.stream(stream):
+        for p, w in cl:
+            g = gvx.Grid(dev.index)
+            g.configure(LOGDIM)
+            g.add_channel(0, gvx.T_FLOAT, 1)
+            g.set_stream(stream.cuda_stream)
+            pd, wd = torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev)
+            keep.append((pd, wd))
+            g.set_points(len(p), pd)
+            g.set_point_attribs(weight=wd)
+            g.rebuild_topology(len(p), 1.0, mode=gvx.TOPO_FULL)
+            g.update_atlas()
+            g.insert_points(len(p))
+            grids.append(g)
+        b = gvx.Batch(dev.index)
+        b.set_stream(stream.cuda_stream)
+        b.set_grids(grids)
+        b.splat(gvx.SPLAT_TRILINEAR, 1.0, graph=True, tune=True)  # tunes, captures
+        b.splat(gvx.SPLAT_TRILINEAR, 1.0, graph=True)
+        for g, (p, _) in zip(grids, cl):
+            g.splat(gvx.SPLAT_TRILINEAR, len(p), 1.0)
+        torch.cuda.synchronize()
+        seq, bat = [], []
+        for k in range(iters):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(stream)
+            for g, (p, _) in zip(grids, cl):
+                g.splat(gvx.SPLAT_TRILINEAR, len(p), 1.0)
+            e[1].record(stream)
+            b.splat(gvx.SPLAT_TRILINEAR, 1.0, graph=True)
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            seq.append(e[0].elapsed_time(e[1]))
+            bat.append(e[1].elapsed_time(e[2]))
+        tun = b.tuning()
+        bricks = sum(g.info()["used_leaves"] for g in grids)
+    b.close()
+    for g in grids:
+        g.close()
+    s_ms, b_ms = sum(seq) / len(seq), sum(bat) / len(bat)
+    npts = int(sum(len(p) for p, _ in cl))
+    return {"workload": "batched: 64 Gaussian-mixture clouds, N_i = floor(exp(U(ln 1e4, ln 2e6))) seed 7, "
+                        "1024^3, TRILINEAR density, one grid per cloud",
+            "clouds": len(cl), "points": npts, "active_bricks": int(bricks),
+            "sequential_ms": round(s_ms, 4), "batched_graph_ms": round(b_ms, 4),
+            "speedup": round(s_ms / b_ms, 3), "batched_mpoints_s": round(npts / (b_ms * 1e-3) / 1e6, 1),
+            "tuning": tun}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -449,7 +512,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=0, help="smaller runs for profiling (same density)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the differentiable-workload timing")
+    ap.add_argument("--no-extras", action="store_true", help="skip the differentiable and batched workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
@@ -467,6 +530,7 @@ def main():
         import torch
 
         out["differentiable"] = run_differentiable(torch.device("cuda", 0))
+        out["batched"] = run_batched(torch.device("cuda", 0))
     if rank == 0:
         if pool is not None:
             out["cpu_baseline"] = cpu_baseline(pool)

@@ -105,6 +105,7 @@ struct SplatArgs {
     float* den;          // channel data (slot-major, P^3 per slot) or nullptr
     float4* vel;         // or nullptr
     int slabs, slab_layers;  // z-slabs per padded brick, layers per slab
+    int lb;              // log2(brick)
     int reach;           // voxels a point's footprint reaches beyond its brick (neighbour pruning)
     float max_radius;    // per-point radii above this reach past the 26 neighbours
     bool accum;
@@ -184,21 +185,26 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     }
     const uint32_t nbmask = __ballot_sync(kFull, has_nb);
     const int len = max(0, rg.y - rg.x);
-    int rank = 0, off = 0, total = 0, m = 0;
-    for (int k = 0; k < 27; k++) {
-        const int sk = __shfl_sync(kFull, rg.x, k), lk = __shfl_sync(kFull, len, k);
-        if (lk > 0) {
-            m++;
-            total += lk;
-            if (sk < rg.x) {
-                rank++;
-                off += lk;
-            }
-        }
+    // Points are sorted by their brick's key, which orders bricks by (x, y, z),
+    // so the ranges lie in the order of the neighbours' (dx, dy, dz): lane t
+    // takes the t-th neighbour in that order, and a scan gives the offsets.
+    const int src = (lane % 3) * 9 + ((lane / 3) % 3) * 3 + lane / 9;  // nbr-table lane of (dx, dy, dz)
+    const int rs = __shfl_sync(kFull, rg.x, src);
+    const int rl_all = __shfl_sync(kFull, len, src);  // every lane takes part in the shuffle
+    const int rl = lane < 27 ? rl_all : 0;
+    int incl = rl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
     }
-    if (lane < 27 && len > 0) {
-        s_rs_w[rank] = rg.x;
-        s_ro_w[rank] = off;
+    const int total = __shfl_sync(kFull, incl, 31);
+    const uint32_t ne = __ballot_sync(kFull, rl > 0);
+    const int m = __popc(ne);
+    if (rl > 0) {
+        const int rank = __popc(ne & ((1u << lane) - 1u));
+        s_rs_w[rank] = rs;
+        s_ro_w[rank] = incl - rl;
     }
     if (lane == 0) s_ro_w[m] = total;
 
@@ -221,7 +227,9 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             }
         }
     } else {
-        for (int i = lane; i < nvox; i += 32) T::set(tile, i, 0.0f);
+        // zeros in 16-byte stores (a slab holds a multiple of 4 voxels: P is even)
+        const int n16 = (int)(T::bytes(nvox) / 16);
+        for (int i = lane; i < n16; i += 32) ((float4*)tile)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
 
@@ -396,16 +404,23 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
         }
     }
 
-    // ---- apron voxels with no neighbouring brick take the boundary value (0)
+    // ---- apron voxels with no neighbouring brick take the boundary value (0):
+    // the apron region facing each missing neighbour (apron 1), clipped to the slab
     if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
-        for (int i = lane; i < nvox; i += 32) {
-            const int z = z0 + i / P2, r = i % P2, y = r / P, x = r % P;
-            const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
-            const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
-            const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
-            if (!(dx | dy | dz)) continue;  // interior voxel
-            if ((nbmask >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u) continue;
-            T::set(tile, i, a.boundval);
+#pragma unroll 1
+        for (int k = 0; k < 27; k++) {
+            if (k == 13 || ((nbmask >> k) & 1u)) continue;
+            const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+            const int xb = dx < 0 ? 0 : (dx > 0 ? P - 1 : 1), yb = dy < 0 ? 0 : (dy > 0 ? P - 1 : 1);
+            const int bx = dx == 0 ? a.lb : 0, by = dy == 0 ? a.lb : 0;  // log2 of the region's x, y extents
+            const int zlo = max(dz < 0 ? 0 : (dz > 0 ? P - 1 : 1), z0);
+            const int zhi = min(dz < 0 ? 0 : (dz > 0 ? P - 1 : P - 2), z0 + nl - 1);
+            const int cnt = zhi >= zlo ? (zhi - zlo + 1) << (bx + by) : 0;
+            for (int c = lane; c < cnt; c += 32) {
+                const int x = xb + (c & ((1 << bx) - 1)), y = yb + ((c >> bx) & ((1 << by) - 1));
+                const int z = zlo + (c >> (bx + by));
+                T::set(tile, ((z - z0) * P + y) * P + x, a.boundval);
+            }
         }
         __syncwarp();
     }
@@ -688,6 +703,10 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
         gvx_set_error("Splat: radius %g reaches beyond the 26 neighbouring bricks", radius);
         return GVX_ERR_UNSUPPORTED;
     }
+    if (g->brick < 2) {
+        gvx_set_error("Splat: bricks of 1 voxel are not supported (tiles are moved in 16-byte units)");
+        return GVX_ERR_UNSUPPORTED;
+    }
     const bool need_svel = has_v || ppr;
     rc = gvx_prepare_points(g, n, trans, need_svel);
     if (rc) return rc;
@@ -717,6 +736,8 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
     a.vel = has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
     a.slab_layers = layers;
     a.slabs = (P + layers - 1) / layers;
+    a.lb = 0;
+    while ((1 << a.lb) < g->brick) a.lb++;
     a.max_radius = (float)(g->brick - 1);
     a.reach = mode == GVX_SPLAT_TRILINEAR ? 1 : (ppr ? g->brick - 1 : (int)ceilf(radius));
     a.accum = accum != 0;
