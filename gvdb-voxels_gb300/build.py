@@ -2,7 +2,9 @@
 
 Compiles every csrc/*.cu translation unit in parallel with nvcc and links them
 into gvdb-voxels_gb300/libgvx.so.  No cmake, no torch extension machinery: the
-library is a plain C-ABI shared object (include/gvx.h).
+library is a plain C-ABI shared object (include/gvx.h).  The nvdb::VolumeGVDB
+drop-in class (cpp/, include/gvx_volume_gvdb.h) is compiled with g++ into
+libgvx_volume.so, linked against libgvx.
 """
 import concurrent.futures as cf
 import os
@@ -56,7 +58,25 @@ def build(verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_volume()
     return LIB
+
+
+VOLUME_SRC = os.path.join(HERE, "cpp", "gvx_volume_gvdb.cpp")
+VOLUME_LIB = os.path.join(HERE, "libgvx_volume.so")
+
+
+def build_volume():
+    """libgvx_volume.so: the nvdb::VolumeGVDB drop-in class (include/gvx_volume_gvdb.h)
+    over libgvx, found next to it at run time"""
+    tmp = VOLUME_LIB + ".tmp"
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", "-I", os.path.join(ROOT, "include"),
+           VOLUME_SRC, "-o", tmp, "-L", HERE, "-lgvx", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for the VolumeGVDB class:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, VOLUME_LIB)
+    return VOLUME_LIB
 
 
 if __name__ == "__main__":

@@ -1,0 +1,442 @@
+// gvx_volume_gvdb.cpp -- nvdb::VolumeGVDB (point -> sparse-volume path) over
+// the libgvx C ABI.  Each method cites the reference method it stands in for
+// (gvdb_volume_gvdb.cpp = VG.cpp).
+#include "gvx_volume_gvdb.h"
+
+#include <cstring>
+
+namespace nvdb {
+
+VolumeGVDB::VolumeGVDB() {}
+
+VolumeGVDB::~VolumeGVDB()
+{
+    FreeData(pnode_);
+    if (g_) gvx_destroy(g_);
+}
+
+void VolumeGVDB::check(gvx_status st) const
+{
+    if (st != GVX_OK) throw GvxError((int)st, std::string("gvx: ") + gvx_last_error());
+}
+
+void VolumeGVDB::need_grid()
+{
+    if (!g_) check(gvx_create(dev_, &g_));
+}
+
+// SetCudaDevice (VG.cpp:186-260): the device of every later allocation
+void VolumeGVDB::SetCudaDevice(int devid, void* ctx)
+{
+    (void)ctx;
+    if (g_ && devid != dev_) {
+        gvx_destroy(g_);
+        g_ = nullptr;
+    }
+    dev_ = devid;
+}
+
+// Initialize (VG.cpp:262-300)
+void VolumeGVDB::Initialize() { need_grid(); }
+
+// Clear (VG.cpp:2487-2503): the next RebuildTopology starts from an empty tree
+void VolumeGVDB::Clear()
+{
+    need_grid();
+    check(gvx_request_full_rebuild(g_, 1));
+    topology_changed();
+}
+
+// Configure(q4..q0) (VG.cpp:2364-2377): level 0 takes the last argument
+void VolumeGVDB::Configure(int r4, int r3, int r2, int r1, int r0)
+{
+    int r[5] = {r0, r1, r2, r3, r4};
+    Configure(5, r, nullptr);
+}
+
+// Configure(levs, r, ncnt) (VG.cpp:2380-2434); pools grow as needed, so ncnt
+// (the initial pool sizes) and bitmasks change nothing here
+void VolumeGVDB::Configure(int levs, int* r, int* ncnt, bool use_masks)
+{
+    (void)use_masks;
+    need_grid();
+    check(gvx_configure(g_, levs, r, ncnt));
+    levels_ = levs;
+    mirror_.assign(levs, std::vector<Node>());
+    mirror_gen_.assign(levs, 0);
+    topology_changed();
+}
+
+void VolumeGVDB::SetChannelDefault(int cx, int cy, int cz)
+{
+    need_grid();
+    check(gvx_set_channel_default(g_, cx, cy, cz));
+}
+
+void VolumeGVDB::SetApron(int n)
+{
+    apron_ = n;
+    apron_set_ = true;
+}
+
+// AddChannel (VG.cpp:2436-2454); filter and border modes belong to texture
+// sampling, which the point path does not use
+void VolumeGVDB::AddChannel(uchar chan, int dt, int apron, int filter, int border, Vector3DI axiscnt)
+{
+    (void)filter;
+    (void)border;
+    need_grid();
+    if (axiscnt.x > 0 && axiscnt.y > 0 && axiscnt.z > 0)
+        check(gvx_set_channel_default(g_, axiscnt.x, axiscnt.y, axiscnt.z));
+    check(gvx_add_channel(g_, chan, dt, apron));
+    apron_ = apron;
+}
+
+// FillChannel (VG.cpp:2456-2471)
+void VolumeGVDB::FillChannel(uchar chan, Vector4DF val)
+{
+    need_grid();
+    const float v[4] = {val.x, val.y, val.z, val.w};
+    check(gvx_fill_channel(g_, chan, v));
+}
+
+// ClearChannel (VG.cpp:1596-1603)
+void VolumeGVDB::ClearChannel(uchar chan)
+{
+    need_grid();
+    check(gvx_clear_channel(g_, chan));
+}
+
+// FinishTopology (VG.cpp:1579-1593): pools are on the device already; bounds
+void VolumeGVDB::FinishTopology(bool pCommitPool, bool pComputeBounds)
+{
+    (void)pCommitPool;
+    need_grid();
+    if (pComputeBounds) check(gvx_finish_topology(g_));
+}
+
+// UpdateAtlas (VG.cpp:2630-2704): leaves get their atlas slots (mValue)
+void VolumeGVDB::UpdateAtlas()
+{
+    need_grid();
+    check(gvx_update_atlas(g_));
+    topology_changed();
+}
+
+// UpdateApron() (VG.cpp:4411-4416)
+void VolumeGVDB::UpdateApron()
+{
+    need_grid();
+    check(gvx_update_apron_all(g_));
+}
+
+// UpdateApron(chan, boundval) (VG.cpp:4418-4457)
+void VolumeGVDB::UpdateApron(uchar chan, float boundval, bool changeCtx)
+{
+    (void)changeCtx;
+    need_grid();
+    check(gvx_update_apron(g_, chan, boundval));
+}
+
+// AtlasRetrieveBrickXYZ (VG.h:412): one brick's interior into dest.cpu, and
+// into dest.gpu when the caller gave one
+void VolumeGVDB::AtlasRetrieveBrickXYZ(uchar channel, Vector3DI minimumCorner, DataPtr& dest)
+{
+    need_grid();
+    int64_t bytes = 0;
+    check(gvx_channel_bytes(g_, channel, &bytes));
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    const int64_t b = inf.brick_res;
+    const int64_t elem = bytes / ((int64_t)inf.atlas_res[0] * inf.atlas_res[1] * inf.atlas_res[2]);
+    const int64_t need = b * b * b * elem;
+    std::vector<char> tmp;
+    char* out = dest.cpu;
+    if (!out) {
+        tmp.resize((size_t)need);
+        out = tmp.data();
+    }
+    const int corner[3] = {minimumCorner.x, minimumCorner.y, minimumCorner.z};
+    check(gvx_retrieve_brick(g_, channel, corner, out, need));
+    if (dest.gpu) check(gvx_memcpy(dev_, (void*)dest.gpu, out, (size_t)need, GVX_COPY_H2D));
+}
+
+// RebuildTopology (VG.cpp:1181-1218), with its full / incremental state machine
+void VolumeGVDB::RebuildTopology(int pNumPnts, float pRadius, Vector3DF pOrig)
+{
+    need_grid();
+    const float o[3] = {pOrig.x, pOrig.y, pOrig.z};
+    check(gvx_rebuild_topology(g_, pNumPnts, pRadius, o, GVX_TOPO_AUTO, 1));
+    topology_changed();
+}
+
+// AccumulateTopology (VG.cpp:1158-1178)
+void VolumeGVDB::AccumulateTopology(int pNumPnts, float pRadius, Vector3DF pOrig, int iDepth)
+{
+    need_grid();
+    const float o[3] = {pOrig.x, pOrig.y, pOrig.z};
+    check(gvx_rebuild_topology(g_, pNumPnts, pRadius, o, GVX_TOPO_ACCUMULATE, iDepth));
+    topology_changed();
+}
+
+// RequestFullRebuild (VG.h:432)
+void VolumeGVDB::RequestFullRebuild(bool tf)
+{
+    need_grid();
+    check(gvx_request_full_rebuild(g_, tf ? 1 : 0));
+}
+
+// AllocData (VG.cpp:4820-4826): (re)allocates when missing, too small or of another stride
+void VolumeGVDB::AllocData(DataPtr& ptr, int cnt, int stride, bool bCPU)
+{
+    if (!((ptr.cpu == nullptr && bCPU) || ptr.gpu == 0 || (uint64)cnt > ptr.max || (uint64)stride != ptr.stride))
+        return;
+    FreeData(ptr);
+    const size_t bytes = (size_t)cnt * (size_t)stride;
+    if (bCPU) {
+        ptr.cpu = new char[bytes ? bytes : 1];
+        ptr.own_cpu = true;
+    }
+    void* d = nullptr;
+    check(gvx_device_alloc(dev_, bytes, &d));
+    ptr.gpu = (CUdeviceptr)d;
+    ptr.own_gpu = true;
+    ptr.max = ptr.lastEle = ptr.usedNum = (uint64)cnt;
+    ptr.stride = (uint64)stride;
+    ptr.size = bytes;
+    ptr.subdim.Set(0, stride, 0);
+}
+
+// FreeData (VG.cpp:4827-4832): releases what AllocData allocated
+void VolumeGVDB::FreeData(DataPtr& ptr)
+{
+    if (ptr.own_cpu) delete[] ptr.cpu;
+    if (ptr.own_gpu && ptr.gpu) gvx_device_free(dev_, (void*)ptr.gpu);
+    ptr = DataPtr();
+}
+
+static size_t data_bytes(const DataPtr& p)
+{
+    return p.size ? (size_t)p.size : (size_t)(p.lastEle * p.stride);
+}
+
+// RetrieveData (VG.cpp:4879-4884): device -> host
+void VolumeGVDB::RetrieveData(DataPtr ptr)
+{
+    if (!ptr.cpu || !ptr.gpu) throw GvxError(GVX_ERR_INVALID_ARG, "RetrieveData: buffer not allocated on both sides");
+    check(gvx_memcpy(dev_, ptr.cpu, (const void*)ptr.gpu, data_bytes(ptr), GVX_COPY_D2H));
+}
+
+// CommitData (VG.cpp:4833-4840): host -> device
+void VolumeGVDB::CommitData(DataPtr ptr)
+{
+    if (!ptr.cpu || !ptr.gpu) throw GvxError(GVX_ERR_INVALID_ARG, "CommitData: buffer not allocated on both sides");
+    check(gvx_memcpy(dev_, (void*)ptr.gpu, ptr.cpu, data_bytes(ptr), GVX_COPY_H2D));
+}
+
+// CommitData(ptr, cnt, cpubuf, offs, stride) (VG.cpp:4841-4861)
+void VolumeGVDB::CommitData(DataPtr& dat, int cnt, char* cptr, int offs, int stride)
+{
+    dat.cpu = cptr;
+    dat.own_cpu = false;
+    dat.usedNum = dat.lastEle = dat.max = (uint64)cnt;
+    dat.stride = (uint64)stride;
+    dat.size = (uint64)cnt * (uint64)stride;
+    dat.subdim.Set(offs, stride, 0);
+    if (dat.gpu == 0) throw GvxError(GVX_ERR_INVALID_ARG, "CommitData: buffer not allocated on the GPU (AllocData)");
+    CommitData(dat);
+}
+
+// SetDataCPU (VG.cpp:4862-4870)
+void VolumeGVDB::SetDataCPU(DataPtr& dat, int cnt, char* cptr, int offs, int stride)
+{
+    dat.usedNum = dat.lastEle = dat.max = (uint64)cnt;
+    dat.cpu = cptr;
+    dat.own_cpu = false;
+    dat.stride = (uint64)stride;
+    dat.size = (uint64)cnt * (uint64)stride;
+    dat.subdim.Set(offs, stride, 0);
+}
+
+// SetDataGPU (VG.cpp:4871-4879): a borrowed device buffer
+void VolumeGVDB::SetDataGPU(DataPtr& dat, int cnt, CUdeviceptr gptr, int offs, int stride)
+{
+    dat.usedNum = dat.lastEle = dat.max = (uint64)cnt;
+    dat.gpu = gptr;
+    dat.own_gpu = false;
+    dat.stride = (uint64)stride;
+    dat.size = (uint64)cnt * (uint64)stride;
+    dat.subdim.Set(offs, stride, 0);
+}
+
+// SetPoints (VG.cpp:4900-4908): binds (does not copy) the point buffers; the
+// xyz of point i is at gpu + i * stride + subdim.x
+void VolumeGVDB::SetPoints(DataPtr& pntpos, DataPtr& pntvel, DataPtr& clrpos)
+{
+    need_grid();
+    pos_ = pntpos;
+    vel_ = pntvel;
+    clr_ = clrpos;
+    pos_.own_cpu = pos_.own_gpu = vel_.own_cpu = vel_.own_gpu = clr_.own_cpu = clr_.own_gpu = false;
+    check(gvx_set_points(g_, (int)pntpos.lastEle, (const void*)pntpos.gpu, pntpos.subdim.x, (int)pntpos.stride,
+                         pntvel.gpu ? (const void*)pntvel.gpu : nullptr, pntvel.subdim.x, (int)pntvel.stride,
+                         clrpos.gpu ? (const void*)clrpos.gpu : nullptr, clrpos.subdim.x, (int)clrpos.stride));
+    pnode_gen_ = 0;
+}
+
+// InsertPoints (VG.cpp:5219-5267): groups the points by brick for the splats
+void VolumeGVDB::InsertPoints(int num_pnts, Vector3DF trans, bool bPrefix)
+{
+    (void)bPrefix;
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_insert_points(g_, num_pnts, t, nullptr));
+    last_insert_n_ = num_pnts;
+    memcpy(last_trans_, t, sizeof(t));
+    pnode_gen_ = 0;
+}
+
+// InsertPointsSubcell (VG.cpp:4971-5092)
+void VolumeGVDB::InsertPointsSubcell(int subcell_size, int num_pnts, float pRadius, Vector3DF trans,
+                                     int& pSCPntsLength)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_insert_points_subcell(g_, subcell_size, num_pnts, pRadius, t, &pSCPntsLength));
+}
+
+// ScatterDensity (VG.cpp:5624-5660)
+void VolumeGVDB::ScatterDensity(int num_pnts, float radius, float amp, Vector3DF trans, bool expand, bool avgColor)
+{
+    need_grid();
+    if (avgColor) throw GvxError(GVX_ERR_UNSUPPORTED, "ScatterDensity: colour averaging is not available");
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_scatter_density(g_, num_pnts, radius, amp, t, expand ? 1 : 0));
+}
+
+// GatherDensity (VG.cpp:5318-5344)
+void VolumeGVDB::GatherDensity(int subcell_size, int num_pnts, float radius, Vector3DF trans, int& pSCPntsLength,
+                               int chanDensity, int chanClr, bool bAccum)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_gather_density(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanDensity, chanClr,
+                             bAccum ? 1 : 0));
+}
+
+// GatherLevelSet (VG.cpp:5348-5373)
+void VolumeGVDB::GatherLevelSet(int subcell_size, int num_pnts, float radius, Vector3DF trans, int& pSCPntsLength,
+                                int chanLevelset, int chanClr, bool bAccum)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_gather_levelset(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanLevelset, chanClr,
+                              bAccum ? 1 : 0));
+}
+
+// getAux (VG.h:625) for the point buffers and AUX_PNODE, the leaf of every
+// point after InsertPoints (ID_UNDEFL when none), on the host and the device
+DataPtr& VolumeGVDB::getAux(int id)
+{
+    switch (id) {
+    case AUX_PNTPOS: return pos_;
+    case AUX_PNTVEL: return vel_;
+    case AUX_PNTCLR: return clr_;
+    case AUX_PNODE:
+        if (pnode_gen_ != gen_ && last_insert_n_ > 0) {
+            AllocData(pnode_, last_insert_n_, sizeof(int), true);
+            check(gvx_insert_points(g_, last_insert_n_, last_trans_, (int32_t*)pnode_.cpu));
+            CommitData(pnode_);
+            pnode_gen_ = gen_;
+        }
+        return pnode_;
+    }
+    throw GvxError(GVX_ERR_UNSUPPORTED, "getAux: buffer " + std::to_string(id) + " is not kept by this library");
+}
+
+uint64 VolumeGVDB::getNumUsedNodes(int lev)
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    if (lev < 0 || lev >= GVX_MAX_LEVELS) return 0;
+    return lev == 0 ? (uint64)inf.used_leaves : (uint64)inf.node_count[lev];
+}
+
+uint64 VolumeGVDB::getNumTotalNodes(int lev)
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    if (lev < 0 || lev >= GVX_MAX_LEVELS) return 0;
+    return (uint64)inf.node_count[lev];
+}
+
+Node* VolumeGVDB::mirror(int lev, uint64 ndx)
+{
+    if (lev < 0 || lev >= (int)mirror_.size()) return nullptr;
+    if (mirror_gen_[lev] != gen_) {
+        const uint64 cnt = getNumTotalNodes(lev);
+        mirror_[lev].resize((size_t)cnt);
+        if (cnt) check(gvx_read_nodes(g_, lev, mirror_[lev].data(), (int64_t)cnt));
+        mirror_gen_[lev] = gen_;
+    }
+    return ndx < mirror_[lev].size() ? &mirror_[lev][ndx] : nullptr;
+}
+
+// getNodeAtLevel (VG.h:643)
+Node* VolumeGVDB::getNodeAtLevel(int n, int lev) { return n < 0 ? nullptr : mirror(lev, (uint64)n); }
+
+// getNode(grp, lev, ndx) (VG.h:451): node pools are group 0
+Node* VolumeGVDB::getNode(int grp, int lev, slong ndx)
+{
+    return (grp != 0 || ndx < 0) ? nullptr : mirror(lev, (uint64)ndx);
+}
+
+// getNode(Elem id) (VG.h:453), id = grp | lev << 8 | ndx << 16
+Node* VolumeGVDB::getNode(slong nodeid)
+{
+    const uint64 id = (uint64)nodeid;
+    return getNode((int)(id & 0xFF), (int)((id >> 8) & 0xFF), (slong)(id >> 16));
+}
+
+Vector3DF VolumeGVDB::getWorldMin()
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    return Vector3DF(inf.obj_min[0], inf.obj_min[1], inf.obj_min[2]);
+}
+
+Vector3DF VolumeGVDB::getWorldMax()
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    return Vector3DF(inf.obj_max[0], inf.obj_max[1], inf.obj_max[2]);
+}
+
+void VolumeGVDB::Splat(int mode, int num_pnts, float radius, Vector3DF trans, int chanDensity, int chanVel,
+                       bool bAccum)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_splat(g_, mode, num_pnts, radius, t, chanDensity, chanVel, bAccum ? 1 : 0));
+}
+
+void VolumeGVDB::SplatBackward(int mode, int num_pnts, float radius, Vector3DF trans, CUdeviceptr dL_drho,
+                               CUdeviceptr grad_pos, CUdeviceptr grad_w, CUdeviceptr grad_r)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_splat_backward(g_, mode, num_pnts, radius, t, (const float*)dL_drho, (float*)grad_pos,
+                             (float*)grad_w, (float*)grad_r));
+}
+
+void VolumeGVDB::SetPointAttribs(CUdeviceptr weight, CUdeviceptr radius)
+{
+    need_grid();
+    check(gvx_set_point_attribs(g_, (const float*)weight, (const float*)radius));
+}
+
+}  // namespace nvdb

@@ -736,4 +736,44 @@ gvx_status gvx_kernel_launches(gvx_grid* g, int64_t* count)
     return GVX_OK;
 }
 
+gvx_status gvx_device_alloc(int device, size_t bytes, void** out)
+{
+    if (!out) {
+        gvx_set_error("device_alloc: null output");
+        return GVX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    GVX_CK(cudaSetDevice(device));
+    GVX_CK(cudaMalloc(out, bytes ? bytes : 16));
+    return GVX_OK;
+}
+
+gvx_status gvx_device_free(int device, void* ptr)
+{
+    if (!ptr) return GVX_OK;
+    GVX_CK(cudaSetDevice(device));
+    GVX_CK(cudaFree(ptr));
+    return GVX_OK;
+}
+
+gvx_status gvx_memcpy(int device, void* dst, const void* src, size_t bytes, int kind)
+{
+    if ((!dst || !src) && bytes) {
+        gvx_set_error("memcpy: null pointer");
+        return GVX_ERR_INVALID_ARG;
+    }
+    const cudaMemcpyKind k = kind == GVX_COPY_H2D   ? cudaMemcpyHostToDevice
+                             : kind == GVX_COPY_D2H ? cudaMemcpyDeviceToHost
+                             : kind == GVX_COPY_D2D ? cudaMemcpyDeviceToDevice
+                                                    : cudaMemcpyDefault;
+    if (kind < 0 || kind > 2) {
+        gvx_set_error("memcpy: unknown kind %d", kind);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (!bytes) return GVX_OK;
+    GVX_CK(cudaSetDevice(device));
+    GVX_CK(cudaMemcpy(dst, src, bytes, k));
+    return GVX_OK;
+}
+
 }  // extern "C"

@@ -61,6 +61,7 @@ typedef int gvx_status;
 #define GVX_SPLAT_CUBIC 1     /* Monaghan M4 cubic spline, support R = 2h (no reference counterpart) */
 
 #define GVX_NODE_BYTES 64 /* Node, gvdb_node.h:27-40 */
+#define GVX_MAX_LEVELS 10 /* tree levels a grid can have */
 
 typedef struct gvx_info {
     int levels;
@@ -222,11 +223,23 @@ gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap_
 gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t* bytes);
 /* AtlasRetrieveBrickXYZ (VG.h:412): one brick's interior (res0^3 values of the
  * channel's element size) at the brick whose interior corner is the atlas
- * voxel `corner`, into host memory, x fastest */
+ * voxel `corner`, into host memory with z fastest, out[(x*b + y)*b + z], the
+ * order of kernelRetrieveTexXYZ (cuda_gvdb_copydata.cu:74-79) */
 gvx_status gvx_retrieve_brick(gvx_grid* g, int chan, const int corner[3], void* out, int64_t cap_bytes);
 
 /* number of kernels the library has launched on this grid (instrumentation) */
 gvx_status gvx_kernel_launches(gvx_grid* g, int64_t* count);
+
+/* device memory for hosts without a CUDA runtime of their own: the backing of
+ * VolumeGVDB::AllocData / FreeData / CommitData / RetrieveData
+ * (VG.h:532-535, VG.cpp:4820-4885).  gvx_memcpy is synchronous; kind is
+ * GVX_COPY_H2D, GVX_COPY_D2H or GVX_COPY_D2D. */
+#define GVX_COPY_H2D 0
+#define GVX_COPY_D2H 1
+#define GVX_COPY_D2D 2
+gvx_status gvx_device_alloc(int device, size_t bytes, void** out);
+gvx_status gvx_device_free(int device, void* ptr);
+gvx_status gvx_memcpy(int device, void* dst, const void* src, size_t bytes, int kind);
 
 /* ---- batched multi-grid splat (no counterpart in the reference, where each
  * VolumeGVDB splats on its own).  A batch splats many grids -- one per point

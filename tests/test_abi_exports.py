@@ -37,3 +37,18 @@ def test_library_has_no_oracle_dependency(gvx_mod):
     # the product library never links the oracle
     lib = ctypes.CDLL(gvx_mod.LIB_PATH)
     assert not hasattr(lib, "orc_create")
+
+
+def test_volume_class_compiles_and_links(gvx_mod, tmp_path):
+    """the nvdb::VolumeGVDB drop-in (include/gvx_volume_gvdb.h, libgvx_volume.so) links a
+    program written against it (run on the GPU by test_gpu_volume_gvdb.py)"""
+    import subprocess
+
+    pkg = os.path.join(ROOT, "gvdb-voxels_gb300")
+    assert os.path.exists(os.path.join(pkg, "libgvx_volume.so"))
+    out = str(tmp_path / "volume_gvdb_points")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "volume_gvdb_points.cpp"), "-o", out, "-L", pkg, "-lgvx_volume",
+           "-lgvx", "-Wl,-rpath," + pkg]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
