@@ -477,6 +477,53 @@ def run_batched(dev, iters=5):
             "tuning": tun}
 
 
+def reference_cuda(frames=3):
+    """The reference's own CUDA kernels (PTX compiled from its sources) driven by the
+    restated host orchestration of oracle/ref_harness.cu, on the same SPH frame: full
+    RebuildTopology (radius 2), UpdateAtlas, ClearChannel, InsertPoints +
+    ScatterDensity (radius 2: the reference has no cubic splat) and UpdateApron of the
+    density channel.  Wall-clock time per frame (the reference synchronises on the host
+    many times per rebuild), positions already on the device."""
+    sys.path.insert(0, ORACLE)
+    try:
+        import ref_harness as rh
+        import torch
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "harness not importable: %s" % e}
+    if not rh.available() or not torch.cuda.is_available():
+        return {"unavailable": "reference kernels not built or no GPU"}
+    import workloads
+
+    try:
+        rh.load()
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "harness not loadable: %s" % e}
+    pos0, vel = workloads.sph_slab(n=N_POINTS, seed=0, box=BOX)
+    r = rh.RefGrid(LOGDIM)
+    r.add_channel(0, 3)
+    times = []
+    for f in range(frames + 1):
+        r.set_points(workloads.advect(pos0, vel, DT * f))
+        t0 = time.perf_counter()
+        st = r.rebuild(RADIUS, mode=1)
+        if st != 0:
+            return {"unavailable": "reference rebuild failed: status %d" % st}
+        r.update_atlas()
+        r.clear_channel(0)
+        r.scatter(RADIUS)
+        r.update_apron(0, 0.0)
+        torch.cuda.synchronize()
+        if f > 0:
+            times.append(time.perf_counter() - t0)
+    used = r.used_leaves()
+    r.close()
+    ms = 1e3 * sum(times) / len(times)
+    return {"value": N_POINTS / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_frame": ms, "frames": frames,
+            "active_bricks": used,
+            "path": "reference kernels (cuda_gvdb_module.cu as PTX, --use_fast_math) + restated host "
+                    "orchestration, thrust sort/unique; ScatterDensity + UpdateApron of density"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -500,7 +547,8 @@ def run_reference(args, world, rank):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
                              "sample": "%d independent sub-boxes of 1/128 of the slab per step (%d points, same "
                                        "density), one per host core" % (workers, pts)},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_cuda": reference_cuda() if not args.no_extras else None}
 
 
 def main():

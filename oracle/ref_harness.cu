@@ -17,9 +17,11 @@
 //   InsertPointsSubcell / Gather*          gvdb_volume_gvdb.cpp:4971-5092, 5318-5373
 //   UpdateApron                            gvdb_volume_gvdb.cpp:4418-4457
 // Departures (none changes a result on the inputs the tests use):
-//   - the reference sorts keys with thrust::sort and finds unique keys with
-//     its FindUnique/PrefixSum/Compact kernels; here the same total order and
-//     unique list come from std::sort/std::unique on the host;
+//   - the reference sorts keys with thrust::sort (CU.cu:11-16) and finds unique
+//     keys with its FindUnique/PrefixSum/Compact kernels; here thrust::sort
+//     and thrust::unique on the device give the same total order and unique
+//     list, which are copied to the host for the allocation loop as the
+//     reference copies AUX_UNIQUE_LEVXYZ;
 //   - the min/max of the bounding box is taken on the host (thrust there);
 //   - key buffers are sized generously (the reference's N*depth buffer can overflow);
 //   - ScatterDensity is launched with the kernel's own argument list (the
@@ -29,6 +31,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
+
+#include <thrust/device_ptr.h>
+#include <thrust/sort.h>
+#include <thrust/unique.h>
 
 #include <algorithm>
 #include <cmath>
@@ -270,16 +276,22 @@ int link_levels(rh_grid* g, int depth, unsigned grid_override)
     return 0;
 }
 
-// keys -> sorted unique keys and per-level counts (thrust::sort + FindUniqueBrick)
-void sort_unique(std::vector<uint64_t>& k, int depth, int* levcnt)
+// the first `count` device keys -> sorted unique keys on the host and per-level
+// counts (RadixSortByByte + FindUniqueBrick, VG.cpp:843-928)
+int sort_unique(rh_grid* g, size_t count, int depth, int* levcnt, std::vector<uint64_t>& k)
 {
-    std::sort(k.begin(), k.end());
-    k.erase(std::unique(k.begin(), k.end()), k.end());
+    RH_CK(cuCtxSynchronize());
+    thrust::device_ptr<uint64_t> d((uint64_t*)g->keys.p);
+    thrust::sort(d, d + count);
+    const size_t u = (size_t)(thrust::unique(d, d + count) - d);
+    k.resize(u);
+    if (u) RH_CK(cuMemcpyDtoH(k.data(), g->keys.p, u * 8));
     for (int l = 0; l < depth; l++) levcnt[l] = 0;
     for (uint64_t key : k) {
         int lev = (int)((key >> 48) & 0xFF);
         if (lev != 255 && lev < depth) levcnt[lev]++;
     }
+    return 0;
 }
 
 void alloc_from_keys(rh_grid* g, const std::vector<uint64_t>& k, const int* levcnt, int depth)
@@ -303,14 +315,6 @@ int upload_range_res(rh_grid* g, int depth)
     return 0;
 }
 
-int read_keys(rh_grid* g, size_t count, std::vector<uint64_t>& k)
-{
-    RH_CK(cuCtxSynchronize());
-    k.resize(count);
-    if (count) RH_CK(cuMemcpyDtoH(k.data(), g->keys.p, count * 8));
-    return 0;
-}
-
 int activate_bricks(rh_grid* g, float3 orig, int depth, const int* rootpos)
 {
     alloc_node(g, depth, rootpos[0], rootpos[1], rootpos[2]);
@@ -323,9 +327,8 @@ int activate_bricks(rh_grid* g, float3 orig, int depth, const int* rootpos)
     void* args[] = {&n, &ld, &rr, &pos, &off, &stride, &orig, &keys};
     if (launch(g_mod.calcbrick, n / 512 + 1, 1, 1, 512, 1, 1, args)) return -1;
     std::vector<uint64_t> k;
-    if (read_keys(g, nk, k)) return -1;
     int levcnt[10];
-    sort_unique(k, depth, levcnt);
+    if (sort_unique(g, nk, depth, levcnt, k)) return -1;
     alloc_from_keys(g, k, levcnt, depth);
     if (commit_pools(g) || prepare(g, false) || link_levels(g, depth, 0) || fetch_pools(g)) return -1;
     return 0;
@@ -348,9 +351,8 @@ int activate_extra(rh_grid* g, float radius, float3 orig, int depth)
         return -1;
     }
     std::vector<uint64_t> k;
-    if (read_keys(g, count, k)) return -1;
     int levcnt[10];
-    sort_unique(k, depth, levcnt);
+    if (sort_unique(g, (size_t)count, depth, levcnt, k)) return -1;
     alloc_from_keys(g, k, levcnt, depth);
     if (commit_pools(g) || prepare(g, false) || link_levels(g, depth, 0) || fetch_pools(g)) return -1;
     return 0;
@@ -383,9 +385,8 @@ int activate_incremental(rh_grid* g, float radius, float3 orig, int depth, bool 
         return 0;
     }
     std::vector<uint64_t> k;
-    if (read_keys(g, count, k)) return -1;
     int levcnt[10];
-    sort_unique(k, depth, levcnt);
+    if (sort_unique(g, (size_t)count, depth, levcnt, k)) return -1;
     RH_CK(cuMemcpyDtoH(marker.data(), g->markers.p, (size_t)total * 4));
     for (int i = 0; i < total; i++) g->nodes[0][i].flags = (uint8_t)marker[i];
     alloc_from_keys(g, k, levcnt, depth);
