@@ -477,6 +477,57 @@ def run_batched(dev, iters=5):
             "tuning": tun}
 
 
+def run_fusion(dev, frames=30):
+    """Surface-fusion workload: 30 depth frames (640x480, f = 525) of an analytic
+    scene in 2048^3, each AccumulateTopology (radius 1) + UpdateAtlas + InsertPoints +
+    accumulating TRILINEAR splats of density (w = 1) and of confidence-weighted
+    density, then UpdateApron of both.  Frames are on the device before timing;
+    CUDA-event time per frame on the grid's stream."""
+    import numpy as np
+    import torch
+
+    import gvx
+    import workloads
+
+    fr = [(torch.from_numpy(p).to(dev), torch.from_numpy(c).to(dev)) for p, c in
+          workloads.depth_fusion(frames=frames, seed=3)]
+    stream = torch.cuda.Stream(device=dev)
+    g = gvx.Grid(dev.index)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx.T_FLOAT, 1)
+    g.add_channel(1, gvx.T_FLOAT, 1)
+    g.set_stream(stream.cuda_stream)
+    ms, pts = [], 0
+    with torch.cuda.stream(stream):
+        for pd, cd in fr:
+            n = pd.shape[0]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.set_points(n, pd)
+            g.set_point_attribs()
+            g.rebuild_topology(n, 1.0, mode=gvx.TOPO_ACCUMULATE)
+            g.update_atlas()
+            g.insert_points(n)
+            g.splat(gvx.SPLAT_TRILINEAR, n, 1.0, chan_density=0, accum=True)
+            g.set_point_attribs(weight=cd)
+            g.splat(gvx.SPLAT_TRILINEAR, n, 1.0, chan_density=1, accum=True)
+            g.update_apron(0, 0.0)
+            g.update_apron(1, 0.0)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            pts += n
+        inf = g.info()
+    g.close()
+    steady = ms[2:]  # the first two AccumulateTopology calls are full rebuilds of a growing tree
+    return {"workload": "fusion: %d depth frames 640x480 (f=525) of 8 spheres + 2 planes in 2048^3, N(0,0.5) "
+                        "noise; AccumulateTopology r=1, TRILINEAR density + confidence-weighted density (accum), "
+                        "UpdateApron x2" % frames,
+            "frames": frames, "points": int(pts), "active_bricks": int(inf["used_leaves"]),
+            "ms_per_frame": round(sum(ms) / len(ms), 4), "ms_per_frame_incremental": round(sum(steady) / len(steady), 4),
+            "mpoints_s": round(pts / (sum(ms) * 1e-3) / 1e6, 1)}
+
+
 def reference_cuda(frames=3):
     """The reference's own CUDA kernels (PTX compiled from its sources) driven by the
     restated host orchestration of oracle/ref_harness.cu, on the same SPH frame: full
@@ -560,7 +611,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--points", type=int, default=0, help="smaller runs for profiling (same density)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the differentiable and batched workloads")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the differentiable, batched and fusion workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
@@ -579,6 +631,7 @@ def main():
 
         out["differentiable"] = run_differentiable(torch.device("cuda", 0))
         out["batched"] = run_batched(torch.device("cuda", 0))
+        out["fusion"] = run_fusion(torch.device("cuda", 0))
     if rank == 0:
         if pool is not None:
             out["cpu_baseline"] = cpu_baseline(pool)
