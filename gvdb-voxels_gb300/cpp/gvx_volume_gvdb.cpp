@@ -7,7 +7,10 @@
 
 namespace nvdb {
 
-VolumeGVDB::VolumeGVDB() {}
+VolumeGVDB::VolumeGVDB()
+{
+    for (int& t : chan_type_) t = -1;
+}
 
 VolumeGVDB::~VolumeGVDB()
 {
@@ -89,15 +92,35 @@ void VolumeGVDB::AddChannel(uchar chan, int dt, int apron, int filter, int borde
     if (axiscnt.x > 0 && axiscnt.y > 0 && axiscnt.z > 0)
         check(gvx_set_channel_default(g_, axiscnt.x, axiscnt.y, axiscnt.z));
     check(gvx_add_channel(g_, chan, dt, apron));
+    if (chan < 32) chan_type_[chan] = dt;
     apron_ = apron;
 }
 
-// FillChannel (VG.cpp:2456-2471)
+// FillChannel (VG.cpp:2456-2471): all zero clears the channel; otherwise the
+// FILL operator of the channel's type over the unpacked atlas (no effect on
+// float3/float4 channels)
 void VolumeGVDB::FillChannel(uchar chan, Vector4DF val)
 {
     need_grid();
-    const float v[4] = {val.x, val.y, val.z, val.w};
-    check(gvx_fill_channel(g_, chan, v));
+    if (val.x == 0 && val.y == 0 && val.z == 0 && val.w == 0) {
+        ClearChannel(chan);
+        return;
+    }
+    const int t = chan < 32 ? chan_type_[chan] : -1;
+    const Vector3DF p(val.x, val.y, val.z);
+    if (t == T_FLOAT) Compute(FUNC_FILL_F, chan, 1, p, false, false);
+    else if (t == T_UCHAR) Compute(FUNC_FILL_C, chan, 1, p, false, false);
+    else if (t == T_UCHAR4) Compute(FUNC_FILL_C4, chan, 1, p, false, false);
+}
+
+// Compute (VG.cpp:4534-4558)
+void VolumeGVDB::Compute(int effect, uchar channel, int num_iterations, Vector3DF parameters, bool bUpdateApron,
+                         bool skipOverAprons, float boundval)
+{
+    need_grid();
+    const float p[3] = {parameters.x, parameters.y, parameters.z};
+    check(gvx_compute(g_, effect, channel, num_iterations, p, bUpdateApron ? 1 : 0, skipOverAprons ? 1 : 0,
+                      boundval));
 }
 
 // ClearChannel (VG.cpp:1596-1603)

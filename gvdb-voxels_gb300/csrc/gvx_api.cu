@@ -176,7 +176,7 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->api_keys[0],
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
-                      &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end};
+                      &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -690,6 +690,7 @@ gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t
         return GVX_ERR_INVALID_ARG;
     }
     *dev_ptr = g->ch[chan].data.p;
+    g->ch[chan].apron_valid = false;  // the caller may write the voxels: UpdateApron runs again
     return GVX_OK;
 }
 

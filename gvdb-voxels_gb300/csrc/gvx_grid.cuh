@@ -101,7 +101,8 @@ struct gvx_grid {
     bool atlas_valid = false;  // mValue/atlas map reflect the topology
     int64_t atlas_used = 0;
     GvxChannel ch[GVX_MAXCH];
-    DevBuf amap;  // 4 ints per slot
+    DevBuf amap;       // 4 ints per slot
+    DevBuf atlas_tmp;  // second atlas of the unpacked (Jacobi) smoothing
 
     // points
     GvxPoints pts;

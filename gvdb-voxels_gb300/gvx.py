@@ -20,6 +20,7 @@ ERR_NAMES = {1: "INVALID_ARG", 2: "NOT_CONFIGURED", 3: "CAPACITY", 4: "DEVICE", 
 T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
 TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
 SPLAT_TRILINEAR, SPLAT_CUBIC = 0, 1
+FUNC_FILL_F, FUNC_FILL_C, FUNC_FILL_C4, FUNC_SMOOTH = 110, 111, 112, 113
 
 NODE_DTYPE = np.dtype([("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "u1"),
                        ("pos", "<i4", (3,)), ("value", "<i4", (3,)), ("vrange", "<f4", (3,)),
@@ -80,6 +81,8 @@ def load(path=None):
         "gvx_splat": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_splat_backward": ([vp, i, i, f, fp, vp, vp, vp, vp], i),
         "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
+        "gvx_compute": ([vp, i, i, i, fp, i, i, f], i),
+        "gvx_memcpy": ([i, vp, vp, ctypes.c_size_t, i], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
         "gvx_read_nodes": ([vp, i, vp, i64], i), "gvx_read_childlist": ([vp, i, vp, i64], i),
         "gvx_read_atlas_map": ([vp, vp, i64], i), "gvx_channel_bytes": ([vp, i, ctypes.POINTER(i64)], i),
@@ -130,6 +133,7 @@ class Grid:
         h = ctypes.c_void_p()
         self._check(self.lib.gvx_create(device, ctypes.byref(h)))
         self.h = h
+        self.device = device
         self._types = {}
         self._keep = []
 
@@ -249,6 +253,12 @@ class Grid:
         else:
             self._check(self.lib.gvx_update_apron(self.h, chan, float(boundval)))
 
+    def compute(self, effect, chan, iterations, params, update_apron, skip_over_aprons, boundval=0.0):
+        """Compute(effect, channel, num_iterations, parameters, bUpdateApron, skipOverAprons, boundval)"""
+        p = (ctypes.c_float * 3)(*[float(x) for x in params])
+        self._check(self.lib.gvx_compute(self.h, effect, chan, iterations, p, int(update_apron),
+                                         int(skip_over_aprons), float(boundval)))
+
     # --- queries
     def info(self):
         inf = Info()
@@ -306,6 +316,15 @@ class Grid:
         X, Y, Z = inf["atlas_res"]
         shp = (Z, Y, X) + ((nc,) if nc > 1 else ())
         return out.reshape(shp)
+
+    def write_channel(self, chan, data):
+        """host data in the brick-major native layout (as read_channel returns) into the channel"""
+        dt, _ = _ELEM[self._types[chan]]
+        a = np.ascontiguousarray(data, dt)
+        ptr, nbytes = self.channel_device_ptr(chan)
+        if a.nbytes != nbytes:
+            raise ValueError("channel %d holds %d bytes, got %d" % (chan, nbytes, a.nbytes))
+        self._check(self.lib.gvx_memcpy(self.device, ptr, _ptr(a), nbytes, 0))
 
     def channel_device_ptr(self, chan):
         p = ctypes.c_void_p()

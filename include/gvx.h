@@ -184,6 +184,30 @@ gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const 
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
 gvx_status gvx_update_apron_all(gvx_grid* g);
 
+/* Compute(effect, channel, num_iterations, parameters, bUpdateApron,
+ * skipOverAprons, boundval) (VG.h:355, VG.cpp:4532-4558) for the operators
+ * the point path uses (FUNC_* ids VG.h:201-204, bodies OP.cuh:352-400),
+ * params = (p1, p2, p3):
+ *   GVX_FUNC_FILL_F   float  = p1 (p3 < 0: sum over the axes of sin(12 X / (30 pi)))
+ *   GVX_FUNC_FILL_C   uchar  = p1 truncated, saturating at 0 and 255
+ *   GVX_FUNC_FILL_C4  uchar4 = CLR2INT(p1, p2, p3, 1): the components * 255 ORed
+ *   GVX_FUNC_SMOOTH   float  = (p1 c + sum of the 6 face neighbours) / (p1 + 6) + p2
+ * As in the reference, each operator's own indexing picks its voxels and
+ * skip_over_aprons only sizes the launch: the fills write the atlas voxels
+ * whose coordinates all lie in [1, hi) with hi = the atlas resolution, or
+ * min(8 ceil(bricks * brick / 8) + 1, atlas resolution) when skip_over_aprons;
+ * FUNC_SMOOTH writes every brick interior, from neighbours read before any
+ * write (in the brick's apron; with apron 0, atlas neighbours, 0 outside the
+ * atlas).  update_apron != 0 runs UpdateApron(chan, boundval) after every
+ * iteration.  An operator the channel's type has no body for ->
+ * GVX_ERR_UNSUPPORTED. */
+#define GVX_FUNC_FILL_F 110
+#define GVX_FUNC_FILL_C 111
+#define GVX_FUNC_FILL_C4 112
+#define GVX_FUNC_SMOOTH 113
+gvx_status gvx_compute(gvx_grid* g, int effect, int chan, int iterations, const float params[3], int update_apron,
+                       int skip_over_aprons, float boundval);
+
 /* RadixSortByByte (VG.h:423, VG.cpp:904-928): stable ascending sort of n
  * (key, value) pairs by the low `bits` (1..32) bits of 32-bit keys -- the
  * onesweep radix sort the topology uses for brick keys.  Device pointers; the
@@ -219,7 +243,10 @@ gvx_status gvx_read_atlas_map(gvx_grid* g, int32_t* out4, int64_t cap_slots);
 gvx_status gvx_channel_bytes(gvx_grid* g, int chan, int64_t* bytes);
 gvx_status gvx_read_channel(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
 gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
-/* device pointer of a channel (for in-HBM consumers) */
+/* device pointer of a channel (for in-HBM consumers and producers).  The
+ * pointer stays the same until the atlas is reallocated (UpdateAtlas growing
+ * it, or a channel re-added); the caller may write through it, so the next
+ * UpdateApron of the channel always runs. */
 gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t* bytes);
 /* AtlasRetrieveBrickXYZ (VG.h:412): one brick's interior (res0^3 values of the
  * channel's element size) at the brick whose interior corner is the atlas

@@ -50,6 +50,13 @@
 #define ID_UNDEFL 0xFFFFFFFF
 #define ID_UNDEF64 0xFFFFFFFFFFFFFFFFull
 #endif
+/* Compute operators, as gvdb_volume_gvdb.h:201-204 */
+#ifndef FUNC_FILL_F
+#define FUNC_FILL_F GVX_FUNC_FILL_F
+#define FUNC_FILL_C GVX_FUNC_FILL_C
+#define FUNC_FILL_C4 GVX_FUNC_FILL_C4
+#define FUNC_SMOOTH GVX_FUNC_SMOOTH
+#endif
 /* auxiliary buffer ids of getAux, as gvdb_volume_gvdb.h:219-258 */
 #ifndef AUX_PNTPOS
 #define AUX_PNTPOS 0
@@ -165,6 +172,10 @@ public:
                         int chanLevelset, int chanClr, bool bAccum = false);
     DataPtr& getAux(int id);
 
+    // ---- compute (VG.h:355): FUNC_FILL_F/C/C4 and FUNC_SMOOTH
+    void Compute(int effect, uchar channel, int num_iterations, Vector3DF parameters, bool bUpdateApron,
+                 bool skipOverAprons, float boundval = 0.0f);
+
     // ---- queries (VG.h:453, 637-643)
     uint64 getNumNodes(int lev) { return getNumTotalNodes(lev); }
     uint64 getNumUsedNodes(int lev);
@@ -202,6 +213,7 @@ private:
     std::vector<uint64> mirror_gen_;
     DataPtr pos_, vel_, clr_, pnode_;
     int last_insert_n_ = 0;
+    int chan_type_[32];  // the type each AddChannel gave, -1 for none
     float last_trans_[3] = {0, 0, 0};
     uint64 pnode_gen_ = 0;
 };

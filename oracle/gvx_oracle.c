@@ -1169,6 +1169,7 @@ int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_strid
 int orc_update_apron(orc_grid* g, int chan, double boundval)
 {
     if (!g || chan < 0 || chan >= MAXCH || !g->ch[chan]) return ORC_ERR_ARG;
+    g->degenerate = 0;
     if (g->apron == 0) return ORC_OK;
     pool* p0 = &g->pools[0];
     int P = g->P, b = g->brick, nc = g->ncomp[chan];
@@ -1201,6 +1202,121 @@ int orc_update_apron(orc_grid* g, int chan, double boundval)
                 }
     }
     return g->degenerate ? ORC_ERR_DEGENERATE : ORC_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Compute (VG.cpp:4534-4558) with the operators gvdbOpFillF / FillC / FillC4
+ * (OP.cuh:352-380) and gvdbOpSmooth (OP.cuh:383-400), over every brick of the
+ * atlas.  skip_over_aprons selects GVDB_VOXPACKED (OP.cuh:189-215: brick
+ * interiors, the stencil reading the brick's own apron) or GVDB_VOXUNPACKED
+ * (OP.cuh:220-223: atlas voxels whose every coordinate is >= 1, the stencil
+ * reading atlas neighbours).  In the unpacked form the reference's smoothing
+ * reads voxels other blocks are writing (a race); the oracle reads every value
+ * before the pass (Jacobi), which is the result of any ordering in which the
+ * reads come first. */
+static double* atlas_voxel(orc_grid* g, int chan, int X, int Y, int Z)
+{
+    int P = g->P;
+    int64_t slot = ((int64_t)(Z / P) * g->sub[1] + Y / P) * g->sub[0] + X / P;
+    int64_t loc = ((slot * P + Z % P) * P + Y % P) * P + X % P;
+    return g->ch[chan] + loc * g->ncomp[chan];
+}
+
+/* float -> uint32 as the GPU converts (truncation, saturating at 0 and 2^32-1) */
+static uint32_t f2u_sat(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)v;
+}
+
+/* Compute (VG.cpp:4532-4558): a launch of 8^3-thread blocks over
+ * T = skipOverAprons ? getAtlasPackres : getAtlasRes threads per axis
+ * (gvdb_allocator.cpp:953-961), rounded up to whole blocks, per iteration,
+ * UpdateApron(channel, boundval) after each when bUpdateApron.
+ * The operator's own index macro picks its voxels (OP.cuh:189-223):
+ *  - the fills (GVDB_VOXUNPACKED, OP.cuh:352-380) write atlas voxel
+ *    blockIdx*8 + threadIdx + 1: every voxel with all coordinates in
+ *    [1, min(8*ceil(T/8) + 1, atlasRes)).
+ *  - FUNC_SMOOTH (GVDB_VOXPACKED, OP.cuh:383-400) writes every brick interior
+ *    voxel (packed voxel p -> p + (p / b) * 2a + a; threads past the atlas
+ *    return, so both thread counts give the same voxels), from the six face
+ *    neighbours in the atlas read before any write (LoadSharedMemory,
+ *    OP.cuh:151-181).  With an apron those lie in the brick's own apron; with
+ *    none they can lie in another brick or outside the atlas, where this
+ *    restatement reads 0 (the reference's surface read there is out of range). */
+int orc_compute(orc_grid* g, int effect, int chan, int iterations, const float params[3], int update_apron,
+                int skip_over_aprons, double boundval)
+{
+    if (!g || chan < 0 || chan >= MAXCH || !g->ch[chan] || !params) return ORC_ERR_ARG;
+    const int P = g->P, a = g->apron, b = g->P - 2 * g->apron, nc = g->ncomp[chan];
+    const int res[3] = {g->sub[0] * P, g->sub[1] * P, g->sub[2] * P};
+    int hi[3];
+    for (int k = 0; k < 3; k++) {
+        int T = skip_over_aprons ? g->sub[k] * b : res[k];
+        int cover = (T + 7) / 8 * 8 + 1;
+        hi[k] = cover < res[k] ? cover : res[k];
+    }
+    const int64_t total = (int64_t)res[0] * res[1] * res[2] * nc;
+    const float p1 = params[0], p2 = params[1], p3 = params[2];
+    if (effect == ORC_FUNC_FILL_F || effect == ORC_FUNC_SMOOTH) { if (nc != 1) return ORC_ERR_ARG; }
+    else if (effect == ORC_FUNC_FILL_C4) { if (nc != 4) return ORC_ERR_ARG; }
+    else if (effect != ORC_FUNC_FILL_C) return ORC_ERR_ARG;
+    for (int it = 0; it < iterations; it++) {
+        double* old = (double*)malloc((size_t)total * sizeof(double));
+        if (!old) return ORC_ERR_NOMEM;
+        memcpy(old, g->ch[chan], (size_t)total * sizeof(double));
+        for (int Z = 0; Z < res[2]; Z++)
+            for (int Y = 0; Y < res[1]; Y++)
+                for (int X = 0; X < res[0]; X++) {
+                    int inside;
+                    if (effect == ORC_FUNC_SMOOTH) {
+                        int lx = X % P, ly = Y % P, lz = Z % P;
+                        inside = lx >= a && ly >= a && lz >= a && lx < P - a && ly < P - a && lz < P - a;
+                    } else {
+                        inside = X >= 1 && Y >= 1 && Z >= 1 && X < hi[0] && Y < hi[1] && Z < hi[2];
+                    }
+                    if (!inside) continue;
+                    double* out = atlas_voxel(g, chan, X, Y, Z);
+                    switch (effect) {
+                    case ORC_FUNC_FILL_F:
+                        if (p3 < 0)
+                            out[0] = (double)(sinf((float)((double)(X * 12) / (3.141592 * 30.0))) +
+                                              sinf((float)((double)(Y * 12) / (3.141592 * 30.0))) +
+                                              sinf((float)((double)(Z * 12) / (3.141592 * 30.0))));
+                        else
+                            out[0] = p1;
+                        break;
+                    case ORC_FUNC_FILL_C: /* static_cast<uchar>(p1) on the GPU: truncated, saturating at 0 and 255 */
+                        out[0] = (double)(f2u_sat(p1) > 255u ? 255u : f2u_sat(p1));
+                        break;
+                    case ORC_FUNC_FILL_C4: { /* CLR2INT (OP.cuh:20): components * 255 ORed, unmasked */
+                        uint32_t c = (255u << 24) | (f2u_sat(p3 * 255.0f) << 16) | (f2u_sat(p2 * 255.0f) << 8) |
+                                     f2u_sat(p1 * 255.0f);
+                        for (int k = 0; k < 4; k++) out[k] = (double)((c >> (8 * k)) & 255u);
+                        break;
+                    }
+                    default: { /* ORC_FUNC_SMOOTH */
+                        const int64_t base = out - g->ch[chan];
+                        double v = p1 * old[base];
+                        static const int d[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+                        for (int k = 0; k < 6; k++) {
+                            int nx = X + d[k][0], ny = Y + d[k][1], nz = Z + d[k][2];
+                            if (nx < 0 || ny < 0 || nz < 0 || nx >= res[0] || ny >= res[1] || nz >= res[2]) continue;
+                            v += old[atlas_voxel(g, chan, nx, ny, nz) - g->ch[chan]];
+                        }
+                        out[0] = v / ((double)p1 + 6.0) + p2;
+                        break;
+                    }
+                    }
+                }
+        free(old);
+        if (update_apron) {
+            int rc = orc_update_apron(g, chan, boundval);
+            if (rc) return rc;
+        }
+    }
+    return ORC_OK;
 }
 
 /* ------------------------------------------------------------------ */

@@ -113,6 +113,13 @@ int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_strid
 
 int orc_update_apron(orc_grid* g, int chan, double boundval);
 
+/* Compute(effect, chan, iterations, (p1,p2,p3), bUpdateApron, skipOverAprons,
+ * boundval) (VG.cpp:4534-4558) for the operators below, numbered as the
+ * reference's FUNC_* ids (VG.h:201-204) */
+enum { ORC_FUNC_FILL_F = 110, ORC_FUNC_FILL_C = 111, ORC_FUNC_FILL_C4 = 112, ORC_FUNC_SMOOTH = 113 };
+int orc_compute(orc_grid* g, int effect, int chan, int iterations, const float params[3], int update_apron,
+                int skip_over_aprons, double boundval);
+
 /* readback of a channel in the native brick-major layout:
  * slot s, padded local (lx,ly,lz), component c ->
  *   out[((s*P + lz)*P + ly)*P + lx)*ncomp + c],  P = brick + 2*apron */

@@ -16,6 +16,7 @@ SRC = os.path.join(HERE, "gvx_oracle.c")
 
 OK, ERR_ARG, ERR_DEPTH, ERR_DEGENERATE, ERR_STATE, ERR_NOMEM = 0, 1, 2, 3, 4, 5
 TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
+FUNC_FILL_F, FUNC_FILL_C, FUNC_FILL_C4, FUNC_SMOOTH = 110, 111, 112, 113
 SPLAT_TRILINEAR, SPLAT_CUBIC, SPLAT_REF_SCATTER, SPLAT_GATHER_DENSITY, SPLAT_GATHER_LEVELSET = 0, 1, 2, 3, 4
 T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
 
@@ -56,6 +57,7 @@ def load():
         "orc_atlas_subdim": ([vp, vp], i), "orc_get_atlas_map": ([vp, vp, i], i),
         "orc_splat": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, i, i, i, i, i, f], i),
         "orc_gather": ([vp, i, i, vp, i, vp, f, f, vp, i, i, i, i, vp], i),
+        "orc_compute": ([vp, i, i, i, vp, i, i, d], i),
         "orc_update_apron": ([vp, i, d], i), "orc_channel_size": ([vp, i], i64),
         "orc_read_channel": ([vp, i, vp, i64], i), "orc_write_channel": ([vp, i, vp, i64], i),
         "orc_activate_space_cpu": ([i, vp, i, vp, i, vp, vp, i, vp], i),
@@ -188,6 +190,12 @@ class Oracle:
                                  float(radius_ins), _p(t), subcell, chan, chan_clr, int(accum), ctypes.byref(n))
         self._ck(st, "gather", allow_degenerate)
         return n.value
+
+    def compute(self, effect, chan, iterations, params, update_apron, skip_over_aprons, boundval=0.0):
+        """Compute (VG.cpp:4534-4558): FUNC_FILL_F/C/C4 (110-112), FUNC_SMOOTH (113)"""
+        p = np.ascontiguousarray(params, np.float32)
+        self._ck(self.lib.orc_compute(self.h, effect, chan, iterations, _p(p), int(update_apron),
+                                      int(skip_over_aprons), float(boundval)), "compute")
 
     def update_apron(self, chan, boundval=0.0):
         self._ck(self.lib.orc_update_apron(self.h, chan, float(boundval)), "update_apron")

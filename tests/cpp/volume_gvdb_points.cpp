@@ -2,11 +2,12 @@
 // the call sequence of an application of the reference that builds a volume
 // from points (configure, channel, AllocData/CommitData/SetPoints,
 // RebuildTopology, FinishTopology, UpdateAtlas, InsertPoints, ScatterDensity or
-// the cubic Splat, UpdateApron), dumping the node pools, the leaf of every
+// the cubic Splat, UpdateApron, Compute(FUNC_SMOOTH)), dumping the node pools, the leaf of every
 // point and every active brick's values for the test to compare.
 //
 //   volume_gvdb_points <in.bin> <out.bin>
-// in:  int32 n, int32 mode (0 ScatterDensity, 1 cubic Splat), float radius, n x float3
+// in:  int32 n, int32 mode (0 ScatterDensity, 1 cubic Splat, 2 ScatterDensity then two
+//      FUNC_SMOOTH iterations as gSprayDeposit runs them), float radius, n x float3
 // out: int32 levels; per level uint64 count + count 64-byte nodes; uint64 used;
 //      n int32 leaf ids (AUX_PNODE); per active leaf in pool order, brick^3 floats
 #include <cstdio>
@@ -52,9 +53,10 @@ int main(int argc, char** argv)
         gvdb.UpdateAtlas();
         gvdb.ClearChannel(0);
         gvdb.InsertPoints(n, Vector3DF(0, 0, 0), false);
-        if (mode == 0) {
+        if (mode == 0 || mode == 2) {
             gvdb.ScatterDensity(n, radius, 1.0f, Vector3DF(0, 0, 0), true, false);
             gvdb.UpdateApron(0, 0.0f);
+            if (mode == 2) gvdb.Compute(FUNC_SMOOTH, 0, 2, Vector3DF(4, 0, 0), true, true);
         } else {
             gvdb.Splat(GVX_SPLAT_CUBIC, n, radius, Vector3DF(0, 0, 0), 0, -1);
         }

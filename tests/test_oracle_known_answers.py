@@ -216,3 +216,99 @@ def test_cpu_activate_space_leaf_set(orc):
     b = {tuple(x) for x in o.nodes(0)["pos"].tolist()}
     assert a == b
     assert root == o.root_level()
+
+
+def _atlas_dense(bricks, sub):
+    """brick-major (slots, P, P, P) -> the atlas as (Z, Y, X)"""
+    P = bricks.shape[1]
+    sx, sy, sz = sub
+    return bricks.reshape(sz, sy, sx, P, P, P).transpose(0, 3, 1, 4, 2, 5).reshape(sz * P, sy * P, sx * P)
+
+
+@pytest.mark.parametrize("skip", [True, False])
+def test_compute_smooth_known_values(orc, skip):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    o.update_atlas()
+    P = 10
+    nslots = int(np.prod(o.atlas_subdim()))
+    data = np.random.default_rng(3).integers(-64, 64, (nslots, P, P, P)) / 8.0
+    o.write_channel(0, data)
+    p1, p2 = 4.0, 0.25
+    o.compute(orc.FUNC_SMOOTH, 0, 1, (p1, p2, 0.0), update_apron=False, skip_over_aprons=skip)
+    # gvdbOpSmooth (OP.cuh:383-400): every brick interior voxel, whatever skipOverAprons
+    d = data
+    nb = (d[:, 1:-1, 1:-1, :-2] + d[:, 1:-1, 1:-1, 2:] + d[:, 1:-1, :-2, 1:-1] + d[:, 1:-1, 2:, 1:-1] +
+          d[:, :-2, 1:-1, 1:-1] + d[:, 2:, 1:-1, 1:-1])
+    want = data.copy()
+    want[:, 1:-1, 1:-1, 1:-1] = (p1 * d[:, 1:-1, 1:-1, 1:-1] + nb) / (p1 + 6.0) + p2
+    np.testing.assert_allclose(o.read_channel(0), want, rtol=0, atol=1e-12)
+
+
+def test_compute_smooth_then_apron(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    o.update_atlas()
+    data = np.zeros((int(np.prod(o.atlas_subdim())), 10, 10, 10))
+    data[0, 1:-1, 1:-1, 1:-1] = 1.0
+    o.write_channel(0, data)
+    o.compute(orc.FUNC_SMOOTH, 0, 2, (4.0, 0.0, 0.0), update_apron=True, skip_over_aprons=True, boundval=3.0)
+    got = o.read_channel(0)
+    # leaf 0 has no active neighbours: after each iteration its apron holds boundval 3
+    assert got[0, 0, 5, 5] == 3.0 and got[0, 9, 9, 9] == 3.0
+    # first iteration reads apron 0s: a corner interior voxel has 3 interior neighbours,
+    # (4 + 3) / 10 = 0.7; the second reads the apron's 3s
+    c1 = np.zeros((10, 10, 10))
+    c1[1:-1, 1:-1, 1:-1] = 1.0
+    it1 = c1.copy()
+    it1[1:-1, 1:-1, 1:-1] = (4 * c1[1:-1, 1:-1, 1:-1] + c1[1:-1, 1:-1, :-2] + c1[1:-1, 1:-1, 2:] +
+                             c1[1:-1, :-2, 1:-1] + c1[1:-1, 2:, 1:-1] + c1[:-2, 1:-1, 1:-1] + c1[2:, 1:-1, 1:-1]) / 10
+    assert math.isclose(it1[1, 1, 1], 0.7)
+    it1[0, :, :] = it1[-1, :, :] = it1[:, 0, :] = it1[:, -1, :] = it1[:, :, 0] = it1[:, :, -1] = 3.0
+    it2 = it1.copy()
+    it2[1:-1, 1:-1, 1:-1] = (4 * it1[1:-1, 1:-1, 1:-1] + it1[1:-1, 1:-1, :-2] + it1[1:-1, 1:-1, 2:] +
+                             it1[1:-1, :-2, 1:-1] + it1[1:-1, 2:, 1:-1] + it1[:-2, 1:-1, 1:-1] + it1[2:, 1:-1, 1:-1]) / 10
+    np.testing.assert_allclose(got[0, 1:-1, 1:-1, 1:-1], it2[1:-1, 1:-1, 1:-1], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("skip", [False, True])
+def test_compute_fill_region(orc, skip):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    o.update_atlas()
+    sub = o.atlas_subdim()
+    assert sub == (16, 16, 1)
+    o.compute(orc.FUNC_FILL_F, 0, 1, (2.5, 0.0, 0.0), update_apron=False, skip_over_aprons=skip)
+    dense = _atlas_dense(o.read_channel(0), sub)
+    # GVDB_VOXUNPACKED (OP.cuh:220-223): voxel blockIdx*8 + threadIdx + 1 over 8^3 blocks covering
+    # getAtlasRes (160, 160, 10) or, skipping aprons, getAtlasPackres (128, 128, 8)
+    hi = (129, 129, 9) if skip else (160, 160, 10)
+    want = np.zeros_like(dense)
+    want[1:hi[2], 1:hi[1], 1:hi[0]] = 2.5
+    assert np.array_equal(dense, want)
+
+
+def test_compute_fill_pattern_and_colours(orc):
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    o.add_channel(1, orc.T_UCHAR4)
+    o.add_channel(2, orc.T_UCHAR)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    o.update_atlas()
+    sub = o.atlas_subdim()
+    o.compute(orc.FUNC_FILL_F, 0, 1, (0.0, 0.0, -1.0), update_apron=False, skip_over_aprons=False)
+    dense = _atlas_dense(o.read_channel(0), sub)
+    s = lambda i: math.sin(i * 12 / (math.pi * 30.0))  # noqa: E731  (3.141592 in the reference)
+    assert math.isclose(dense[3, 7, 11], s(11) + s(7) + s(3), abs_tol=1e-5)
+    # CLR2INT (OP.cuh:20): 255 * (0.5, 1, 2, 1) truncated and ORed unmasked: the 510 of blue
+    # spills into alpha's byte
+    o.compute(orc.FUNC_FILL_C4, 1, 1, (0.5, 1.0, 2.0), update_apron=False, skip_over_aprons=False)
+    c = o.read_channel(1)
+    assert c[0, 1, 1, 1].tolist() == [127, 255, 254, 255]
+    assert c[0, 0, 0, 0].tolist() == [0, 0, 0, 0]
+    for p1, want in ((7.9, 7), (300.0, 255), (-3.0, 0)):
+        o.compute(orc.FUNC_FILL_C, 2, 1, (p1, 0.0, 0.0), update_apron=False, skip_over_aprons=False)
+        assert o.read_channel(2)[0, 1, 1, 1] == want
