@@ -332,9 +332,8 @@ void VolumeGVDB::InsertPointsSubcell(int subcell_size, int num_pnts, float pRadi
 void VolumeGVDB::ScatterDensity(int num_pnts, float radius, float amp, Vector3DF trans, bool expand, bool avgColor)
 {
     need_grid();
-    if (avgColor) throw GvxError(GVX_ERR_UNSUPPORTED, "ScatterDensity: colour averaging is not available");
     const float t[3] = {trans.x, trans.y, trans.z};
-    check(gvx_scatter_density(g_, num_pnts, radius, amp, t, expand ? 1 : 0));
+    check(gvx_scatter_density(g_, num_pnts, radius, amp, t, expand ? 1 : 0, avgColor ? 1 : 0));
 }
 
 // GatherDensity (VG.cpp:5318-5344)
@@ -355,6 +354,35 @@ void VolumeGVDB::GatherLevelSet(int subcell_size, int num_pnts, float radius, Ve
     const float t[3] = {trans.x, trans.y, trans.z};
     check(gvx_gather_levelset(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanLevelset, chanClr,
                               bAccum ? 1 : 0));
+}
+
+// InsertPointsSubcell_FP16 (VG.cpp:5094-5190)
+void VolumeGVDB::InsertPointsSubcell_FP16(int subcell_size, int num_pnts, float pRadius, Vector3DF trans,
+                                          int& pSCPntsLength)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_insert_points_subcell_fp16(g_, subcell_size, num_pnts, pRadius, t, &pSCPntsLength));
+}
+
+// GatherLevelSet_FP16 (VG.cpp:5375-5401)
+void VolumeGVDB::GatherLevelSet_FP16(int subcell_size, int num_pnts, float radius, Vector3DF trans,
+                                     int& pSCPntsLength, int chanLevelSet, int chanClr)
+{
+    need_grid();
+    const float t[3] = {trans.x, trans.y, trans.z};
+    check(gvx_gather_levelset_fp16(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanLevelSet, chanClr));
+}
+
+// ConvertAndTransform (VG.cpp:5668-5682) on the DataPtrs' device buffers
+void VolumeGVDB::ConvertAndTransform(DataPtr& psrc, char psrcbits, DataPtr& pdest, char pdestbits, int num_pnts,
+                                     Vector3DF wMin, Vector3DF wDelta, Vector3DF trans, Vector3DF scal)
+{
+    need_grid();
+    const float mn[3] = {wMin.x, wMin.y, wMin.z}, dl[3] = {wDelta.x, wDelta.y, wDelta.z};
+    const float tr[3] = {trans.x, trans.y, trans.z}, sc[3] = {scal.x, scal.y, scal.z};
+    check(gvx_convert_and_transform(g_, (const void*)psrc.gpu, psrcbits, (void*)pdest.gpu, pdestbits, num_pnts, mn,
+                                    dl, tr, sc));
 }
 
 // getAux (VG.h:625) for the point buffers and AUX_PNODE, the leaf of every

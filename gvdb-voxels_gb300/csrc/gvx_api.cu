@@ -176,7 +176,8 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->d_counts, &g->d_err, &g->d_bbox, &g->host_stage, &g->api_keys[0],
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
-                      &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp};
+                      &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp,
+                      &g->sc_q, &g->sc_qclr};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -348,6 +349,11 @@ gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, i
         gvx_set_error("SetPoints: need float3 positions with a stride >= 12 and 4-byte alignment");
         return GVX_ERR_INVALID_ARG;
     }
+    if (((uintptr_t)pos & 3) || ((uintptr_t)vel & 3) ||
+        (clr && (clr_stride < 4 || (clr_stride & 3) || (clr_offset & 3) || ((uintptr_t)clr & 3)))) {
+        gvx_set_error("SetPoints: buffers must be 4-byte aligned, colours 4 bytes (uchar4) per point");
+        return GVX_ERR_INVALID_ARG;
+    }
     g->pts.n = n;
     g->pts.pos = (const char*)pos;
     g->pts.pos_off = pos_offset;
@@ -446,11 +452,12 @@ gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* 
     return GVX_OK;
 }
 
-gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3], int expand)
+gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3], int expand,
+                               int avg_color)
 {
     GVX_GUARD(g);
     (void)amp;  // unused by the reference kernel as well (PT.cuh:525-573)
-    return gvx_scatter_ref(g, n, radius, trans, expand);
+    return gvx_scatter_ref(g, n, radius, trans, expand, avg_color);
 }
 
 gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int sc_len,

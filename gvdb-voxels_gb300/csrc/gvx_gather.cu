@@ -7,6 +7,10 @@
 //   gvdbCalcSubcellPos                  cuda_gvdb_particles.cuh:677-694
 //   VolumeGVDB::GatherDensity / GatherLevelSet   gvdb_volume_gvdb.cpp:5318-5373
 //   gvdbGatherDensity / gvdbGatherLevelSet       cuda_gvdb_particles.cuh:696-773
+//   VolumeGVDB::InsertPointsSubcell_FP16         gvdb_volume_gvdb.cpp:5094-5190
+//   gvdbInsertSubcell_fp16                       cuda_gvdb_particles.cuh:154-216
+//   VolumeGVDB::GatherLevelSet_FP16              gvdb_volume_gvdb.cpp:5375-5401
+//   gvdbGatherLevelSet_fp16                      cuda_gvdb_particles.cuh:775-813
 //
 // Every point adds itself to each subcell (size s) of an existing leaf that
 // its box [(int(p-r)/s)s, (int(p+1+r)/s)s] touches; every voxel of every
@@ -120,6 +124,33 @@ __global__ void k_sc_copy(const uint32_t* __restrict__ skeys, const uint32_t* __
     if (k + 1 == m || skeys[k + 1] != key) end[key] = k + 1;
 }
 
+// FP16 lists (gvdbInsertSubcell_fp16, PT.cuh:204-207): each entry's translated
+// position as 16-bit fractions of the last GetBoundingBox's box,
+// (w - mPosMin) / mPosRange * 65535 truncated, each float step rounded on its own
+__global__ void k_sc_copy_q(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t m,
+                            const char* pos, int off, int stride, const char* clr, int clr_off, int clr_stride,
+                            float3 t, float3 qmin, float3 qrange, uint2* q, uint32_t* qclr, uint32_t* beg,
+                            uint32_t* end)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    const uint32_t i = svals[k];
+    const float* p = (const float*)(pos + (size_t)i * (size_t)stride + off);
+    const float w[3] = {__fadd_rn(p[0], t.x), __fadd_rn(p[1], t.y), __fadd_rn(p[2], t.z)};
+    const float mn[3] = {qmin.x, qmin.y, qmin.z}, rg[3] = {qrange.x, qrange.y, qrange.z};
+    uint32_t u[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float f = __fmul_rn(__fdiv_rn(__fsub_rn(w[a], mn[a]), rg[a]), 65535.0f);
+        u[a] = f > 0.0f ? (f >= 65535.0f ? 65535u : __float2uint_rz(f)) : 0u;  // saturating, NaN -> 0
+    }
+    q[k] = make_uint2(u[0] | (u[1] << 16), u[2]);
+    if (qclr) qclr[k] = clr ? *(const uint32_t*)(clr + (size_t)i * (size_t)clr_stride + clr_off) : 0u;
+    const uint32_t key = skeys[k];
+    if (k == 0 || skeys[k - 1] != key) beg[key] = k;
+    if (k + 1 == m || skeys[k + 1] != key) end[key] = k + 1;
+}
+
 namespace {
 
 struct GatherArgs {
@@ -148,7 +179,97 @@ __device__ __forceinline__ uint32_t clr_to_char(const float c[4])
     return u;
 }
 
+struct GatherQArgs {
+    uint32_t nsub;
+    int sc, scdim, spb, P, apron;
+    const int* slot_leaf;
+    const GvxNode* nodes0;
+    const uint32_t* beg;
+    const uint32_t* end;
+    const uint2* q;
+    const uint32_t* qclr;  // null: no colours
+    float qmin[3], qrange[3];
+    float radius;
+    float* out;           // T_FLOAT channel
+    uint32_t* clr_out;    // any 4-byte channel, or null
+};
+
+// float -> uint32 as the GPU's conversion does: truncation, saturating, NaN -> 0
+__device__ __forceinline__ uint32_t f2u_sat(float v)
+{
+    return v > 0.0f ? (v >= 4294967296.0f ? 0xFFFFFFFFu : __float2uint_rz(v)) : 0u;
+}
+
 }  // namespace
+
+// GatherLevelSet_FP16 (PT.cuh:775-813): one warp per subcell, VPL voxels per
+// lane.  Every voxel of every subcell: dist from 3, min(|p - v| - R) over the
+// list, positions read back as q / 65535 * range + min; with colours, the sum
+// of INT2CLR(c) / |p - v| from 0 (uninitialised in the reference) written as
+// particles.cuh's CLR2INT (components * 255 added, carries included).  Every
+// float step is rounded on its own, as the oracle restates them.
+template <int VPL>
+__global__ void k_gather_fp16(GatherQArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int sc = a.sc, nv = sc * sc * sc;
+    for (uint32_t s = warp0; s < a.nsub; s += nwarps) {
+        const uint32_t slot = s / (uint32_t)a.spb;
+        const int loc = (int)(s - slot * (uint32_t)a.spb);
+        const GvxNode& nd = a.nodes0[a.slot_leaf[slot]];
+        const int so[3] = {(loc % a.scdim) * sc, ((loc / a.scdim) % a.scdim) * sc, (loc / a.scdim / a.scdim) * sc};
+        const uint32_t jb = a.beg[s], je = a.end[s];
+        for (int v0 = 0; v0 < nv; v0 += 32 * VPL) {
+            float dist[VPL], wx[VPL], wy[VPL], wz[VPL], c4[VPL][4];
+            size_t idx[VPL];
+#pragma unroll
+            for (int q = 0; q < VPL; q++) {
+                const int v = v0 + q * 32 + lane;
+                const int vv = v < nv ? v : 0;
+                const int lx = so[0] + vv % sc, ly = so[1] + (vv / sc) % sc, lz = so[2] + vv / (sc * sc);
+                wx[q] = (float)(nd.pos[0] + lx);
+                wy[q] = (float)(nd.pos[1] + ly);
+                wz[q] = (float)(nd.pos[2] + lz);
+                idx[q] = (((size_t)slot * a.P + (lz + a.apron)) * a.P + (ly + a.apron)) * a.P + (lx + a.apron);
+                dist[q] = 3.0f;
+                c4[q][0] = c4[q][1] = c4[q][2] = c4[q][3] = 0.0f;
+            }
+            for (uint32_t j = jb; j < je; j++) {
+                const uint2 qq = a.q[j];
+                const uint32_t u[3] = {qq.x & 0xFFFFu, qq.x >> 16, qq.y};
+                float p[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    p[k] = __fadd_rn(__fmul_rn(__fdiv_rn((float)u[k], 65535.0f), a.qrange[k]), a.qmin[k]);
+                const uint32_t cu = a.clr_out ? a.qclr[j] : 0u;
+#pragma unroll
+                for (int q = 0; q < VPL; q++) {
+                    const float dx = __fsub_rn(p[0], wx[q]), dy = __fsub_rn(p[1], wy[q]), dz = __fsub_rn(p[2], wz[q]);
+                    const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    const float c = __fsqrt_rn(s2);
+                    dist[q] = fminf(dist[q], __fsub_rn(c, a.radius));
+                    if (a.clr_out) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            c4[q][k] = __fadd_rn(c4[q][k], __fdiv_rn(__fdiv_rn((float)((cu >> (8 * k)) & 255u), 255.0f), c));
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < VPL; q++) {
+                if (v0 + q * 32 + lane >= nv) continue;
+                a.out[idx[q]] = dist[q];
+                if (!a.clr_out) continue;
+                uint32_t u = 0u;
+#pragma unroll
+                for (int k = 0; k < 4; k++) u += f2u_sat(__fmul_rn(c4[q][k], 255.0f)) << (8 * k);
+                a.clr_out[idx[q]] = u;
+            }
+        }
+    }
+}
 
 // one warp per subcell; VPL voxels per lane per pass over the subcell's list
 template <int VPL>
@@ -216,9 +337,10 @@ __global__ void k_gather(GatherArgs a)
     }
 }
 
-extern "C" {
-
-gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int* sc_len)
+// InsertPointsSubcell and InsertPointsSubcell_FP16: the same lists, FP32
+// translated positions or 16-bit fractions of the bounding box
+static gvx_status insert_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int* sc_len,
+                                 bool fp16)
 {
     if (!g) {
         gvx_set_error("null grid handle");
@@ -263,6 +385,12 @@ gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radi
     GVX_CK(cudaMemsetAsync(g->sc_beg.p, 0, (size_t)nsub * 4, st));
     GVX_CK(cudaMemsetAsync(g->sc_end.p, 0, (size_t)nsub * 4, st));
     const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    // mPosMin / mPosRange of the last GetBoundingBox (VG.cpp:5452-5462), host floats as the reference's
+    float qmin[3], qrange[3];
+    for (int k = 0; k < 3; k++) {
+        qmin[k] = g->bbox_min[k];
+        qrange[k] = g->bbox_max[k] - g->bbox_min[k];
+    }
 
     ScPointArgs a;
     memset(&a, 0, sizeof(a));
@@ -296,7 +424,12 @@ gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radi
         GVX_CK(gvx_ensure(g->sc_keys[1], (size_t)m * 4));
         GVX_CK(gvx_ensure(g->sc_vals[0], (size_t)m * 4));
         GVX_CK(gvx_ensure(g->sc_vals[1], (size_t)m * 4));
-        GVX_CK(gvx_ensure(g->sc_pts, (size_t)m * sizeof(float4)));
+        if (fp16) {
+            GVX_CK(gvx_ensure(g->sc_q, (size_t)m * sizeof(uint2)));
+            if (g->pts.clr) GVX_CK(gvx_ensure(g->sc_qclr, (size_t)m * 4));
+        } else {
+            GVX_CK(gvx_ensure(g->sc_pts, (size_t)m * sizeof(float4)));
+        }
         a.cnt = g->sc_off.as<uint32_t>();
         a.keys = g->sc_keys[0].as<uint32_t>();
         a.vals = g->sc_vals[0].as<uint32_t>();
@@ -308,10 +441,20 @@ gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radi
         gvx_status rc = gvx_sort_pairs(kk, vv, m, std::max(1, ceil_log2(nsub)), g->sort, false, st,
                                        g->d_err.as<uint32_t>(), &res, &g->launches);
         if (rc) return rc;
-        k_sc_copy<<<blocks_for(m, 256), 256, 0, st>>>(kk[res], vv[res], m, g->pts.pos, g->pts.pos_off,
-                                                      g->pts.pos_stride, g->pts.clr, g->pts.clr_off,
-                                                      g->pts.clr_stride, t[0], t[1], t[2], g->sc_pts.as<float4>(),
-                                                      g->sc_beg.as<uint32_t>(), g->sc_end.as<uint32_t>());
+        if (fp16) {
+            k_sc_copy_q<<<blocks_for(m, 256), 256, 0, st>>>(
+                kk[res], vv[res], m, g->pts.pos, g->pts.pos_off, g->pts.pos_stride, g->pts.clr, g->pts.clr_off,
+                g->pts.clr_stride, make_float3(t[0], t[1], t[2]), make_float3(qmin[0], qmin[1], qmin[2]),
+                make_float3(qrange[0], qrange[1], qrange[2]), g->sc_q.as<uint2>(),
+                g->pts.clr ? g->sc_qclr.as<uint32_t>() : nullptr, g->sc_beg.as<uint32_t>(),
+                g->sc_end.as<uint32_t>());
+        } else {
+            k_sc_copy<<<blocks_for(m, 256), 256, 0, st>>>(kk[res], vv[res], m, g->pts.pos, g->pts.pos_off,
+                                                          g->pts.pos_stride, g->pts.clr, g->pts.clr_off,
+                                                          g->pts.clr_stride, t[0], t[1], t[2],
+                                                          g->sc_pts.as<float4>(), g->sc_beg.as<uint32_t>(),
+                                                          g->sc_end.as<uint32_t>());
+        }
         g->launches++;
     }
     GVX_CK(cudaGetLastError());
@@ -321,8 +464,89 @@ gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radi
     g->sc_len = m;
     g->sc_nsub = (uint32_t)nsub;
     g->sc_has_clr = g->pts.clr != nullptr;
+    g->sc_fp16 = fp16;
+    for (int k = 0; k < 3; k++) {
+        g->sc_qmin[k] = qmin[k];
+        g->sc_qrange[k] = qrange[k];
+    }
     g->sc_valid = true;
     if (sc_len) *sc_len = (int)m;
+    return GVX_OK;
+}
+
+extern "C" {
+
+gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int* sc_len)
+{
+    return insert_subcell(g, subcell, n, radius, trans, sc_len, false);
+}
+
+gvx_status gvx_insert_points_subcell_fp16(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                                          int* sc_len)
+{
+    return insert_subcell(g, subcell, n, radius, trans, sc_len, true);
+}
+
+// GatherLevelSet_FP16 (VG.cpp:5375-5401): no accumulation, no entry-count test,
+// the colour (when the lists hold colours) into any 4-byte channel, after the
+// level set (the same channel may take both: the colour then stays)
+gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int sc_len,
+                                    int chan_levelset, int chan_clr)
+{
+    if (!g) {
+        gvx_set_error("null grid handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaSetDevice(g->device));
+    (void)n;      // the lists hold the points
+    (void)trans;  // stored translated by the insert
+    (void)sc_len;
+    if (g->root_level < 0 || g->used_leaves == 0) return GVX_OK;  // num_brick == 0 (VG.cpp:5378)
+    const int cl = chan_levelset;
+    if (cl < 0 || cl >= GVX_MAXCH || !g->ch[cl].used || g->ch[cl].type != GVX_T_FLOAT) {
+        gvx_set_error("GatherLevelSet_FP16: channel %d is not a T_FLOAT channel", cl);
+        return GVX_ERR_INVALID_ARG;
+    }
+    const bool want_clr = g->sc_has_clr && chan_clr >= 0;
+    if (want_clr && (chan_clr >= GVX_MAXCH || !g->ch[chan_clr].used || g->ch[chan_clr].elem_bytes != 4)) {
+        gvx_set_error("GatherLevelSet_FP16: colour channel %d is not a 4-byte channel", chan_clr);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (!g->sc_valid || !g->sc_fp16 || g->sc_size != subcell || !g->atlas_valid) {
+        gvx_set_error("GatherLevelSet_FP16: no FP16 subcell lists of size %d for this topology "
+                      "(call InsertPointsSubcell_FP16 first)", subcell);
+        return GVX_ERR_STATE;
+    }
+    GatherQArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nsub = g->sc_nsub;
+    a.sc = subcell;
+    a.scdim = g->brick / subcell;
+    a.spb = a.scdim * a.scdim * a.scdim;
+    a.P = g->P;
+    a.apron = g->apron;
+    a.slot_leaf = g->slot_leaf.as<int>();
+    a.nodes0 = g->nodes[0].as<GvxNode>();
+    a.beg = g->sc_beg.as<uint32_t>();
+    a.end = g->sc_end.as<uint32_t>();
+    a.q = g->sc_q.as<uint2>();
+    a.qclr = want_clr ? g->sc_qclr.as<uint32_t>() : nullptr;
+    for (int k = 0; k < 3; k++) {
+        a.qmin[k] = g->sc_qmin[k];
+        a.qrange[k] = g->sc_qrange[k];
+    }
+    a.radius = radius;
+    a.out = g->ch[cl].data.as<float>();
+    a.clr_out = want_clr ? g->ch[chan_clr].data.as<uint32_t>() : nullptr;
+    const unsigned blocks = std::min<unsigned>(blocks_for((uint64_t)a.nsub * 32u, 256), 152u * 16u);
+    if (subcell * subcell * subcell <= 64)
+        k_gather_fp16<2><<<blocks, 256, 0, g->stream>>>(a);
+    else
+        k_gather_fp16<8><<<blocks, 256, 0, g->stream>>>(a);
+    g->launches++;
+    GVX_CK(cudaGetLastError());
+    g->ch[cl].apron_valid = false;
+    if (a.clr_out) g->ch[chan_clr].apron_valid = false;
     return GVX_OK;
 }
 
@@ -343,9 +567,9 @@ gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, 
         gvx_set_error("%s: colour channel %d is not a T_UCHAR4 channel", what, chan_clr);
         return GVX_ERR_INVALID_ARG;
     }
-    if (!g->sc_valid || g->sc_size != subcell || !g->atlas_valid) {
-        gvx_set_error("%s: no subcell lists of size %d for this topology (call InsertPointsSubcell first)", what,
-                      subcell);
+    if (!g->sc_valid || g->sc_fp16 || g->sc_size != subcell || !g->atlas_valid) {
+        gvx_set_error("%s: no FP32 subcell lists of size %d for this topology (call InsertPointsSubcell first)",
+                      what, subcell);
         return GVX_ERR_STATE;
     }
     GatherArgs a;

@@ -136,6 +136,10 @@ struct gvx_grid {
     DevBuf sc_keys[2], sc_vals[2];  // entries: subcell index, point index
     DevBuf sc_pts;                  // float4 per entry: translated position, colour bits in .w
     DevBuf sc_beg, sc_end;          // per subcell: [beg, end) in the entry arrays
+    DevBuf sc_q, sc_qclr;           // FP16 lists: uint2 (x | y << 16, z) per entry, colour per entry
+    float sc_qmin[3] = {0, 0, 0}, sc_qrange[3] = {0, 0, 0};  // mPosMin / mPosRange they were stored against
+    bool sc_fp16 = false;           // the lists are InsertPointsSubcell_FP16's
+    bool colavg_seen = false;       // an avgColor ScatterDensity ran (the reference's AUX_COLAVG exists)
     int sc_size = 0;
     uint32_t sc_len = 0, sc_nsub = 0;
     bool sc_has_clr = false;
@@ -160,7 +164,7 @@ gvx_status gvx_check_device_error(gvx_grid* g, const char* stage);
 // splats (gvx_splat.cu) and gathers (gvx_gather.cu)
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
                          int chan_v, int accum);
-gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand);
+gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand, int avg_color);
 gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, int sc_len, int chan, int chan_clr,
                           int accum);
 

@@ -511,7 +511,12 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
 
-// ScatterDensity, race-free: own points only, into the own padded tile
+// ScatterDensity, race-free: own points only, into the own padded tile.  With
+// point colours (PT.cuh:555-571, 610-642) each point also colours the interior
+// voxel it lies in: clr_mode 1 (avgColor) = integer mean of the voxel's
+// points' r, g, b with alpha 255, into channel 1; clr_mode 2 = the colour of
+// the voxel's highest-index point (the reference's writers race), channel 3.
+// Both are counted with shared-memory integer atomics: deterministic.
 struct ScatterArgs {
     int brick, P, apron;
     uint32_t nslots;
@@ -523,6 +528,11 @@ struct ScatterArgs {
     int expand;
     float* den;
     uint32_t* err;
+    int clr_mode;             // 0 none, 1 average, 2 one point's colour
+    const uint32_t* perm;     // sorted position -> point index
+    const char* clr;
+    int clr_off, clr_stride;
+    uint32_t* clr_out;        // 4-byte channel, brick-major padded
 };
 
 __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
@@ -530,8 +540,10 @@ __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
     extern __shared__ __align__(128) unsigned char smem[];
     float* tden = (float*)smem;
     __shared__ __align__(8) uint64_t s_bar;
-    const int P = a.P, P3 = P * P * P, b = a.brick, ap = a.apron, tid = threadIdx.x;
+    const int P = a.P, P3 = P * P * P, b = a.brick, ap = a.apron, tid = threadIdx.x, b3 = b * b * b;
     const uint32_t bytes = (uint32_t)P3 * 4u;
+    // colour tables after the tile: average = count, r, g, b per interior voxel; one point = its index
+    uint32_t* tclr = (uint32_t*)(smem + (((size_t)P3 * 4 + 15) & ~(size_t)15));
     if (tid == 0) {
         mbar_init(&s_bar, 1);
         mbar_fence_init();
@@ -548,8 +560,14 @@ __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
             mbar_expect_tx(&s_bar, bytes);
             bulk_g2s(tden, a.den + (size_t)s * P3, bytes, &s_bar);
         }
+        if (a.clr_mode) {
+            const int words = a.clr_mode == 1 ? 4 * b3 : b3;
+            const uint32_t init = a.clr_mode == 1 ? 0u : 0xFFFFFFFFu;
+            for (int i = tid; i < words; i += kSplatThreads) tclr[i] = init;
+        }
         if (!mbar_wait_bounded(&s_bar, phase)) atomicOr(a.err, GVX_DERR_TIMEOUT);
         phase ^= 1u;
+        if (a.clr_mode) __syncthreads();
         const float vx = (float)nd.pos[0], vy = (float)nd.pos[1], vz = (float)nd.pos[2];
         const int cnt = a.expand ? 7 : 1;
         for (int e = rg.x + tid; e < rg.y; e += kSplatThreads) {
@@ -557,6 +575,19 @@ __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
             const float px = w.x - vx, py = w.y - vy, pz = w.z - vz;
             const float pix = (float)(int)px, piy = (float)(int)py, piz = (float)(int)pz;
             if (pix < 0 || piy < 0 || piz < 0 || pix >= b || piy >= b || piz >= b) continue;
+            if (a.clr_mode) {
+                const int v = ((int)piz * b + (int)piy) * b + (int)pix;
+                const uint32_t pt = a.perm[e];
+                if (a.clr_mode == 1) {
+                    const uint32_t c = *(const uint32_t*)(a.clr + (size_t)pt * (size_t)a.clr_stride + a.clr_off);
+                    atomicAdd(&tclr[v], 1u);
+                    atomicAdd(&tclr[b3 + v], c & 255u);
+                    atomicAdd(&tclr[2 * b3 + v], (c >> 8) & 255u);
+                    atomicAdd(&tclr[3 * b3 + v], (c >> 16) & 255u);
+                } else {
+                    atomicMax((int*)&tclr[v], (int)pt);  // the highest point index; -1 = none
+                }
+            }
             for (int k = 0; k < cnt; k++) {
                 const int ox = (k == 1) ? -1 : (k == 2) ? 1 : 0;
                 const int oy = (k == 3) ? -1 : (k == 4) ? 1 : 0;
@@ -574,8 +605,24 @@ __global__ void __launch_bounds__(kSplatThreads) k_scatter_ref(ScatterArgs a)
         if (tid == 0) {
             bulk_s2g(a.den + (size_t)s * P3, tden, bytes);
             bulk_commit();
-            bulk_wait_read_all();
         }
+        if (a.clr_mode) {
+            uint32_t* out = a.clr_out + (size_t)s * P3;
+            for (int v = tid; v < b3; v += kSplatThreads) {
+                const int o = (((v / (b * b)) + ap) * P + ((v / b) % b + ap)) * P + (v % b + ap);
+                if (a.clr_mode == 1) {
+                    const uint32_t n = tclr[v];
+                    if (n == 0u) continue;
+                    out[o] = (tclr[b3 + v] / n & 255u) | ((tclr[2 * b3 + v] / n & 255u) << 8) |
+                             ((tclr[3 * b3 + v] / n & 255u) << 16) | (255u << 24);
+                } else {
+                    const int pt = (int)tclr[v];
+                    if (pt < 0) continue;
+                    out[o] = *(const uint32_t*)(a.clr + (size_t)pt * (size_t)a.clr_stride + a.clr_off);
+                }
+            }
+        }
+        if (tid == 0) bulk_wait_read_all();
         __syncthreads();
     }
     if (tid == 0) bulk_wait_all();
@@ -1155,7 +1202,7 @@ gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* out)
 
 }  // extern "C"
 
-gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand)
+gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3], int expand, int avg_color)
 {
     gvx_status rc = check_splat_state(g, "ScatterDensity");
     if (rc) return rc;
@@ -1167,10 +1214,24 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
         gvx_set_error("ScatterDensity: radius must be nonzero");
         return GVX_ERR_INVALID_ARG;
     }
+    // the colour half (VG.cpp:5638-5655): with point colours, avgColor averages into channel 1; without,
+    // each voxel takes a point's colour in channel 3, unless an avgColor call ever ran on this grid
+    // (the reference's colour buffer then exists and silently takes the sums)
+    int clr_mode = 0;
+    if (g->pts.clr) {
+        if (avg_color) clr_mode = 1;
+        else if (!g->colavg_seen) clr_mode = 2;
+    }
+    const int clr_chan = clr_mode == 1 ? 1 : 3;
+    if (clr_mode && (!g->ch[clr_chan].used || g->ch[clr_chan].elem_bytes != 4)) {
+        gvx_set_error("ScatterDensity: point colours go to channel %d, which must be a 4-byte channel", clr_chan);
+        return GVX_ERR_INVALID_ARG;
+    }
     rc = gvx_prepare_points(g, n, trans, false);
     if (rc) return rc;
-    const int P = g->P, P3 = P * P * P;
-    const size_t smem = (size_t)P3 * 4;
+    if (clr_mode == 1) g->colavg_seen = true;
+    const int P = g->P, P3 = P * P * P, b3 = g->brick * g->brick * g->brick;
+    const size_t smem = (((size_t)P3 * 4 + 15) & ~(size_t)15) + (clr_mode == 1 ? 16 : clr_mode == 2 ? 4 : 0) * (size_t)b3;
     ScatterArgs a;
     a.brick = g->brick;
     a.P = P;
@@ -1184,7 +1245,14 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
     a.expand = expand;
     a.den = g->ch[0].data.as<float>();
     a.err = g->d_err.as<uint32_t>();
+    a.clr_mode = clr_mode;
+    a.perm = g->vals[g->sorted_buf].as<uint32_t>();
+    a.clr = g->pts.clr;
+    a.clr_off = g->pts.clr_off;
+    a.clr_stride = g->pts.clr_stride;
+    a.clr_out = clr_mode ? g->ch[clr_chan].data.as<uint32_t>() : nullptr;
     g->ch[0].apron_valid = false;
+    if (clr_mode) g->ch[clr_chan].apron_valid = false;
     if (a.nslots == 0) return GVX_OK;
     GVX_CK(cudaFuncSetAttribute(k_scatter_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

@@ -74,7 +74,7 @@ def load(path=None):
         "gvx_rebuild_topology": ([vp, i, f, fp, i, i], i), "gvx_request_full_rebuild": ([vp, i], i),
         "gvx_finish_topology": ([vp], i), "gvx_update_atlas": ([vp], i),
         "gvx_insert_points": ([vp, i, fp, vp], i),
-        "gvx_scatter_density": ([vp, i, f, f, fp, i], i),
+        "gvx_scatter_density": ([vp, i, f, f, fp, i, i], i),
         "gvx_insert_points_subcell": ([vp, i, i, f, fp, ip], i),
         "gvx_gather_density": ([vp, i, i, f, fp, i, i, i, i], i),
         "gvx_gather_levelset": ([vp, i, i, f, fp, i, i, i, i], i),
@@ -82,6 +82,9 @@ def load(path=None):
         "gvx_splat_backward": ([vp, i, i, f, fp, vp, vp, vp, vp], i),
         "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
         "gvx_compute": ([vp, i, i, i, fp, i, i, f], i),
+        "gvx_insert_points_subcell_fp16": ([vp, i, i, f, fp, ctypes.POINTER(i)], i),
+        "gvx_gather_levelset_fp16": ([vp, i, i, f, fp, i, i, i], i),
+        "gvx_convert_and_transform": ([vp, vp, i, vp, i, i, fp, fp, fp, fp], i),
         "gvx_memcpy": ([i, vp, vp, ctypes.c_size_t, i], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
         "gvx_read_nodes": ([vp, i, vp, i64], i), "gvx_read_childlist": ([vp, i, vp, i64], i),
@@ -220,8 +223,9 @@ class Grid:
         self._check(self.lib.gvx_insert_points(self.h, n, _f3(trans), _ptr(out)))
         return out
 
-    def scatter_density(self, n, radius, amp=1.0, trans=None, expand=True):
-        self._check(self.lib.gvx_scatter_density(self.h, n, float(radius), float(amp), _f3(trans), int(expand)))
+    def scatter_density(self, n, radius, amp=1.0, trans=None, expand=True, avg_color=False):
+        self._check(self.lib.gvx_scatter_density(self.h, n, float(radius), float(amp), _f3(trans), int(expand),
+                                                 int(avg_color)))
 
     def splat(self, mode, n, radius, trans=None, chan_density=0, chan_vel=-1, accum=False):
         self._check(self.lib.gvx_splat(self.h, mode, n, float(radius), _f3(trans), chan_density, chan_vel,
@@ -246,6 +250,21 @@ class Grid:
     def gather_levelset(self, subcell, n, radius, sc_len, trans=None, chan=0, chan_clr=-1, accum=False):
         self._check(self.lib.gvx_gather_levelset(self.h, subcell, n, float(radius), _f3(trans), sc_len, chan,
                                                  chan_clr, int(accum)))
+
+    def insert_points_subcell_fp16(self, subcell, n, radius, trans=None):
+        out = ctypes.c_int(0)
+        self._check(self.lib.gvx_insert_points_subcell_fp16(self.h, subcell, n, float(radius), _f3(trans),
+                                                            ctypes.byref(out)))
+        return out.value
+
+    def gather_levelset_fp16(self, subcell, n, radius, sc_len, trans=None, chan=0, chan_clr=-1):
+        self._check(self.lib.gvx_gather_levelset_fp16(self.h, subcell, n, float(radius), _f3(trans), sc_len, chan,
+                                                      chan_clr))
+
+    def convert_and_transform(self, src, src_bits, dst, n, wmin, wdelta, trans=(0, 0, 0), scal=(1, 1, 1)):
+        """ConvertAndTransform: device uint16x3 (src_bits 2) or float3 (4) points -> device float3"""
+        self._check(self.lib.gvx_convert_and_transform(self.h, _ptr(src), src_bits, _ptr(dst), 4, n, _f3(wmin),
+                                                       _f3(wdelta), _f3(trans), _f3(scal)))
 
     def update_apron(self, chan=None, boundval=0.0):
         if chan is None:

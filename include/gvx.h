@@ -106,7 +106,8 @@ gvx_status gvx_fill_channel(gvx_grid* g, int chan, const float value[4]);
 
 /* SetPoints (VG.h:541, VG.cpp:4900-4908) + SetDataGPU (VG.cpp:4872-4880):
  * borrowed device pointers, byte offset and byte stride per point.
- * vel and clr may be NULL. */
+ * vel and clr may be NULL; clr holds 4 bytes (uchar4) per point.  All
+ * pointers, offsets and strides 4-byte aligned. */
 gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, int pos_stride,
                           const void* vel, int vel_offset, int vel_stride,
                           const void* clr, int clr_offset, int clr_stride);
@@ -135,12 +136,18 @@ gvx_status gvx_update_atlas(gvx_grid* g);
  * grouped by brick for the splats.  If pnode_out is not NULL it receives the
  * leaf pool index of every point (0xFFFFFFFF if none), host memory. */
 gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* pnode_out);
-/* ScatterDensity (VG.h:555, VG.cpp:5624-5660, kernel PT.cuh:525-573):
+/* ScatterDensity (VG.h:555, VG.cpp:5624-5660, kernels PT.cuh:525-573, 610-642):
  * (1 - d^2/r^2)^3 at the point's voxel and, with expand, its 6 face
  * neighbours, summed into channel 0 of the point's own brick (apron included),
- * without the reference's racy read-modify-write. */
+ * without the reference's racy read-modify-write.  With point colours bound
+ * (gvx_set_points clr), each point also colours the interior voxel it lies in:
+ * avg_color != 0 -> channel 1 = (integer mean of r, g, b, 255) over the
+ * voxel's points; avg_color == 0 -> channel 3 = one point's colour (the
+ * highest index; the reference's writers race) -- unless an avg_color call
+ * ever ran on this grid, after which, as in the reference, no colour is
+ * written.  The colour channel must be a 4-byte channel. */
 gvx_status gvx_scatter_density(gvx_grid* g, int n, float radius, float amp, const float trans[3],
-                               int expand);
+                               int expand, int avg_color);
 /* InsertPointsSubcell (VG.h:551, VG.cpp:4971-5092): every point joins each
  * subcell (size `subcell`, dividing the brick size) of an active brick that
  * its box [(int(p-r)/s)s, (int(p+1+r)/s)s] touches.  sc_len receives the
@@ -160,6 +167,32 @@ gvx_status gvx_gather_density(gvx_grid* g, int subcell, int n, float radius, con
                               int sc_len, int chan_density, int chan_clr, int accum);
 gvx_status gvx_gather_levelset(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
                                int sc_len, int chan_levelset, int chan_clr, int accum);
+/* InsertPointsSubcell_FP16 (VG.h:552, VG.cpp:5094-5190): the subcell lists of
+ * gvx_insert_points_subcell, each entry's position kept as 16-bit fractions
+ * (w - mPosMin) / mPosRange * 65535 of the last topology build's bounding box
+ * (gvx_info bbox_min / bbox_max), half the bytes per entry.  The point
+ * velocities the reference also quantises are read by no kernel and are not
+ * stored. */
+gvx_status gvx_insert_points_subcell_fp16(gvx_grid* g, int subcell, int n, float radius,
+                                          const float trans[3], int* sc_len);
+/* GatherLevelSet_FP16 (VG.h:558, VG.cpp:5375-5401, kernel PT.cuh:775-813):
+ * every interior voxel v of every active brick = min(3, min over the listed
+ * points of |p - v| - R), p read back as q / 65535 * range + min; no
+ * accumulation.  When the lists hold colours and chan_clr >= 0, chan_clr (any
+ * 4-byte channel, possibly chan_levelset) then receives the inverse-distance
+ * colour sum of the reference: sum of colour / |p - v|, each component * 255
+ * truncated and added at byte offsets (carries included).  n, trans and
+ * sc_len are accepted as the reference's arguments; the lists hold the rest. */
+gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
+                                    int sc_len, int chan_levelset, int chan_clr);
+/* ConvertAndTransform (VG.h:559, VG.cpp:5668-5682, kernel PT.cuh:120-142):
+ * device points src (three uint16 per point when src_bits is 2, three floats
+ * when 4, densely packed) -> device float3 dst = (wmin + p * wdelta) * scal +
+ * trans, each multiply-add one FMA.  dst is always float3, whatever dst_bits
+ * says (as the reference writes it). */
+gvx_status gvx_convert_and_transform(gvx_grid* g, const void* src, int src_bits, void* dst, int dst_bits, int n,
+                                     const float wmin[3], const float wdelta[3], const float trans[3],
+                                     const float scal[3]);
 /* TRILINEAR / CUBIC splat of weight (and velocity*weight into a FLOAT3/FLOAT4
  * channel) of the points that lie in active bricks; chan_vel may be -1.
  * Every voxel of each active brick, apron included, receives the sum of the

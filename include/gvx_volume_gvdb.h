@@ -170,6 +170,12 @@ public:
                        int chanDensity, int chanClr, bool bAccum = false);
     void GatherLevelSet(int subcell_size, int num_pnts, float radius, Vector3DF trans, int& pSCPntsLength,
                         int chanLevelset, int chanClr, bool bAccum = false);
+    void InsertPointsSubcell_FP16(int subcell_size, int num_pnts, float radius, Vector3DF trans,
+                                  int& pSCPntsLength);
+    void GatherLevelSet_FP16(int subcell_size, int num_pnts, float radius, Vector3DF trans, int& pSCPntsLength,
+                             int chanLevelSet, int chanClr);
+    void ConvertAndTransform(DataPtr& psrc, char psrcbits, DataPtr& pdest, char pdestbits, int num_pnts,
+                             Vector3DF wMin, Vector3DF wDelta, Vector3DF trans, Vector3DF scal);
     DataPtr& getAux(int id);
 
     // ---- compute (VG.h:355): FUNC_FILL_F/C/C4 and FUNC_SMOOTH

@@ -46,6 +46,8 @@ struct orc_grid {
     int rebuild_topo; /* mRebuildTopo */
     int curr_depth;   /* mCurrDepth */
     int last_mode;
+    float pos_min[3], pos_max[3]; /* mPosMin / mPosMax of the last GetBoundingBox */
+    int colavg_seen;              /* AUX_COLAVG exists: an avgColor ScatterDensity ran */
     int degenerate;
     /* atlas (shared subdim, as UpdateAtlas resizes every channel together) */
     int sub[3];
@@ -396,6 +398,8 @@ static int bbox_depth(orc_grid* g, int n, const float* pos, int stride, const fl
         float lo = mn[a] - 1.0f, hi = mx[a] + 2.0f;
         lo = 0 > lo ? 0 : lo;
         hi = 0 > hi ? 0 : hi;
+        g->pos_min[a] = lo;
+        g->pos_max[a] = hi;
         pmin[a] = (int)lo;
         pmax[a] = (int)hi;
     }
@@ -1011,15 +1015,129 @@ static int splat_ref_scatter(orc_grid* g, int n, const float* pos, int ps, float
     return ORC_OK;
 }
 
+/* the colour half of gvdbScatterPointDensity (PT.cuh:555-571) and
+ * gvdbScatterPointAvgCol (PT.cuh:610-642), from VolumeGVDB::ScatterDensity
+ * (VG.cpp:5624-5660).  A point colours the interior voxel it lies in:
+ *  - avg_color: the voxel of channel 1 = (sum r / count, sum g / count,
+ *    sum b / count, 255), integer sums and division, over the voxel's points;
+ *  - otherwise, unless an avg_color scatter ever ran on this grid (its colour
+ *    buffer then exists and takes the sums, which nothing reads): channel 3
+ *    gets one point's colour as given; the reference's writers race, the
+ *    restatement takes the point of highest index. */
+typedef struct { int64_t vox; int pt; } vox_pt;
+static int cmp_vox_pt(const void* a, const void* b)
+{
+    const vox_pt *x = (const vox_pt*)a, *y = (const vox_pt*)b;
+    if (x->vox != y->vox) return x->vox < y->vox ? -1 : 1;
+    return x->pt < y->pt ? -1 : (x->pt > y->pt);
+}
+
+static int scatter_colour(orc_grid* g, int n, const float* pos, int ps, const uint8_t* clr, const float* tr,
+                          int avg_color)
+{
+    const int chan = avg_color ? 1 : 3;
+    if (avg_color) g->colavg_seen = 1;
+    else if (g->colavg_seen) return ORC_OK;
+    if (!g->ch[chan] || g->ncomp[chan] != 4) return ORC_ERR_ARG;
+    int res0 = g->res[0];
+    vox_pt* list = (vox_pt*)malloc((size_t)(n + 1) * sizeof(vox_pt));
+    int64_t m = 0;
+    for (int i = 0; i < n; i++) {
+        const float* raw = pos + (int64_t)i * ps;
+        if (raw[2] == NOHIT) continue;
+        float w[3] = {raw[0] + tr[0], raw[1] + tr[1], raw[2] + tr[2]};
+        int64_t nid = get_node_at_point(g, w);
+        if (nid < 0) continue;
+        orc_node* nd = &g->pools[0].nodes[nid];
+        int pi[3];
+        for (int a = 0; a < 3; a++) pi[a] = (int)(w[a] - (float)nd->pos[a]);
+        if (pi[0] < 0 || pi[1] < 0 || pi[2] < 0 || pi[0] >= res0 || pi[1] >= res0 || pi[2] >= res0) continue;
+        if (nd->value[0] < 0) continue;
+        list[m].vox = vox_ptr(g, chan, nd->value, pi[0], pi[1], pi[2]) - g->ch[chan];
+        list[m].pt = i;
+        m++;
+    }
+    qsort(list, (size_t)m, sizeof(vox_pt), cmp_vox_pt);
+    for (int64_t k = 0; k < m;) {
+        int64_t e = k;
+        uint32_t cnt = 0, sum[3] = {0, 0, 0};
+        while (e < m && list[e].vox == list[k].vox) {
+            for (int c = 0; c < 3; c++) sum[c] += clr[(int64_t)list[e].pt * 4 + c];
+            cnt++;
+            e++;
+        }
+        double* out = g->ch[chan] + list[k].vox;
+        if (avg_color) {
+            for (int c = 0; c < 3; c++) out[c] = (double)(uint8_t)(sum[c] / cnt);
+            out[3] = 255.0;
+        } else {
+            const uint8_t* src = clr + (int64_t)list[e - 1].pt * 4;
+            for (int c = 0; c < 4; c++) out[c] = (double)src[c];
+        }
+        k = e;
+    }
+    free(list);
+    return ORC_OK;
+}
+
+int orc_scatter_density(orc_grid* g, int n, const float* pos, int pos_stride, const uint8_t* clr, float radius,
+                        const float trans[3], int expand, int avg_color)
+{
+    if (!g || n < 0 || (n > 0 && !pos) || pos_stride < 3) return ORC_ERR_ARG;
+    if (g->root_level < 0) return ORC_ERR_STATE;
+    float tr[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    g->degenerate = 0;
+    int rc = splat_ref_scatter(g, n, pos, pos_stride, radius, tr, expand);
+    if (rc || !clr) return rc;
+    return scatter_colour(g, n, pos, pos_stride, clr, tr, avg_color);
+}
+
+/* float -> uint16 / uint32 as the GPU converts (truncation, saturating, NaN -> 0) */
+static uint32_t f2u16_sat(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 65535.0f) return 65535u;
+    return (uint32_t)v;
+}
+static uint32_t f2u32_sat(float v)
+{
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)v;
+}
+
+/* the FP16 variant's point storage (gvdbInsertSubcell_fp16, PT.cuh:204-207):
+ * (w - mPosMin) / mPosRange * 65535 per axis, truncated to 16 bits, and its
+ * read-back in gvdbGatherLevelSet_fp16 (PT.cuh:797-799): q / 65535 * range + min,
+ * every step a rounded float operation */
+static void quantize_pos(const orc_grid* g, const float w[3], uint32_t q[3])
+{
+    for (int a = 0; a < 3; a++) {
+        float range = g->pos_max[a] - g->pos_min[a];
+        float t = (w[a] - g->pos_min[a]) / range;
+        q[a] = f2u16_sat(t * 65535.0f);
+    }
+}
+static void dequantize_pos(const orc_grid* g, const uint32_t q[3], float p[3])
+{
+    for (int a = 0; a < 3; a++) {
+        float range = g->pos_max[a] - g->pos_min[a];
+        float t = (float)q[a] / 65535.0f;
+        t = t * range;
+        p[a] = t + g->pos_min[a];
+    }
+}
+
 /* InsertPointsSubcell (VG.cpp:4971-5092; PT.cuh:109-118, 218-315, 677-694) and
  * GatherDensity / GatherLevelSet (VG.cpp:5318-5373; PT.cuh:696-773) */
 static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int ps, const uint8_t* clr,
                         float radius, float rins, const float* tr, int sc, int chan, int chan_clr, int accum,
-                        int64_t* sc_len)
+                        int64_t* sc_len, int fp16)
 {
     pool* p0 = &g->pools[0];
     if (!g->ch[chan]) return ORC_ERR_STATE;
-    if (chan_clr >= 0 && (chan_clr >= MAXCH || !g->ch[chan_clr] || g->ncomp[chan_clr] != 4)) return ORC_ERR_ARG;
+    if (!fp16 && chan_clr >= 0 && (chan_clr >= MAXCH || !g->ch[chan_clr] || g->ncomp[chan_clr] != 4)) return ORC_ERR_ARG;
+    if (fp16 && chan_clr >= 0 && (chan_clr >= MAXCH || !g->ch[chan_clr])) return ORC_ERR_ARG;
     if (!clr) chan_clr = -1; /* no point colours: the colour channel is not written */
     int b = g->brick;
     if (sc <= 0 || b % sc) return ORC_ERR_ARG;
@@ -1093,6 +1211,48 @@ static int splat_gather(orc_grid* g, int levelset, int n, const float* pos, int 
                         double vpos[3] = {(double)(nd->pos[0] + lx), (double)(nd->pos[1] + ly),
                                           (double)(nd->pos[2] + lz)};
                         double* out = vox_ptr(g, chan, nd->value, lx, ly, lz);
+                        if (fp16) {
+                            /* gvdbGatherLevelSet_fp16 (PT.cuh:775-813) in its own float arithmetic:
+                             * dist from 3, min(|p - v| - R); the colour sum of INT2CLR(c) / |p - v|
+                             * from 0 (the reference leaves it uninitialised), written as CLR2INT of
+                             * particles.cuh (components * 255 added with carries) */
+                            float vf[3] = {(float)(nd->pos[0] + lx), (float)(nd->pos[1] + ly),
+                                           (float)(nd->pos[2] + lz)};
+                            float dist = 3.0f, c4[4] = {0.f, 0.f, 0.f, 0.f};
+                            for (int64_t j = off[idx]; j < off[idx + 1]; j++) {
+                                const float* raw = pos + (int64_t)list[j] * ps;
+                                float w[3] = {raw[0] + tr[0], raw[1] + tr[1], raw[2] + tr[2]}, pq[3];
+                                uint32_t q[3];
+                                quantize_pos(g, w, q);
+                                dequantize_pos(g, q, pq);
+                                float dx = pq[0] - vf[0], dy = pq[1] - vf[1], dz = pq[2] - vf[2];
+                                float s2 = dx * dx;
+                                s2 = s2 + dy * dy;
+                                s2 = s2 + dz * dz;
+                                float c = sqrtf(s2);
+                                float t = c - radius;
+                                dist = t < dist ? t : dist;
+                                if (chan_clr >= 0)
+                                    for (int k = 0; k < 4; k++) {
+                                        float comp = (float)clr[(int64_t)list[j] * 4 + k] / 255.0f;
+                                        c4[k] = c4[k] + comp / c;
+                                    }
+                            }
+                            *out = (double)dist;
+                            if (chan_clr >= 0) {
+                                uint32_t u = 0;
+                                for (int k = 0; k < 4; k++) u += f2u32_sat(c4[k] * 255.0f) << (8 * k);
+                                double* co = vox_ptr(g, chan_clr, nd->value, lx, ly, lz);
+                                if (g->ncomp[chan_clr] == 4)
+                                    for (int k = 0; k < 4; k++) co[k] = (double)((u >> (8 * k)) & 255u);
+                                else {
+                                    float bits;
+                                    memcpy(&bits, &u, 4);
+                                    co[0] = (double)bits;
+                                }
+                            }
+                            continue;
+                        }
                         double val = accum ? *out : (levelset ? 3.0 : 0.0);
                         for (int64_t j = off[idx]; j < off[idx + 1]; j++) {
                             const float* raw = pos + (int64_t)list[j] * ps;
@@ -1145,7 +1305,7 @@ int orc_splat(orc_grid* g, int mode, int n, const float* pos, int pos_stride, co
     case ORC_SPLAT_GATHER_DENSITY:
     case ORC_SPLAT_GATHER_LEVELSET:
         return splat_gather(g, mode == ORC_SPLAT_GATHER_LEVELSET, n, pos, pos_stride, NULL, radius, radius_ins, tr,
-                            subcell, chan_density, -1, accum, NULL);
+                            subcell, chan_density, -1, accum, NULL, 0);
     }
     return ORC_ERR_ARG;
 }
@@ -1160,7 +1320,47 @@ int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_strid
     float tr[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
     g->degenerate = 0;
     return splat_gather(g, levelset, n, pos, pos_stride, clr, radius, radius_ins, tr, subcell, chan, chan_clr,
-                        accum, sc_len);
+                        accum, sc_len, 0);
+}
+
+/* ConvertAndTransform (VG.cpp:5668-5682, gvdbConvAndTransform PT.cuh:120-142):
+ * (wmin + p * wdelta) * scal + trans per axis, each multiply-add one fused
+ * (single-rounding) operation, p from three uint16 (src_bits 2) or floats (4) */
+int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, const float wmin[3],
+                              const float wdelta[3], const float trans[3], const float scal[3])
+{
+    if (n < 0 || (src_bits != 2 && src_bits != 4)) return ORC_ERR_ARG;
+    for (int i = 0; i < n; i++) {
+        for (int a = 0; a < 3; a++) {
+            float p = src_bits == 2 ? (float)((const uint16_t*)src)[(int64_t)i * 3 + a]
+                                    : ((const float*)src)[(int64_t)i * 3 + a];
+            dst[(int64_t)i * 3 + a] = fmaf(fmaf(p, wdelta[a], wmin[a]), scal[a], trans[a]);
+        }
+    }
+    return ORC_OK;
+}
+
+void orc_pos_bounds(orc_grid* g, float out[6])
+{
+    for (int a = 0; a < 3; a++) {
+        out[a] = g->pos_min[a];
+        out[3 + a] = g->pos_max[a];
+    }
+}
+
+/* InsertPointsSubcell_FP16 (VG.cpp:5094-5190) + GatherLevelSet_FP16
+ * (VG.cpp:5375-5401): the same subcell lists, positions stored as 16-bit
+ * fractions of the last GetBoundingBox's box; chan_clr may be any 4-byte channel */
+int orc_gather_fp16(orc_grid* g, int n, const float* pos, int pos_stride, const uint8_t* clr, float radius,
+                    float radius_ins, const float trans[3], int subcell, int chan, int chan_clr, int64_t* sc_len)
+{
+    if (!g || n < 0 || (n > 0 && !pos) || pos_stride < 3) return ORC_ERR_ARG;
+    if (g->root_level < 0) return ORC_ERR_STATE;
+    if (chan < 0 || chan >= MAXCH || !g->ch[chan] || g->ncomp[chan] != 1) return ORC_ERR_ARG;
+    float tr[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    g->degenerate = 0;
+    return splat_gather(g, 1, n, pos, pos_stride, clr, radius, radius_ins, tr, subcell, chan, chan_clr, 0, sc_len,
+                        1);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1205,15 +1405,7 @@ int orc_update_apron(orc_grid* g, int chan, double boundval)
 }
 
 /* ------------------------------------------------------------------ */
-/* Compute (VG.cpp:4534-4558) with the operators gvdbOpFillF / FillC / FillC4
- * (OP.cuh:352-380) and gvdbOpSmooth (OP.cuh:383-400), over every brick of the
- * atlas.  skip_over_aprons selects GVDB_VOXPACKED (OP.cuh:189-215: brick
- * interiors, the stencil reading the brick's own apron) or GVDB_VOXUNPACKED
- * (OP.cuh:220-223: atlas voxels whose every coordinate is >= 1, the stencil
- * reading atlas neighbours).  In the unpacked form the reference's smoothing
- * reads voxels other blocks are writing (a race); the oracle reads every value
- * before the pass (Jacobi), which is the result of any ordering in which the
- * reads come first. */
+/* atlas voxel (X, Y, Z) of a channel, brick-major storage */
 static double* atlas_voxel(orc_grid* g, int chan, int X, int Y, int Z)
 {
     int P = g->P;

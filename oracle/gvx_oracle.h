@@ -110,6 +110,19 @@ int orc_splat(orc_grid* g, int mode, int n, const float* pos, int pos_stride,
 int orc_gather(orc_grid* g, int levelset, int n, const float* pos, int pos_stride, const uint8_t* clr,
                float radius, float radius_ins, const float trans[3], int subcell, int chan, int chan_clr,
                int accum, int64_t* sc_len);
+/* ScatterDensity (VG.cpp:5624-5660) with the point colours of clr (4 bytes per
+ * point, may be NULL): density into channel 0, colours into channel 1
+ * (avg_color) or 3 */
+int orc_scatter_density(orc_grid* g, int n, const float* pos, int pos_stride, const uint8_t* clr, float radius,
+                        const float trans[3], int expand, int avg_color);
+/* InsertPointsSubcell_FP16 + GatherLevelSet_FP16 (VG.cpp:5094-5190, 5375-5401) */
+int orc_gather_fp16(orc_grid* g, int n, const float* pos, int pos_stride, const uint8_t* clr, float radius,
+                    float radius_ins, const float trans[3], int subcell, int chan, int chan_clr, int64_t* sc_len);
+/* ConvertAndTransform (VG.cpp:5668-5682) on host arrays */
+int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, const float wmin[3],
+                              const float wdelta[3], const float trans[3], const float scal[3]);
+/* mPosMin / mPosMax of the last GetBoundingBox */
+void orc_pos_bounds(orc_grid* g, float out[6]);
 
 int orc_update_apron(orc_grid* g, int chan, double boundval);
 

@@ -26,9 +26,10 @@ NODE_DTYPE = np.dtype([("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "
 
 
 def build():
-    """gcc the restatement into oracle/liboracle.so"""
-    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-D_POSIX_C_SOURCE=200809L", "-o", LIB_PATH + ".tmp",
-           SRC, "-lm"]
+    """gcc the restatement into oracle/liboracle.so (no FMA contraction: the float
+    steps it restates round one by one, on x86 and Arm alike)"""
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-D_POSIX_C_SOURCE=200809L", "-ffp-contract=off", "-o",
+           LIB_PATH + ".tmp", SRC, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n%s" % r.stderr)
@@ -57,6 +58,9 @@ def load():
         "orc_atlas_subdim": ([vp, vp], i), "orc_get_atlas_map": ([vp, vp, i], i),
         "orc_splat": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, i, i, i, i, i, f], i),
         "orc_gather": ([vp, i, i, vp, i, vp, f, f, vp, i, i, i, i, vp], i),
+        "orc_gather_fp16": ([vp, i, vp, i, vp, f, f, vp, i, i, i, vp], i), "orc_pos_bounds": ([vp, vp], None),
+        "orc_scatter_density": ([vp, i, vp, i, vp, f, vp, i, i], i),
+        "orc_convert_and_transform": ([i, vp, i, vp, vp, vp, vp, vp], i),
         "orc_compute": ([vp, i, i, i, vp, i, i, d], i),
         "orc_update_apron": ([vp, i, d], i), "orc_channel_size": ([vp, i], i64),
         "orc_read_channel": ([vp, i, vp, i64], i), "orc_write_channel": ([vp, i, vp, i64], i),
@@ -191,6 +195,35 @@ class Oracle:
         self._ck(st, "gather", allow_degenerate)
         return n.value
 
+    def scatter_density(self, pos, radius, clr=None, trans=(0, 0, 0), expand=True, avg_color=False,
+                        allow_degenerate=False):
+        """ScatterDensity (VG.cpp:5624-5660): REF_SCATTER into channel 0 and, with point
+        colours, channel 1 (avg_color) or channel 3"""
+        pos = np.ascontiguousarray(pos, np.float32)
+        c = None if clr is None else np.ascontiguousarray(clr, np.uint8).reshape(-1, 4)
+        t = np.ascontiguousarray(trans, np.float32)
+        st = self.lib.orc_scatter_density(self.h, pos.shape[0], _p(pos), 3, _p(c), float(radius), _p(t),
+                                          int(expand), int(avg_color))
+        return self._ck(st, "scatter_density", allow_degenerate)
+
+    def gather_fp16(self, pos, radius, radius_ins, subcell=4, chan=0, chan_clr=-1, clr=None, trans=(0, 0, 0),
+                    allow_degenerate=False):
+        """InsertPointsSubcell_FP16 + GatherLevelSet_FP16; returns the entry count"""
+        pos = np.ascontiguousarray(pos, np.float32)
+        c = None if clr is None else np.ascontiguousarray(clr, np.uint8).reshape(-1, 4)
+        t = np.ascontiguousarray(trans, np.float32)
+        n = ctypes.c_int64(0)
+        st = self.lib.orc_gather_fp16(self.h, pos.shape[0], _p(pos), 3, _p(c), float(radius), float(radius_ins),
+                                      _p(t), subcell, chan, chan_clr, ctypes.byref(n))
+        self._ck(st, "gather_fp16", allow_degenerate)
+        return n.value
+
+    def pos_bounds(self):
+        """(mPosMin, mPosMax) of the last GetBoundingBox"""
+        out = np.zeros(6, np.float32)
+        self.lib.orc_pos_bounds(self.h, _p(out))
+        return out[:3], out[3:]
+
     def compute(self, effect, chan, iterations, params, update_apron, skip_over_aprons, boundval=0.0):
         """Compute (VG.cpp:4534-4558): FUNC_FILL_F/C/C4 (110-112), FUNC_SMOOTH (113)"""
         p = np.ascontiguousarray(params, np.float32)
@@ -211,6 +244,18 @@ class Oracle:
         P = (1 << self.logdim[0]) + 2 * self.apron
         nc = self.ncomp[chan]
         return out.reshape((-1, P, P, P) + ((nc,) if nc > 1 else ()))
+
+
+def convert_and_transform(src, src_bits, wmin, wdelta, trans=(0, 0, 0), scal=(1, 1, 1)):
+    """ConvertAndTransform on host arrays: (n, 3) uint16 (src_bits 2) or float32 (4) -> (n, 3) float32"""
+    lib = load()
+    a = np.ascontiguousarray(src, np.uint16 if src_bits == 2 else np.float32)
+    out = np.zeros((a.shape[0], 3), np.float32)
+    vecs = [np.ascontiguousarray(v, np.float32) for v in (wmin, wdelta, trans, scal)]
+    st = lib.orc_convert_and_transform(a.shape[0], _p(a), src_bits, _p(out), *[_p(v) for v in vecs])
+    if st != OK:
+        raise OracleError(st, "convert_and_transform")
+    return out
 
 
 def activate_space_cpu(pos, logdim=(3, 3, 3, 3, 5), orig=(0, 0, 0)):

@@ -109,7 +109,7 @@ struct Mod {
     bool loaded = false;
     CUmodule m = nullptr;
     CUfunction splitpos, calcbrick, link, extra, increextra, delinkleaf, delink, insertpts, scatter, setflag,
-        countsc, insertsc, scpos, gatherd, gatherl, apronf, apronf4;
+        countsc, insertsc, scpos, gatherd, gatherl, apronf, apronf4, insertsc16, gatherl16, convxform;
 } g_mod;
 
 struct DBuf {
@@ -164,6 +164,7 @@ struct rh_grid {
     DBuf pnode, poff, gcnt;
     DBuf scflag, scmap, sccnt, scoff, scpts, scpos, scnid;
     int sc_len = 0, num_sc = 0;
+    float3 pos_min{0, 0, 0}, pos_range{0, 0, 0};  // mPosMin, mPosRange of GetBoundingBox (VG.cpp:5452-5462)
 };
 
 namespace {
@@ -514,7 +515,8 @@ int rh_load(const char* module_ptx)
               {&g_mod.countsc, "gvdbCountSubcell"},       {&g_mod.insertsc, "gvdbInsertSubcell"},
               {&g_mod.scpos, "gvdbCalcSubcellPos"},       {&g_mod.gatherd, "gvdbGatherDensity"},
               {&g_mod.gatherl, "gvdbGatherLevelSet"},     {&g_mod.apronf, "gvdbUpdateApronF"},
-              {&g_mod.apronf4, "gvdbUpdateApronF4"}};
+              {&g_mod.apronf4, "gvdbUpdateApronF4"},      {&g_mod.insertsc16, "gvdbInsertSubcell_fp16"},
+              {&g_mod.gatherl16, "gvdbGatherLevelSet_fp16"}, {&g_mod.convxform, "gvdbConvAndTransform"}};
     for (auto& e : fs) RH_CK(cuModuleGetFunction(e.f, g_mod.m, e.name));
     g_mod.loaded = true;
     return 0;
@@ -611,13 +613,18 @@ int rh_rebuild(rh_grid* g, float radius, const float* orig, int mode, int min_de
         mx[a] = *std::max_element(v[a].begin(), v[a].end());
     }
     int pmin[3], pmax[3];
+    float plo[3], phi[3];
     for (int a = 0; a < 3; a++) {
         float lo = mn[a] - 1, hi = mx[a] + 2;
         lo = 0 > lo ? 0 : lo;
         hi = 0 > hi ? 0 : hi;
+        plo[a] = lo;
+        phi[a] = hi;
         pmin[a] = (int)lo;
         pmax[a] = (int)hi;
     }
+    g->pos_min = make_float3(plo[0], plo[1], plo[2]);
+    g->pos_range = make_float3(phi[0] - plo[0], phi[1] - plo[1], phi[2] - plo[2]);
     int depth = -1, rootpos[3] = {0, 0, 0};
     for (int lev = 0; lev < g->levels; lev++) {
         int r = g->range[lev];
@@ -788,6 +795,104 @@ int rh_gather(rh_grid* g, int levelset, int sc, float radius, float rins, const 
     if (launch(levelset ? g_mod.gatherl : g_mod.gatherd, numSC, 1, 1, sc, sc, sc, a5)) return -1;
     RH_CK(cuCtxSynchronize());
     return 0;
+}
+
+// InsertPointsSubcell_FP16 + GatherLevelSet_FP16 (VG.cpp:5094-5190, 5375-5401): the
+// FP32 orchestration above with the reference's FP16 kernels (ushort3 entries, no
+// velocities or colours)
+int rh_gather_fp16(rh_grid* g, int sc, float radius, float rins, const float* trans, int chan)
+{
+    float3 t = make_float3(trans[0], trans[1], trans[2]);
+    if (prepare(g, true)) return -1;
+    int numBrick = g->used0;
+    int scdim = g->res[0] / sc;
+    int spb = scdim * scdim * scdim;
+    int numSC = spb * numBrick;
+    int3 range = make_int3(g->range[0] / scdim, g->range[0] / scdim, g->range[0] / scdim);
+    int M = (int)g->nodes[0].size();
+    if (dens(g->scflag, (size_t)M * 4 + 4) || dens(g->scmap, (size_t)M * 4 + 4)) return -1;
+    CUdeviceptr info = g->dinfo.p, fl = g->scflag.p;
+    void* a1[] = {&info, &M, &fl};
+    if (launch(g_mod.setflag, M / 512 + 1, 1, 1, 512, 1, 1, a1)) return -1;
+    RH_CK(cuCtxSynchronize());
+    std::vector<int> flag(M), map(M);
+    RH_CK(cuMemcpyDtoH(flag.data(), g->scflag.p, (size_t)M * 4));
+    int acc = 0;
+    for (int i = 0; i < M; i++) {
+        map[i] = acc;
+        acc += flag[i];
+    }
+    RH_CK(cuMemcpyHtoD(g->scmap.p, map.data(), (size_t)M * 4));
+    if (dens(g->sccnt, (size_t)numSC * 4 + 4) || dens(g->scoff, (size_t)numSC * 4 + 4)) return -1;
+    RH_CK(cuMemsetD8(g->sccnt.p, 0, (size_t)numSC * 4 + 4));
+    int n = g->n, off = 0, stride = 12;
+    CUdeviceptr pos = g->dpos.p, cnt = g->sccnt.p, mp = g->scmap.p;
+    void* a2[] = {&info, &sc, &spb, &n, &pos, &off, &stride, &cnt, &range, &t, &scdim, &rins, &numSC, &mp};
+    if (launch(g_mod.countsc, n / 512 + 1, 1, 1, 512, 1, 1, a2)) return -1;
+    RH_CK(cuCtxSynchronize());
+    std::vector<int> c(numSC), o(numSC);
+    RH_CK(cuMemcpyDtoH(c.data(), g->sccnt.p, (size_t)numSC * 4));
+    int len = 0;
+    for (int i = 0; i < numSC; i++) {
+        o[i] = len;
+        len += c[i];
+    }
+    g->sc_len = len;
+    g->num_sc = numSC;
+    RH_CK(cuMemcpyHtoD(g->scoff.p, o.data(), (size_t)numSC * 4));
+    RH_CK(cuMemsetD8(g->sccnt.p, 0, (size_t)numSC * 4));
+    if (dens(g->scpts, (size_t)len * 6 + 8) || dens(g->scpos, (size_t)numSC * 12 + 12) ||
+        dens(g->scnid, (size_t)numSC * 4 + 4))
+        return -1;
+    CUdeviceptr offp = g->scoff.p, pts = g->scpts.p, zero = 0;
+    int zi = 0;
+    float3 vmin = make_float3(0, 0, 0), vrange = make_float3(1, 1, 1);
+    void* a3[] = {&info, &sc, &spb, &n, &cnt, &offp, &mp, &g->pos_min, &g->pos_range, &vmin, &vrange, &range, &t,
+                  &scdim, &rins, &pos, &off, &stride, &pts, &zero, &zi, &zi, &zero, &zero, &zi, &zi, &zero};
+    if (len > 0 && launch(g_mod.insertsc16, n / 512 + 1, 1, 1, 512, 1, 1, a3)) return -1;
+    CUdeviceptr nid = g->scnid.p, scp = g->scpos.p;
+    void* a4[] = {&info, &nid, &scp, &M, &scdim, &spb, &sc, &mp};
+    if (launch(g_mod.scpos, M / 512 + 1, 1, 1, 512, 1, 1, a4)) return -1;
+    int chanc = -1;
+    void* a5[] = {&info, &n, &numSC, &radius, &g->pos_min, &g->pos_range, &vmin, &vrange, &nid, &cnt, &offp, &scp,
+                  &pts, &zero, &zero, &chan, &chanc};
+    if (launch(g_mod.gatherl16, numSC, 1, 1, sc, sc, sc, a5)) return -1;
+    RH_CK(cuCtxSynchronize());
+    return 0;
+}
+
+int rh_pos_bounds(rh_grid* g, float* out)
+{
+    out[0] = g->pos_min.x;
+    out[1] = g->pos_min.y;
+    out[2] = g->pos_min.z;
+    out[3] = g->pos_range.x;
+    out[4] = g->pos_range.y;
+    out[5] = g->pos_range.z;
+    return 0;
+}
+
+// ConvertAndTransform (VG.cpp:5668-5682) on host arrays through the reference's kernel
+int rh_convert(int n, const void* src, int srcbits, float* dst, const float* wmin, const float* wdelta,
+               const float* trans, const float* scal)
+{
+    CUdeviceptr ds = 0, dd = 0;
+    const size_t sb = (size_t)n * (srcbits == 2 ? 6 : 12);
+    RH_CK(cuMemAlloc(&ds, sb + 16));
+    RH_CK(cuMemAlloc(&dd, (size_t)n * 12 + 16));
+    RH_CK(cuMemcpyHtoD(ds, src, sb));
+    char sbits = (char)srcbits, dbits = 4;
+    float3 mn = make_float3(wmin[0], wmin[1], wmin[2]), dl = make_float3(wdelta[0], wdelta[1], wdelta[2]);
+    float3 tr = make_float3(trans[0], trans[1], trans[2]), sc = make_float3(scal[0], scal[1], scal[2]);
+    void* args[] = {&n, &ds, &sbits, &dd, &dbits, &mn, &dl, &tr, &sc};
+    int rc = launch(g_mod.convxform, n / 512 + 1, 1, 1, 512, 1, 1, args);
+    if (rc == 0) {
+        RH_CK(cuCtxSynchronize());
+        RH_CK(cuMemcpyDtoH(dst, dd, (size_t)n * 12));
+    }
+    cuMemFree(ds);
+    cuMemFree(dd);
+    return rc;
 }
 
 int rh_sc_len(rh_grid* g) { return g->sc_len; }

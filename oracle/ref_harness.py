@@ -61,7 +61,9 @@ def load():
            "rh_sc_len": ([vp], i), "rh_update_apron": ([vp, i, f], i), "rh_root_level": ([vp], i),
            "rh_num_nodes": ([vp, i], i), "rh_used_leaves": ([vp], i), "rh_last_mode": ([vp], i),
            "rh_atlas_subdim": ([vp, vp], i), "rh_get_nodes": ([vp, i, vp, i], i),
-           "rh_get_childlist": ([vp, i, vp, i64], i)}
+           "rh_get_childlist": ([vp, i, vp, i64], i),
+           "rh_gather_fp16": ([vp, i, f, f, vp, i], i), "rh_pos_bounds": ([vp, vp], i),
+           "rh_convert": ([i, vp, i, vp, vp, vp, vp, vp], i)}
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
         fn.argtypes = args
@@ -152,6 +154,19 @@ class RefGrid:
                                     int(accum)), "gather")
         return self.lib.rh_sc_len(self.h)
 
+    def gather_fp16(self, subcell, radius, radius_ins, trans=(0, 0, 0), chan=0):
+        """InsertPointsSubcell_FP16 + GatherLevelSet_FP16 through the reference's kernels"""
+        t = np.ascontiguousarray(trans, np.float32)
+        self._ck(self.lib.rh_gather_fp16(self.h, subcell, float(radius), float(radius_ins), _p(t), chan),
+                 "gather_fp16")
+        return self.lib.rh_sc_len(self.h)
+
+    def pos_bounds(self):
+        """(mPosMin, mPosRange) of the last GetBoundingBox"""
+        out = np.zeros(6, np.float32)
+        self.lib.rh_pos_bounds(self.h, _p(out))
+        return out[:3], out[3:]
+
     def update_apron(self, chan, boundval=0.0):
         self._ck(self.lib.rh_update_apron(self.h, chan, float(boundval)), "update_apron")
 
@@ -184,6 +199,17 @@ class RefGrid:
         out = np.zeros(n, np.uint64)
         self._ck(self.lib.rh_get_childlist(self.h, lev, _p(out), n), "get_childlist")
         return out
+
+
+def convert_and_transform(src, src_bits, wmin, wdelta, trans=(0, 0, 0), scal=(1, 1, 1)):
+    """ConvertAndTransform through the reference's gvdbConvAndTransform kernel"""
+    lib = load()
+    a = np.ascontiguousarray(src, np.uint16 if src_bits == 2 else np.float32)
+    out = np.zeros((a.shape[0], 3), np.float32)
+    vecs = [np.ascontiguousarray(v, np.float32) for v in (wmin, wdelta, trans, scal)]
+    if lib.rh_convert(a.shape[0], _p(a), src_bits, _p(out), *[_p(v) for v in vecs]) != 0:
+        raise RuntimeError("rh_convert: %s" % lib.rh_error().decode())
+    return out
 
 
 def dense_to_bricks(dense, subdim, P):

@@ -7,7 +7,9 @@
 //
 //   volume_gvdb_points <in.bin> <out.bin>
 // in:  int32 n, int32 mode (0 ScatterDensity, 1 cubic Splat, 2 ScatterDensity then two
-//      FUNC_SMOOTH iterations as gSprayDeposit runs them), float radius, n x float3
+//      FUNC_SMOOTH iterations as gSprayDeposit runs them, 3 gPointCloud's FP16 level set:
+//      topology at 2 radius, InsertPointsSubcell_FP16 + GatherLevelSet_FP16, UpdateApron(0, 3),
+//      two FUNC_SMOOTH iterations), float radius, n x float3
 // out: int32 levels; per level uint64 count + count 64-byte nodes; uint64 used;
 //      n int32 leaf ids (AUX_PNODE); per active leaf in pool order, brick^3 floats
 #include <cstdio>
@@ -48,12 +50,18 @@ int main(int argc, char** argv)
         gvdb.SetPoints(pos, vel, clr);
 
         gvdb.RequestFullRebuild(true);
-        gvdb.RebuildTopology(n, radius, Vector3DF(0, 0, 0));
+        gvdb.RebuildTopology(n, mode == 3 ? 2.0f * radius : radius, Vector3DF(0, 0, 0));
         gvdb.FinishTopology(false, true);
         gvdb.UpdateAtlas();
         gvdb.ClearChannel(0);
         gvdb.InsertPoints(n, Vector3DF(0, 0, 0), false);
-        if (mode == 0 || mode == 2) {
+        if (mode == 3) {
+            int sc_len = 0;
+            gvdb.InsertPointsSubcell_FP16(4, n, radius, Vector3DF(0, 0, 0), sc_len);
+            gvdb.GatherLevelSet_FP16(4, n, radius, Vector3DF(0, 0, 0), sc_len, 0, 0);
+            gvdb.UpdateApron(0, 3.0f);
+            gvdb.Compute(FUNC_SMOOTH, 0, 2, Vector3DF(1, 0, 0), true, true, 3.0f);
+        } else if (mode == 0 || mode == 2) {
             gvdb.ScatterDensity(n, radius, 1.0f, Vector3DF(0, 0, 0), true, false);
             gvdb.UpdateApron(0, 0.0f);
             if (mode == 2) gvdb.Compute(FUNC_SMOOTH, 0, 2, Vector3DF(4, 0, 0), true, true);

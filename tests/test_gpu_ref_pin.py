@@ -182,3 +182,61 @@ def test_gathers_match_reference_kernels(orc, gvx_mod, levelset):
         g.gather_density(4, len(pos), 1.0, n, chan=0)
     mine = g.read_channel(0)[:used, 1:-1, 1:-1, 1:-1].astype(np.float64)
     assert np.abs(mine - got).max() <= 1e-5 * max(1.0, np.abs(got).max())
+
+
+@pytest.mark.parametrize("src_bits", [2, 4])
+def test_convert_matches_reference_kernel(orc, src_bits):
+    """ConvertAndTransform: gPointCloud's point decode, (wmin + q * wdelta) * scal + trans; the
+    reference's build contracts both multiply-adds to FMAs, which the oracle restates"""
+    rng = np.random.default_rng(61 + src_bits)
+    n = 200_000
+    if src_bits == 2:
+        src = rng.integers(0, 65536, (n, 3)).astype(np.uint16)
+    else:
+        src = (rng.standard_normal((n, 3)) * 500).astype(np.float32)
+    wmin, wmax = np.array([-12.5, 3.25, 0.7], np.float32), np.array([1020.3, 511.9, 250.1], np.float32)
+    wdelta = ((wmax - wmin) / np.float32(65535.0)).astype(np.float32)
+    args = (wmin, wdelta, (0.5, -1.0, 2.0), (0.9, 1.1, 1.0))
+    a = rh.convert_and_transform(src, src_bits, *args)
+    b = orc.convert_and_transform(src, src_bits, *args)
+    assert np.array_equal(a, b), "%d of %d values differ" % (int((a != b).sum()), a.size)
+
+
+def test_fp16_gather_matches_reference_kernels(orc, gvx_mod):
+    """InsertPointsSubcell_FP16 + GatherLevelSet_FP16: the entry count bit for bit; the level set
+    within one quantisation step, the reference dividing with fast-math (2 ulp) where the oracle
+    and libgvx round correctly"""
+    import torch
+
+    pos = slab(30_000, 62)
+    r, o = pair(orc)
+    r.set_points(pos)
+    assert r.rebuild(2.0) == 0
+    r.update_atlas()
+    assert o.rebuild_topology(pos, 2.0) == orc.OK
+    o.update_atlas()
+    rmin, rrange = r.pos_bounds()
+    omin, omax = o.pos_bounds()
+    assert np.array_equal(rmin, omin) and np.array_equal(rrange, (omax - omin).astype(np.float32))
+    n_r = r.gather_fp16(4, 1.0, 1.0)
+    n_o = o.gather_fp16(pos, 1.0, 1.0, subcell=4, chan=0)
+    assert n_r == n_o
+    used = o.used_leaves()
+    a = r.read_bricks(0)[:used, 1:-1, 1:-1, 1:-1].astype(np.float64)
+    b = o.read_channel(0)[:used, 1:-1, 1:-1, 1:-1]
+    step = float(np.sqrt(3.0)) * float(rrange.max()) / 65535.0
+    assert np.abs(a - b).max() <= step + 1e-5 * max(1.0, float(np.abs(b).max()))
+    # libgvx against the reference's kernels the same way
+    g = gvx_mod.Grid(0)
+    g.configure((3, 3, 3, 3, 5))
+    g.add_channel(0, gvx_mod.T_FLOAT, 1)
+    pd = torch.from_numpy(pos).cuda()
+    g.set_points(len(pos), pd)
+    g.rebuild_topology(len(pos), 2.0, mode=gvx_mod.TOPO_FULL)
+    g.update_atlas()
+    n_g = g.insert_points_subcell_fp16(4, len(pos), 1.0)
+    g.gather_levelset_fp16(4, len(pos), 1.0, n_g, chan=0)
+    assert n_g == n_r
+    c = g.read_channel(0)[:used, 1:-1, 1:-1, 1:-1].astype(np.float64)
+    assert np.abs(c - a).max() <= step + 1e-5 * max(1.0, float(np.abs(a).max()))
+    print("FP16 level set: %.4f of voxels bit-identical to the reference's kernels" % float((c == a).mean()))

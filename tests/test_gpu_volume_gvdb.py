@@ -58,7 +58,7 @@ def run(program, tmp_path, pos, mode, radius):
     return nodes, used, pnode, bricks
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_volume_gvdb_class_matches_oracle(program, orc, tmp_path, mode):
     rng = np.random.default_rng(31 + mode)
     if mode in (0, 2):
@@ -66,13 +66,16 @@ def test_volume_gvdb_class_matches_oracle(program, orc, tmp_path, mode):
         gx = np.stack(np.meshgrid(np.arange(24), np.arange(16), np.arange(20), indexing="ij"), -1).reshape(-1, 3)
         pos = (3.0 * gx + 2.0 + rng.random(gx.shape) * 0.9).astype(np.float32)
         radius = 1.5
-    else:
+    elif mode == 1:
         pos = (rng.random((30_000, 3)) * np.array([100.0, 70.0, 130.0]) + 3.0).astype(np.float32)
         radius = 2.0
+    else:
+        pos = (rng.random((30_000, 3)) * np.array([100.0, 70.0, 130.0]) + 3.0).astype(np.float32)
+        radius = 1.0
     nodes, used, pnode, bricks = run(program, tmp_path, pos, mode, radius)
     o = orc.Oracle((3, 3, 3, 3, 5))
     o.add_channel(0, orc.T_FLOAT)
-    assert o.rebuild_topology(pos, radius) == orc.OK
+    assert o.rebuild_topology(pos, 2 * radius if mode == 3 else radius) == orc.OK
     o.update_atlas()
     for lev in range(o.root_level() + 1):
         ref = o.nodes(lev)
@@ -83,7 +86,11 @@ def test_volume_gvdb_class_matches_oracle(program, orc, tmp_path, mode):
     # every point's leaf holds it
     leaf_pos = nodes[0]["pos"][pnode]
     assert (pnode >= 0).all() and np.array_equal(leaf_pos, (np.floor(pos).astype(np.int32) // 8) * 8)
-    if mode in (0, 2):
+    if mode == 3:
+        o.gather_fp16(pos, radius, radius, subcell=4, chan=0)
+        o.update_apron(0, 3.0)
+        o.compute(orc.FUNC_SMOOTH, 0, 2, (1.0, 0.0, 0.0), update_apron=True, skip_over_aprons=True, boundval=3.0)
+    elif mode in (0, 2):
         o.splat(orc.SPLAT_REF_SCATTER, pos, radius)
         o.update_apron(0, 0.0)
         if mode == 2:
@@ -92,7 +99,10 @@ def test_volume_gvdb_class_matches_oracle(program, orc, tmp_path, mode):
         o.splat(orc.SPLAT_CUBIC, pos, radius)
     ref = o.read_channel(0)[:used, 1:-1, 1:-1, 1:-1]
     # bricks come out in pool order of the active leaves = atlas slot order
-    if mode == 2:
+    if mode == 3:
+        # the FP16 gather is bit-exact; the two smoothing passes are float sums against FP64
+        assert np.abs(bricks - ref).max() <= 2e-6 * max(1.0, np.abs(ref).max())
+    elif mode == 2:
         # smoothing averages the scatter's FP32 error down; judged as the scatter is
         assert np.abs(bricks - ref).max() <= 1e-6 * np.abs(ref).max()
         assert rel_error_significant(bricks, ref, frac=1e-2) <= DENSITY_TOL

@@ -312,3 +312,72 @@ def test_compute_fill_pattern_and_colours(orc):
     for p1, want in ((7.9, 7), (300.0, 255), (-3.0, 0)):
         o.compute(orc.FUNC_FILL_C, 2, 1, (p1, 0.0, 0.0), update_apron=False, skip_over_aprons=False)
         assert o.read_channel(2)[0, 1, 1, 1] == want
+
+
+def test_fp16_gather_known_values(orc):
+    """InsertPointsSubcell_FP16 + GatherLevelSet_FP16 (PT.cuh:154-216, 775-813): the point comes back
+    as q / 65535 * range + min with q = trunc((w - min) / range * 65535), each a float32 step"""
+    pos = np.array([[10.3, 11.7, 12.2], [13.9, 9.1, 10.6], [300.5, 200.5, 100.5]], np.float32)
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(pos, 1.0) == orc.OK
+    o.update_atlas()
+    lo, hi = o.pos_bounds()
+    # GetBoundingBox (VG.cpp:5452-5462): min - 1 and max + 2, clamped at 0
+    f32 = np.float32
+    assert lo.tolist() == [f32(10.3) - f32(1), f32(9.1) - f32(1), f32(10.6) - f32(1)]
+    assert hi.tolist() == [f32(300.5) + f32(2), f32(200.5) + f32(2), f32(100.5) + f32(2)]
+    n_sc = o.gather_fp16(pos, 1.0, 1.0, subcell=4, chan=0)
+    assert n_sc > 0
+    f = np.float32
+    rng = (hi - lo).astype(f)
+    q = np.floor(((pos - lo).astype(f) / rng).astype(f) * f(65535)).astype(np.uint16)
+    back = ((q.astype(f) / f(65535)).astype(f) * rng).astype(f) + lo
+    ch = o.read_channel(0)
+    leaf = o.nodes(0)
+    # the voxel (12, 10, 11) lies in leaf (8, 8, 8), slot 0: the two first points are listed in its subcell
+    assert leaf["pos"][0].tolist() == [8, 8, 8]
+    v = np.array([12, 10, 11], f)
+    d = (back[:2] - v).astype(f)
+    s2 = (d[:, 0] * d[:, 0]).astype(f)
+    s2 = (s2 + (d[:, 1] * d[:, 1]).astype(f)).astype(f)
+    s2 = (s2 + (d[:, 2] * d[:, 2]).astype(f)).astype(f)
+    want = min(f(3.0), *(np.sqrt(s2).astype(f) - f(1.0)))
+    assert ch[0, 1 + 3, 1 + 2, 1 + 4] == want  # local (4, 2, 3), padded, stored [z][y][x]
+    # a voxel no listed point reaches keeps 3
+    assert ch[0, 1 + 0, 1 + 7, 1 + 7] == 3.0
+
+
+def test_scatter_colours(orc):
+    """ScatterDensity with point colours (PT.cuh:555-571, 610-642)"""
+    pos = np.array([[10.2, 10.2, 10.2], [10.7, 10.4, 10.9], [10.5, 10.5, 10.1], [20.5, 10.5, 10.5]], np.float32)
+    clr = np.array([[10, 20, 30, 40], [20, 40, 61, 50], [0, 0, 0, 0], [7, 8, 9, 10]], np.uint8)
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    o.add_channel(1, orc.T_UCHAR4)
+    o.add_channel(3, orc.T_UCHAR4)
+    assert o.rebuild_topology(pos, 0.0) == orc.OK
+    o.update_atlas()
+    o.scatter_density(pos, 1.5, clr=clr, avg_color=False)
+    c3 = o.read_channel(3)
+    # voxel (10, 10, 10) of leaf (8, 8, 8): the three first points race; the highest index wins
+    assert c3[0, 1 + 2, 1 + 2, 1 + 2].tolist() == [0, 0, 0, 0]
+    assert c3[1, 1 + 2, 1 + 2, 1 + 4].tolist() == [7, 8, 9, 10]
+    o.clear_channel(0)
+    o.scatter_density(pos, 1.5, clr=clr, avg_color=True)
+    c1 = o.read_channel(1)
+    # integer means (10+20+0)/3, (20+40+0)/3, (30+61+0)/3, alpha 255
+    assert c1[0, 1 + 2, 1 + 2, 1 + 2].tolist() == [10, 20, 30, 255]
+    # after an avgColor call the colour buffer exists: a plain call then writes no colour
+    o.clear_channel(3)
+    o.scatter_density(pos, 1.5, clr=clr, avg_color=False)
+    assert not o.read_channel(3).any()
+
+
+def test_convert_and_transform_known_values(orc):
+    src = np.array([[0, 65535, 1000], [7, 8, 9]], np.uint16)
+    out = orc.convert_and_transform(src, 2, wmin=(-1.0, 0.0, 2.0), wdelta=(0.5, 2.0 ** -16, 1.0),
+                                    trans=(1.0, 0.25, -3.0), scal=(2.0, 4.0, 0.5))
+    assert out.tolist() == [[-1.0, 65535 * 2.0 ** -14 + 0.25, 498.0], [6.0, 8 * 2.0 ** -14 + 0.25, 2.5]]
+    f = np.array([[1.5, -2.0, 3.25]], np.float32)
+    assert orc.convert_and_transform(f, 4, (0, 0, 0), (1, 1, 1)).tolist() == [[1.5, -2.0, 3.25]]
