@@ -150,7 +150,8 @@ struct Tile {
 // depend on the split.  splat_unit processes work unit u = slot * slabs + slab.
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
 __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u, unsigned char* tile, uint64_t* bar,
-                                           int* s_rs_w, int* s_ro_w, uint32_t& phase, const int lane)
+                                           int* s_rs_w, int* s_ro_w, const uint16_t* s_magic, uint32_t& phase,
+                                           const int lane)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
     constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
@@ -234,11 +235,12 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     __syncwarp();
 
     // ---- candidates, 32 at a time, in sorted order.  Each lane tests one
-    // candidate and sizes the cells of its footprint in the slab (a cell = an
-    // x pair of a (y, z) row); the cells of all hits are then dealt to the
-    // lanes 32 at a time, and updates are applied point by point in sorted
-    // order, so every voxel sums its contributions in the same order in every
-    // brick that holds it.
+    // candidate and sizes the cells of its footprint in the slab (a cell = up
+    // to 4 consecutive x voxels of one (y, z) row); the cells of all hits are
+    // then dealt to the lanes 32 at a time.  Lanes whose cells share a row
+    // apply their updates one after another in lane order, which is the
+    // points' sorted order, so every voxel sums its contributions in the same
+    // order in every brick that holds it.
     for (int base = 0; base < total; base += 32) {
         const int v = base + lane;
         int idx = -1;
@@ -274,12 +276,13 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
                 zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
             }
             if (xl <= xh && yl <= yh && zl <= zh) {
-                const int nxp = (xh - xl + 2) >> 1, ny = yh - yl + 1;
-                ncell = nxp * ny * (zh - zl + 1);
+                const int nch = (xh - xl + 4) >> 2, ny = yh - yl + 1;
+                ncell = nch * ny * (zh - zl + 1);
                 box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
                 box1 = (uint32_t)zl | ((uint32_t)zh << 8);
-                // ceil(2^15 / n): (c * magic) >> 15 == c / n for c <= 2^15 / n (cells <= 7*14*14 here)
-                magic = ((32767u + (uint32_t)nxp) / (uint32_t)nxp) | (((32767u + (uint32_t)ny) / (uint32_t)ny) << 16);
+                // ceil(2^15 / n) from the table: (c * magic) >> 15 == c / n for c < 2^15 / n
+                // (a footprint has at most 3 chunks x 14 rows x 14 layers of cells here)
+                magic = (uint32_t)s_magic[nch] | ((uint32_t)s_magic[ny] << 16);
             }
         }
         // inclusive scan of the cell counts over the lanes
@@ -319,25 +322,25 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
             const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
             const int zl = (int)(b1 & 255u);
-            const int nxp = (xh - xl + 2) >> 1, ny = (int)(b0 >> 24) - yl + 1;
+            const int nch = (xh - xl + 4) >> 2, ny = (int)(b0 >> 24) - yl + 1;
             const int r = (int)(((uint32_t)cell * (mg & 0xFFFFu)) >> 15);
             const int zz = (int)(((uint32_t)r * (mg >> 16)) >> 15);
-            const int lx = xl + 2 * (cell - r * nxp), ly = yl + (r - zz * ny), lz = zl + zz;
-            // the lane's two voxels (lx, lx + 1) of row (ly, lz): index and value
-            int vi0 = -1, vi1 = -1;
-            float w0 = 0.f, w1 = 0.f;
+            const int lx = xl + 4 * (cell - r * nch), ly = yl + (r - zz * ny), lz = zl + zz;
+            // the lane's voxels lx .. min(lx + 3, xh) of row (ly, lz): values, and a bit per voxel touched
+            float w[4] = {0.f, 0.f, 0.f, 0.f};
+            uint32_t vm = 0u;
+            const int t0 = (lz * P + ly) * P + lx;
             if (act) {
-                const int t0 = (lz * P + ly) * P + lx;
                 if (!CUBIC) {
                     const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
                     const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
                     const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
                     const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
-                    w0 = pw * wxa * wyz;
-                    vi0 = t0;
+                    w[0] = pw * wxa * wyz;
+                    vm = 1u;
                     if (lx + 1 <= xh) {
-                        w1 = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
-                        vi1 = t0 + 1;
+                        w[1] = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
+                        vm |= 2u;
                     }
                 } else {
                     // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
@@ -367,7 +370,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
                     const float cl = e2 + r2l - ((ey + ez) + e1);
                     if (c1 + cl > 0.0f) {
 #pragma unroll
-                        for (int k = 0; k < 2; k++) {
+                        for (int k = 0; k < 4; k++) {
                             if (lx + k > xh) break;
                             const float dx = (float)(lx + k + Ox) - px;
                             const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
@@ -377,27 +380,23 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
                             const float q = d * inv_h;
                             const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
                             const float uu = __fdividef(t, h * (R + d));               // 2 - q
-                            const float wv = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
-                            if (k == 0) {
-                                w0 = wv;
-                                vi0 = t0;
-                            } else {
-                                w1 = wv;
-                                vi1 = t0 + 1;
-                            }
+                            w[k] = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
+                            vm |= 1u << k;
                         }
                     }
                 }
             }
-            // apply point by point: the lanes of one point touch distinct voxels
-            const int jprev = __shfl_up_sync(kFull, j, 1);
-            const uint32_t first = __ballot_sync(kFull, act && (lane == 0 || jprev != j));
-            const int npts = __popc(first);
-            const int pr = __popc(first & (0xFFFFFFFFu >> (31 - lane))) - 1;
-            for (int ph = 0; ph < npts; ph++) {
-                if (act && pr == ph) {
-                    if (vi0 >= 0) T::add(tile, vi0, w0, ux, uy, uz);
-                    if (vi1 >= 0) T::add(tile, vi1, w1, ux, uy, uz);
+            // lanes sharing a row apply in lane order (the cells of one point lie in distinct rows
+            // or distinct chunks of a row); rows apart apply together
+            const int key = act ? (lz * P + ly) : -1 - lane;
+            const uint32_t grp = __match_any_sync(kFull, key);
+            const int rank = __popc(grp & ((1u << lane) - 1u));
+            const int nph = (int)__reduce_max_sync(kFull, (uint32_t)rank) + 1;
+            for (int ph = 0; ph < nph; ph++) {
+                if (rank == ph && vm) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if ((vm >> k) & 1u) T::add(tile, t0 + k, w[k], ux, uy, uz);
                 }
                 __syncwarp();
             }
@@ -459,16 +458,19 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
     __shared__ int s_rs[kSlabWarps][28];
     __shared__ int s_ro[kSlabWarps][28];
+    __shared__ uint16_t s_magic[32];
+    if (threadIdx.x < 32) s_magic[threadIdx.x] = (uint16_t)(threadIdx.x ? (32767u + threadIdx.x) / threadIdx.x : 0u);
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
     }
-    __syncwarp();
+    __syncthreads();
     uint32_t phase = 0;
     const uint32_t units = a.nslots * (uint32_t)a.slabs;
     const uint32_t nw = gridDim.x * kSlabWarps;
     for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw)
-        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], phase, lane);
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], s_magic, phase,
+                                                lane);
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
 
@@ -487,7 +489,9 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     __shared__ int s_rs[kSlabWarps][28];
     __shared__ int s_ro[kSlabWarps][28];
     __shared__ uint32_t s_us[kBatchMaxGrids + 1];
+    __shared__ uint16_t s_magic[32];
     for (int i = threadIdx.x; i <= ngrids; i += blockDim.x) s_us[i] = ustart[i];
+    if (threadIdx.x < 32) s_magic[threadIdx.x] = (uint16_t)(threadIdx.x ? (32767u + threadIdx.x) / threadIdx.x : 0u);
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
@@ -506,7 +510,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
                 hi = mid - 1;
         }
         splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid], s_ro[wid],
-                                                phase, lane);
+                                                s_magic, phase, lane);
     }
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
