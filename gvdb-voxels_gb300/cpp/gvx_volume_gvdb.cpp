@@ -3,6 +3,7 @@
 // (gvdb_volume_gvdb.cpp = VG.cpp).
 #include "gvx_volume_gvdb.h"
 
+#include <cstdio>
 #include <cstring>
 
 namespace nvdb {
@@ -111,6 +112,31 @@ void VolumeGVDB::FillChannel(uchar chan, Vector4DF val)
     if (t == T_FLOAT) Compute(FUNC_FILL_F, chan, 1, p, false, false);
     else if (t == T_UCHAR) Compute(FUNC_FILL_C, chan, 1, p, false, false);
     else if (t == T_UCHAR4) Compute(FUNC_FILL_C4, chan, 1, p, false, false);
+}
+
+// LoadVBX (VG.cpp:507-686): false when the file cannot be opened, as the
+// reference returns; a malformed file throws
+bool VolumeGVDB::LoadVBX(const std::string fname, int force_maj, int force_min)
+{
+    need_grid();
+    FILE* probe = fopen(fname.c_str(), "rb");
+    if (!probe) return false;
+    fclose(probe);
+    check(gvx_load_vbx(g_, fname.c_str(), force_maj, force_min));
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    levels_ = inf.levels;
+    apron_ = inf.apron;
+    for (int c = 0; c < 32; c++) check(gvx_channel_type(g_, c, &chan_type_[c]));
+    topology_changed();
+    return true;
+}
+
+// SaveVBX (VG.cpp:1626-1768)
+void VolumeGVDB::SaveVBX(const std::string fname)
+{
+    need_grid();
+    check(gvx_save_vbx(g_, fname.c_str()));
 }
 
 // Compute (VG.cpp:4534-4558)

@@ -688,6 +688,17 @@ gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap)
     return GVX_OK;
 }
 
+gvx_status gvx_channel_type(gvx_grid* g, int chan, int* type)
+{
+    GVX_GUARD(g);
+    if (chan < 0 || chan >= GVX_MAXCH || !type) {
+        gvx_set_error("channel_type: channel %d", chan);
+        return GVX_ERR_INVALID_ARG;
+    }
+    *type = g->ch[chan].used ? g->ch[chan].type : -1;
+    return GVX_OK;
+}
+
 gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t* bytes)
 {
     gvx_status rc = gvx_channel_bytes(g, chan, bytes);

@@ -154,6 +154,9 @@ struct gvx_grid {
 // topology (gvx_topology.cu)
 gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth);
 gvx_status gvx_topo_update_atlas(gvx_grid* g);
+// a tree given as host node pools / child lists (levels 0..root_level; clists[0] unused)
+gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
+                           const uint64_t* const* clists);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);

@@ -1620,6 +1620,81 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     return GVX_OK;
 }
 
+// A tree given as node pools and child lists (LoadVBX, VG.cpp:507-686: Configure, PoolRead per level,
+// FinishTopology).  The pools are taken as they are; the leaf lookup, leaf keys and neighbour table
+// are derived from the level-0 pool as after a build, over a compact key space spanning the leaves;
+// the next RebuildTopology is a full one (Clear, VG.cpp:2487-2503, sets mRebuildTopo).
+gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
+                           const uint64_t* const* clists)
+{
+    if (!g->configured) {
+        gvx_set_error("topology import: Configure was not called");
+        return GVX_ERR_NOT_CONFIGURED;
+    }
+    if (root_level < 1 || root_level >= g->levels || counts[root_level] < 1) {
+        gvx_set_error("topology import: root level %d of a %d-level tree", root_level, g->levels);
+        return GVX_ERR_INVALID_ARG;
+    }
+    gvx_status rc = ensure_grid_scratch(g);
+    if (rc) return rc;
+    cudaStream_t st = g->stream;
+    const int b = g->brick, R = root_level;
+    // ---- compact key space over the leaves, aligned as a build aligns it inside the root
+    const GvxNode& root = nodes[R][0];
+    KeySpace ks;
+    const int root_span = g->range[R] / b;
+    const int align = 1 << g->tshift[R - 1];
+    int64_t total_bits = 0;
+    for (int a = 0; a < 3; a++) {
+        const int rl = root.pos[a] / b;
+        int lo = rl + root_span - 1, hi = rl;
+        for (int64_t i = 0; i < counts[0]; i++) {
+            const int c = nodes[0][i].pos[a] / b;
+            lo = std::min(lo, c);
+            hi = std::max(hi, c);
+        }
+        lo = std::max(lo, rl);
+        hi = std::min(hi, rl + root_span - 1);
+        if (hi < lo) hi = lo;
+        lo = rl + ((lo - rl) / align) * align;
+        ks.lo[a] = lo;
+        ks.bits[a] = ceil_log2((int64_t)hi - lo + 1);
+        total_bits += ks.bits[a];
+    }
+    if (total_bits > 30) {
+        gvx_set_error("topology import: the leaves span 2^%lld leaf cells; the compact key space holds 2^30",
+                      (long long)total_bits);
+        return GVX_ERR_UNSUPPORTED;
+    }
+    ks.total_bits = (int)total_bits;
+    // ---- pools
+    for (int l = 0; l < g->levels; l++) {
+        const int64_t c = l <= R ? counts[l] : 0;
+        g->count[l] = c;
+        if (c == 0) continue;
+        rc = grow_nodes(g, l, c);
+        if (rc) return rc;
+        GVX_CK(cudaMemcpyAsync(g->nodes[l].p, nodes[l], (size_t)c * sizeof(GvxNode), cudaMemcpyHostToDevice, st));
+        if (l > 0) {
+            const size_t vc = (size_t)g->res[l] * g->res[l] * g->res[l];
+            GVX_CK(cudaMemcpyAsync(g->clist[l].p, clists[l], (size_t)c * vc * sizeof(uint64_t),
+                                   cudaMemcpyHostToDevice, st));
+        }
+    }
+    g->root_level = R;
+    for (int a = 0; a < 3; a++) g->root_pos[a] = root.pos[a];
+    g->rebuild_topo = true;
+    g->last_rebuild = 1;
+    g->n_sorted = 0;
+    g->group_valid = false;
+    g->perm_valid = false;
+    g->sc_valid = false;
+    g->atlas_valid = false;
+    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, st));
+    const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << total_bits) / 32ull));
+    return build_active_lookup(g, ks, words0, true);
+}
+
 gvx_status gvx_topo_update_atlas(gvx_grid* g)
 {
     if (g->root_level < 0) {

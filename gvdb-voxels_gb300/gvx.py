@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libgvx.so")
 
 OK = 0
 ERR_NAMES = {1: "INVALID_ARG", 2: "NOT_CONFIGURED", 3: "CAPACITY", 4: "DEVICE", 5: "TIMEOUT",
-             6: "UNSUPPORTED", 7: "DEPTH", 8: "STATE"}
+             6: "UNSUPPORTED", 7: "DEPTH", 8: "STATE", 9: "IO"}
 
 T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
 TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
@@ -85,6 +85,8 @@ def load(path=None):
         "gvx_insert_points_subcell_fp16": ([vp, i, i, f, fp, ctypes.POINTER(i)], i),
         "gvx_gather_levelset_fp16": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_convert_and_transform": ([vp, vp, i, vp, i, i, fp, fp, fp, fp], i),
+        "gvx_channel_type": ([vp, i, ip], i),
+        "gvx_save_vbx": ([vp, ctypes.c_char_p], i), "gvx_load_vbx": ([vp, ctypes.c_char_p, i, i], i),
         "gvx_memcpy": ([i, vp, vp, ctypes.c_size_t, i], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
         "gvx_read_nodes": ([vp, i, vp, i64], i), "gvx_read_childlist": ([vp, i, vp, i64], i),
@@ -265,6 +267,19 @@ class Grid:
         """ConvertAndTransform: device uint16x3 (src_bits 2) or float3 (4) points -> device float3"""
         self._check(self.lib.gvx_convert_and_transform(self.h, _ptr(src), src_bits, _ptr(dst), 4, n, _f3(wmin),
                                                        _f3(wdelta), _f3(trans), _f3(scal)))
+
+    def _channel_type(self, chan):
+        t = ctypes.c_int(-1)
+        self._check(self.lib.gvx_channel_type(self.h, chan, ctypes.byref(t)))
+        return t.value
+
+    def save_vbx(self, path):
+        self._check(self.lib.gvx_save_vbx(self.h, os.fsencode(path)))
+
+    def load_vbx(self, path, force_major=0, force_minor=0):
+        """LoadVBX: configures the grid and its channels from the file"""
+        self._check(self.lib.gvx_load_vbx(self.h, os.fsencode(path), force_major, force_minor))
+        self._types = {c: t for c in range(32) for t in [self._channel_type(c)] if t >= 0}
 
     def update_apron(self, chan=None, boundval=0.0):
         if chan is None:

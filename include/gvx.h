@@ -43,6 +43,7 @@ typedef int gvx_status;
 #define GVX_ERR_UNSUPPORTED 6
 #define GVX_ERR_DEPTH 7
 #define GVX_ERR_STATE 8
+#define GVX_ERR_IO 9
 
 /* channel types: gvdb_types.h:70-78 */
 #define GVX_T_UCHAR 0
@@ -185,6 +186,21 @@ gvx_status gvx_insert_points_subcell_fp16(gvx_grid* g, int subcell, int n, float
  * sc_len are accepted as the reference's arguments; the lists hold the rest. */
 gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
                                     int sc_len, int chan_levelset, int chan_clr);
+/* SaveVBX / LoadVBX (VG.h:374-375, VG.cpp:1626-1768 / 507-686): the VBX
+ * file (GVDB_FILESPEC.txt, version 1.11 written) with the field order those
+ * functions use: header, one grid of topology type 2 (node pools and child
+ * lists of every level) and atlas layout 0 (each channel's dense atlas, slice
+ * by slice; FLOAT3 voxels 12 bytes on file).  Channels must be numbered
+ * 0..n-1.  LoadVBX configures the grid from the file (levels, dimensions,
+ * apron, atlas brick counts), takes the pools as they are, adds the channels,
+ * runs UpdateAtlas and uploads the atlas; it reads every grid of the file in
+ * turn, leaving the last, and the next RebuildTopology is a full one.
+ * force_major / force_minor > 0 override the file's version, as the
+ * reference's arguments do.  GVX_ERR_IO when the file cannot be opened,
+ * written or parsed. */
+gvx_status gvx_save_vbx(gvx_grid* g, const char* path);
+gvx_status gvx_load_vbx(gvx_grid* g, const char* path, int force_major, int force_minor);
+
 /* ConvertAndTransform (VG.h:559, VG.cpp:5668-5682, kernel PT.cuh:120-142):
  * device points src (three uint16 per point when src_bits is 2, three floats
  * when 4, densely packed) -> device float3 dst = (wmin + p * wdelta) * scal +
@@ -276,6 +292,9 @@ gvx_status gvx_read_atlas_map(gvx_grid* g, int32_t* out4, int64_t cap_slots);
 gvx_status gvx_channel_bytes(gvx_grid* g, int chan, int64_t* bytes);
 gvx_status gvx_read_channel(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
 gvx_status gvx_read_channel_dense(gvx_grid* g, int chan, void* out, int64_t cap_bytes);
+/* type of channel chan (GVX_T_*), -1 when the channel does not exist
+ * (mPool->getAtlas(chan).type, gvdb_allocator.h) */
+gvx_status gvx_channel_type(gvx_grid* g, int chan, int* type);
 /* device pointer of a channel (for in-HBM consumers and producers).  The
  * pointer stays the same until the atlas is reallocated (UpdateAtlas growing
  * it, or a channel re-added); the caller may write through it, so the next

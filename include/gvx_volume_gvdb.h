@@ -178,6 +178,10 @@ public:
                              Vector3DF wMin, Vector3DF wDelta, Vector3DF trans, Vector3DF scal);
     DataPtr& getAux(int id);
 
+    // ---- files (VG.h:374-375): VBX 1.11
+    bool LoadVBX(const std::string fname, int force_maj = 0, int force_min = 0);
+    void SaveVBX(const std::string fname);
+
     // ---- compute (VG.h:355): FUNC_FILL_F/C/C4 and FUNC_SMOOTH
     void Compute(int effect, uchar channel, int num_iterations, Vector3DF parameters, bool bUpdateApron,
                  bool skipOverAprons, float boundval = 0.0f);
