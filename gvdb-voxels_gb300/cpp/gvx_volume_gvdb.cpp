@@ -44,10 +44,11 @@ void VolumeGVDB::SetCudaDevice(int devid, void* ctx)
 void VolumeGVDB::Initialize() { need_grid(); }
 
 // Clear (VG.cpp:2487-2503): the next RebuildTopology starts from an empty tree
+// Clear (VG.cpp:2487-2503): empty tree, next rebuild full
 void VolumeGVDB::Clear()
 {
     need_grid();
-    check(gvx_request_full_rebuild(g_, 1));
+    check(gvx_clear(g_));
     topology_changed();
 }
 
@@ -127,6 +128,8 @@ bool VolumeGVDB::LoadVBX(const std::string fname, int force_maj, int force_min)
     check(gvx_get_info(g_, &inf));
     levels_ = inf.levels;
     apron_ = inf.apron;
+    mirror_.assign(levels_, std::vector<Node>());
+    mirror_gen_.assign(levels_, 0);
     for (int c = 0; c < 32; c++) check(gvx_channel_type(g_, c, &chan_type_[c]));
     topology_changed();
     return true;
@@ -156,12 +159,34 @@ void VolumeGVDB::ClearChannel(uchar chan)
     check(gvx_clear_channel(g_, chan));
 }
 
-// FinishTopology (VG.cpp:1579-1593): pools are on the device already; bounds
+// FinishTopology (VG.cpp:1579-1593): space activated on the host is committed
+// to the device (whatever pCommitPool says: the device pools are the tree);
+// the bounds of the active leaves
 void VolumeGVDB::FinishTopology(bool pCommitPool, bool pComputeBounds)
 {
     (void)pCommitPool;
+    (void)pComputeBounds;
     need_grid();
-    if (pComputeBounds) check(gvx_finish_topology(g_));
+    check(gvx_finish_topology(g_));
+    topology_changed();
+}
+
+// ActivateSpace(Vector3DF) (VG.cpp:2768-2776): the leaf's id when it existed, else ID_UNDEFL
+slong VolumeGVDB::ActivateSpace(Vector3DF pos)
+{
+    need_grid();
+    const float p[3] = {pos.x, pos.y, pos.z};
+    uint64_t id = ID_UNDEFL;
+    check(gvx_activate_space(g_, p, &id));
+    return (slong)id;
+}
+
+// RebuildTopologyCPU (VG.cpp:1220-1227): ActivateSpace of every point + pOrig
+void VolumeGVDB::RebuildTopologyCPU(int pNumPnts, Vector3DF pOrig, Vector3DF* pPos)
+{
+    need_grid();
+    const float o[3] = {pOrig.x, pOrig.y, pOrig.z};
+    check(gvx_rebuild_topology_cpu(g_, pNumPnts, o, (const float*)pPos));
 }
 
 // UpdateAtlas (VG.cpp:2630-2704): leaves get their atlas slots (mValue)

@@ -184,6 +184,7 @@ gvx_status gvx_destroy(gvx_grid* g)
         gvx_free(g->clist[l]);
     }
     for (int c = 0; c < GVX_MAXCH; c++) gvx_free(g->ch[c].data);
+    gvx_host_tree_free(g);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GVX_OK;
@@ -235,6 +236,7 @@ gvx_status gvx_configure(gvx_grid* g, int levels, const int* logdim, const int* 
     g->brick = g->res[0];
     g->P = g->brick + 2 * g->apron;
     g->configured = true;
+    g->topo_gen++;
     g->root_level = -1;
     g->rebuild_topo = true;
     g->curr_depth = -1;
@@ -425,7 +427,22 @@ gvx_status gvx_request_full_rebuild(gvx_grid* g, int on)
 gvx_status gvx_finish_topology(gvx_grid* g)
 {
     GVX_GUARD(g);
+    gvx_status rc = gvx_host_tree_commit(g);  // pools grown by ActivateSpace go to the device
+    if (rc) return rc;
     return gvx_topo_compute_bounds(g);
+}
+
+gvx_status gvx_clear(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    g->root_level = -1;
+    for (int l = 0; l < GVX_MAXLEV; l++) g->count[l] = 0;
+    g->used_leaves = 0;
+    g->rebuild_topo = true;
+    g->lookup_valid = g->group_valid = g->atlas_valid = g->nbr_valid = g->sc_valid = false;
+    g->perm_valid = false;
+    g->topo_gen++;
+    return GVX_OK;
 }
 
 gvx_status gvx_update_atlas(gvx_grid* g)

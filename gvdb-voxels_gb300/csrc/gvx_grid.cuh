@@ -149,11 +149,18 @@ struct gvx_grid {
     DevBuf api_keys[2], api_vals[2];
 
     int64_t launches = 0;
+
+    // host copy of the pools for ActivateSpace / RebuildTopologyCPU (gvx_cputopo.cu)
+    struct GvxHostTree* htree = nullptr;
+    uint64_t topo_gen = 0;  // advances whenever the device tree changes
 };
 
 // topology (gvx_topology.cu)
 gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth);
 gvx_status gvx_topo_update_atlas(gvx_grid* g);
+// host-side topology (gvx_cputopo.cu): FinishTopology's commit, release
+gvx_status gvx_host_tree_commit(gvx_grid* g);
+void gvx_host_tree_free(gvx_grid* g);
 // a tree given as host node pools / child lists (levels 0..root_level; clists[0] unused)
 gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
                            const uint64_t* const* clists);

@@ -1590,6 +1590,7 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
             gvx_set_error("AccumulateTopology: depth %d outside 1..%d", d, g->levels - 1);
             return GVX_ERR_DEPTH;
         }
+        g->topo_gen++;
         return incremental_status(g, topo_incremental(g, n, radius, o, d, true, mn, mx, act));
     }
     if (depth <= 0) {
@@ -1607,6 +1608,7 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
         g->rebuild_topo = true;  // "Depth change in rebuild": Clear + full rebuild
         g->curr_depth = depth;
     }
+    g->topo_gen++;  // the device tree changes (or is rebuilt) from here on
     if (!g->rebuild_topo) return incremental_status(g, topo_incremental(g, n, radius, o, depth, false, mn, mx, act));
     rc = topo_full(g, n, radius, o, depth, rootpos, mn, mx);
     if (rc) {
@@ -1682,6 +1684,7 @@ gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, c
         }
     }
     g->root_level = R;
+    g->topo_gen++;
     for (int a = 0; a < 3; a++) g->root_pos[a] = root.pos[a];
     g->rebuild_topo = true;
     g->last_rebuild = 1;

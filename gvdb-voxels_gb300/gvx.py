@@ -86,6 +86,8 @@ def load(path=None):
         "gvx_gather_levelset_fp16": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_convert_and_transform": ([vp, vp, i, vp, i, i, fp, fp, fp, fp], i),
         "gvx_channel_type": ([vp, i, ip], i),
+        "gvx_clear": ([vp], i), "gvx_activate_space": ([vp, fp, ctypes.POINTER(ctypes.c_uint64)], i),
+        "gvx_rebuild_topology_cpu": ([vp, i, fp, vp], i),
         "gvx_save_vbx": ([vp, ctypes.c_char_p], i), "gvx_load_vbx": ([vp, ctypes.c_char_p, i, i], i),
         "gvx_memcpy": ([i, vp, vp, ctypes.c_size_t, i], i),
         "gvx_get_info": ([vp, ctypes.POINTER(Info)], i),
@@ -267,6 +269,20 @@ class Grid:
         """ConvertAndTransform: device uint16x3 (src_bits 2) or float3 (4) points -> device float3"""
         self._check(self.lib.gvx_convert_and_transform(self.h, _ptr(src), src_bits, _ptr(dst), 4, n, _f3(wmin),
                                                        _f3(wdelta), _f3(trans), _f3(scal)))
+
+    def clear(self):
+        self._check(self.lib.gvx_clear(self.h))
+
+    def activate_space(self, pos):
+        """ActivateSpace: the leaf's id when it existed, else ID_UNDEFL (0xFFFFFFFF)"""
+        out = ctypes.c_uint64(0)
+        self._check(self.lib.gvx_activate_space(self.h, _f3(pos), ctypes.byref(out)))
+        return out.value
+
+    def rebuild_topology_cpu(self, pos, orig=None):
+        """RebuildTopologyCPU over host float3 points"""
+        p = np.ascontiguousarray(pos, np.float32)
+        self._check(self.lib.gvx_rebuild_topology_cpu(self.h, p.shape[0], _f3(orig), _ptr(p)))
 
     def _channel_type(self, chan):
         t = ctypes.c_int(-1)

@@ -128,8 +128,23 @@ gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float or
                                 int min_depth);
 /* RequestFullRebuild (VG.h:432) */
 gvx_status gvx_request_full_rebuild(gvx_grid* g, int on);
-/* FinishTopology (VG.h:405, VG.cpp:1579-1593) */
+/* FinishTopology (VG.h:405, VG.cpp:1579-1593): commits the space activated
+ * by gvx_activate_space / gvx_rebuild_topology_cpu to the device, then the
+ * bounds of the active leaves */
 gvx_status gvx_finish_topology(gvx_grid* g);
+/* Clear (VG.h:327, VG.cpp:2487-2503): empty tree, next rebuild full */
+gvx_status gvx_clear(gvx_grid* g);
+/* ActivateSpace(Vector3DF) (VG.h:398, VG.cpp:2768-2855) and
+ * RebuildTopologyCPU (VG.h:430, VG.cpp:1220-1227): the reference's host-side
+ * topology, one point at a time on the CPU (positions truncated to integers),
+ * on a host copy of the tree that FinishTopology commits: nodes are created in
+ * the reference's order (the leaf covering the point and its ancestors;
+ * Reparent grows the root upward), with mFlags 1.  node_id receives the leaf's
+ * id when it existed already, ID_UNDEFL (0xFFFFFFFF) when it is new.  A tree
+ * that needs more levels than configured makes FinishTopology fail with
+ * GVX_ERR_DEPTH.  host_pos: n float3, host memory. */
+gvx_status gvx_activate_space(gvx_grid* g, const float pos[3], uint64_t* node_id);
+gvx_status gvx_rebuild_topology_cpu(gvx_grid* g, int n, const float orig[3], const float* host_pos);
 /* UpdateAtlas (VG.h:406, VG.cpp:2630-2704) */
 gvx_status gvx_update_atlas(gvx_grid* g);
 

@@ -114,6 +114,7 @@ struct alignas(16) Node {
     uint64 mMask;
 };
 static_assert(sizeof(Node) == 64, "Node is 64 bytes");
+static_assert(sizeof(Vector3DF) == 12, "point arrays are packed float3");
 
 class GvxError : public std::runtime_error {
 public:
@@ -148,6 +149,8 @@ public:
     void UpdateApron(uchar chan, float boundval = 0.0f, bool changeCtx = true);
     void AtlasRetrieveBrickXYZ(uchar channel, Vector3DI minimumCorner, DataPtr& dest);
     void RebuildTopology(int pNumPnts, float pRadius, Vector3DF pOrig);
+    void RebuildTopologyCPU(int pNumPnts, Vector3DF pOrig, Vector3DF* pPos);
+    slong ActivateSpace(Vector3DF pos);
     void AccumulateTopology(int pNumPnts, float pRadius, Vector3DF pOrig, int iDepth = 1);
     void RequestFullRebuild(bool tf);
     int GetLevels() { return levels_; }

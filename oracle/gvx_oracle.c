@@ -1671,6 +1671,65 @@ static int64_t cpu_activate(cpu_tree* t, uint64_t nid, const int* pos, int* bnew
     }
 }
 
+/* the host tree kept across calls, its pools read back whole (the reference's
+ * host pools after ActivateSpace calls: nodes, child lists, root) */
+void* orc_cpu_tree_new(int levels, const int* logdim)
+{
+    if (levels < 2 || levels > MAXLEV) return NULL;
+    cpu_tree* t = (cpu_tree*)calloc(1, sizeof(cpu_tree));
+    t->levels = levels;
+    int r = 1;
+    for (int l = 0; l < levels; l++) {
+        t->logdim[l] = logdim[l];
+        t->res[l] = 1 << logdim[l];
+        r = l == 0 ? t->res[0] : r * t->res[l];
+        t->range[l] = r;
+    }
+    t->root = -1;
+    return t;
+}
+
+void orc_cpu_tree_free(void* h)
+{
+    cpu_tree* t = (cpu_tree*)h;
+    if (!t) return;
+    for (int l = 0; l < MAXLEV; l++) { free(t->nodes[l]); free(t->clist[l]); }
+    free(t);
+}
+
+/* ActivateSpace of each point + orig (RebuildTopologyCPU, VG.cpp:1220-1227) */
+int orc_cpu_tree_activate(void* h, int n, const float* pos, int stride, const float orig[3])
+{
+    cpu_tree* t = (cpu_tree*)h;
+    for (int i = 0; i < n; i++) {
+        int p[3];
+        for (int a = 0; a < 3; a++) p[a] = (int)(pos[(int64_t)i * stride + a] + (orig ? orig[a] : 0.f));
+        int bnew = 0;
+        if (cpu_activate(t, (uint64_t)t->root, p, &bnew, -1, 0) < 0) return ORC_ERR_DEPTH;
+    }
+    return ORC_OK;
+}
+
+int orc_cpu_tree_count(void* h, int lev) { return ((cpu_tree*)h)->cnt[lev]; }
+int64_t orc_cpu_tree_root(void* h) { return ((cpu_tree*)h)->root; }
+
+int orc_cpu_tree_nodes(void* h, int lev, orc_node* out, int cap)
+{
+    cpu_tree* t = (cpu_tree*)h;
+    if (cap < t->cnt[lev]) return ORC_ERR_ARG;
+    memcpy(out, t->nodes[lev], (size_t)t->cnt[lev] * sizeof(orc_node));
+    return ORC_OK;
+}
+
+int orc_cpu_tree_childlist(void* h, int lev, uint64_t* out, int64_t cap)
+{
+    cpu_tree* t = (cpu_tree*)h;
+    int64_t n = (int64_t)t->cnt[lev] * cpu_vc(t, lev);
+    if (lev < 1 || cap < n) return ORC_ERR_ARG;
+    memcpy(out, t->clist[lev], (size_t)n * sizeof(uint64_t));
+    return ORC_OK;
+}
+
 int orc_activate_space_cpu(int levels, const int* logdim, int n, const float* pos, int stride,
                            const float orig[3], int32_t* leaf_pos_out, int cap, int* root_level_out)
 {

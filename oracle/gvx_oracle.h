@@ -118,6 +118,14 @@ int orc_scatter_density(orc_grid* g, int n, const float* pos, int pos_stride, co
 /* InsertPointsSubcell_FP16 + GatherLevelSet_FP16 (VG.cpp:5094-5190, 5375-5401) */
 int orc_gather_fp16(orc_grid* g, int n, const float* pos, int pos_stride, const uint8_t* clr, float radius,
                     float radius_ins, const float trans[3], int subcell, int chan, int chan_clr, int64_t* sc_len);
+/* the reference's host tree (ActivateSpace, VG.cpp:2707-3027) kept across calls */
+void* orc_cpu_tree_new(int levels, const int* logdim);
+void orc_cpu_tree_free(void* h);
+int orc_cpu_tree_activate(void* h, int n, const float* pos, int stride, const float orig[3]);
+int orc_cpu_tree_count(void* h, int lev);
+int64_t orc_cpu_tree_root(void* h);
+int orc_cpu_tree_nodes(void* h, int lev, orc_node* out, int cap);
+int orc_cpu_tree_childlist(void* h, int lev, uint64_t* out, int64_t cap);
 /* ConvertAndTransform (VG.cpp:5668-5682) on host arrays */
 int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, const float wmin[3],
                               const float wdelta[3], const float trans[3], const float scal[3]);

@@ -61,6 +61,10 @@ def load():
         "orc_gather_fp16": ([vp, i, vp, i, vp, f, f, vp, i, i, i, vp], i), "orc_pos_bounds": ([vp, vp], None),
         "orc_scatter_density": ([vp, i, vp, i, vp, f, vp, i, i], i),
         "orc_convert_and_transform": ([i, vp, i, vp, vp, vp, vp, vp], i),
+        "orc_cpu_tree_new": ([i, vp], vp), "orc_cpu_tree_free": ([vp], None),
+        "orc_cpu_tree_activate": ([vp, i, vp, i, vp], i), "orc_cpu_tree_count": ([vp, i], i),
+        "orc_cpu_tree_root": ([vp], i64), "orc_cpu_tree_nodes": ([vp, i, vp, i], i),
+        "orc_cpu_tree_childlist": ([vp, i, vp, i64], i),
         "orc_compute": ([vp, i, i, i, vp, i, i, d], i),
         "orc_update_apron": ([vp, i, d], i), "orc_channel_size": ([vp, i], i64),
         "orc_read_channel": ([vp, i, vp, i64], i), "orc_write_channel": ([vp, i, vp, i64], i),
@@ -244,6 +248,46 @@ class Oracle:
         P = (1 << self.logdim[0]) + 2 * self.apron
         nc = self.ncomp[chan]
         return out.reshape((-1, P, P, P) + ((nc,) if nc > 1 else ()))
+
+
+class CpuTree:
+    """The reference's host tree (ActivateSpace / RebuildTopologyCPU), kept across calls"""
+
+    def __init__(self, logdim=(3, 3, 3, 3, 5)):
+        self.lib = load()
+        ld = np.ascontiguousarray(logdim, np.int32)
+        self.h = self.lib.orc_cpu_tree_new(len(logdim), _p(ld))
+        self.logdim = tuple(logdim)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_cpu_tree_free(self.h)
+            self.h = None
+
+    def activate(self, pos, orig=(0, 0, 0)):
+        pos = np.ascontiguousarray(pos, np.float32)
+        o = np.ascontiguousarray(orig, np.float32)
+        st = self.lib.orc_cpu_tree_activate(self.h, pos.shape[0], _p(pos), 3, _p(o))
+        if st != OK:
+            raise OracleError(st, "cpu_tree_activate")
+
+    def root(self):
+        return self.lib.orc_cpu_tree_root(self.h)
+
+    def nodes(self, lev):
+        n = self.lib.orc_cpu_tree_count(self.h, lev)
+        out = np.zeros(n, NODE_DTYPE)
+        if n:
+            self.lib.orc_cpu_tree_nodes(self.h, lev, _p(out), n)
+        return out
+
+    def childlist(self, lev):
+        r = 1 << self.logdim[lev]
+        n = self.lib.orc_cpu_tree_count(self.h, lev) * r * r * r
+        out = np.zeros(n, np.uint64)
+        if n:
+            self.lib.orc_cpu_tree_childlist(self.h, lev, _p(out), n)
+        return out
 
 
 def convert_and_transform(src, src_bits, wmin, wdelta, trans=(0, 0, 0), scal=(1, 1, 1)):

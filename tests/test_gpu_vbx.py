@@ -118,3 +118,26 @@ def test_vbx_errors(gvx_mod, tmp_path):
     g.add_channel(0, gvx_mod.T_FLOAT, 1)
     with pytest.raises(gvx_mod.GvxError):
         g.save_vbx(str(tmp_path / "empty.vbx"))  # no topology yet
+
+
+def test_vbx_through_the_drop_in_class(gvx_mod, tmp_path):
+    """SaveVBX / LoadVBX of nvdb::VolumeGVDB (tests/cpp/volume_gvdb_vbx.cpp)"""
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    pkg = os.path.join(root, "gvdb-voxels_gb300")
+    exe = str(tmp_path / "volume_gvdb_vbx")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(root, "include"),
+           os.path.join(root, "tests", "cpp", "volume_gvdb_vbx.cpp"), "-o", exe, "-L", pkg, "-lgvx_volume", "-lgvx",
+           "-Wl,-rpath," + pkg]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pos = (np.random.default_rng(72).random((20_000, 3)) * np.array([90.0, 70.0, 110.0]) + 2.0).astype(np.float32)
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([len(pos)], np.int32).tofile(f)
+        pos.tofile(f)
+    r = subprocess.run([exe, str(inp), str(tmp_path / "grid.vbx")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr + r.stdout
+    assert "bricks identical" in r.stdout and not r.stdout.startswith("0 ")

@@ -381,3 +381,29 @@ def test_convert_and_transform_known_values(orc):
     assert out.tolist() == [[-1.0, 65535 * 2.0 ** -14 + 0.25, 498.0], [6.0, 8 * 2.0 ** -14 + 0.25, 2.5]]
     f = np.array([[1.5, -2.0, 3.25]], np.float32)
     assert orc.convert_and_transform(f, 4, (0, 0, 0), (1, 1, 1)).tolist() == [[1.5, -2.0, 3.25]]
+
+
+def test_cpu_tree_known_answer(orc):
+    """ActivateSpace (VG.cpp:2805-2855) from an empty tree: the first point's leaf is the root,
+    the second point Reparents to the level-2 node covering both (VG.cpp:2726-2763); the old
+    root comes back as a child through the stop-node path"""
+    t = orc.CpuTree()
+    t.activate(two_points())
+    assert t.root() == 0x200  # Elem(0, 2, 0)
+    n0, n1, n2 = t.nodes(0), t.nodes(1), t.nodes(2)
+    assert n0["pos"].tolist() == [[8, 8, 8], [296, 200, 96]]
+    assert n1["pos"].tolist() == [[0, 0, 0], [256, 192, 64]]
+    assert n2["pos"].tolist() == [[0, 0, 0]]
+    assert (n0["flags"] == 1).all() and (n0["value"] == -1).all()
+    assert n0["parent"].tolist() == [0x100, 0x10100] and n1["parent"].tolist() == [0x200, 0x200]
+    assert n2["parent"].tolist() == [0xFFFFFFFF]
+    assert n1["childlist"].tolist() == [0x101, 0x10101] and n2["childlist"].tolist() == [0x201]
+    assert n0["childlist"].tolist() == [0xFFFFFFFF, 0xFFFFFFFF]
+    l1 = t.childlist(1).reshape(2, 512)
+    assert {(n, i): int(l1[n, i]) for n in range(2) for i in range(512) if l1[n, i] != UNDEF64} == {
+        (0, 73): 0x0, (1, 269): 0x10000}
+    root = t.childlist(2)
+    assert {i: int(v) for i, v in enumerate(root) if v != UNDEF64} == {0: 0x100, 92: 0x10100}
+    # a point in an existing leaf adds nothing
+    t.activate(np.array([[9.9, 12.0, 15.5]], np.float32))
+    assert len(t.nodes(0)) == 2
