@@ -177,7 +177,7 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
                       &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp,
-                      &g->sc_q, &g->sc_qclr};
+                      &g->sc_q, &g->sc_qclr, &g->own_stage};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -380,6 +380,39 @@ gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* 
     return GVX_OK;
 }
 
+// strided float3 records (staged on the device as they are) -> packed float3
+__global__ void k_pack_float3(const unsigned char* __restrict__ src, int stride, uint32_t n, float* __restrict__ dst)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* s = (const float*)(src + (size_t)i * stride);
+        dst[3 * (size_t)i] = s[0];
+        dst[3 * (size_t)i + 1] = s[1];
+        dst[3 * (size_t)i + 2] = s[2];
+    }
+}
+
+// one host -> device copy of n float3 records with a byte stride: packed records in one flat copy;
+// strided ones as the raw bytes, packed by a kernel (a 2D copy of 12-byte rows is one DMA row a point)
+static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int stride, int n)
+{
+    GVX_CK(gvx_ensure(dst, (size_t)n * 12));
+    if (stride == 12) {
+        GVX_CK(cudaMemcpyAsync(dst.p, src, (size_t)n * 12, cudaMemcpyHostToDevice, g->stream));
+        return GVX_OK;
+    }
+    if (stride & 3) {
+        gvx_set_error("CommitData: the point stride %d is not a multiple of 4 bytes", stride);
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(gvx_ensure(g->own_stage, (size_t)n * stride));
+    GVX_CK(cudaMemcpyAsync(g->own_stage.p, src, (size_t)(n - 1) * stride + 12, cudaMemcpyHostToDevice, g->stream));
+    k_pack_float3<<<std::min<unsigned>((unsigned)((n + 255) / 256), 152u * 16u), 256, 0, g->stream>>>(
+        g->own_stage.as<unsigned char>(), stride, (uint32_t)n, dst.as<float>());
+    g->launches++;
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
 gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_stride, const void* vel,
                                   int vel_stride, const float* weight, const float* radius)
 {
@@ -388,11 +421,11 @@ gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_s
         gvx_set_error("CommitData: invalid host points");
         return GVX_ERR_INVALID_ARG;
     }
-    GVX_CK(gvx_ensure(g->own_pos, (size_t)n * 12));
-    GVX_CK(cudaMemcpy2DAsync(g->own_pos.p, 12, pos, pos_stride, 12, n, cudaMemcpyHostToDevice, g->stream));
+    gvx_status rc0 = upload_float3(g, g->own_pos, pos, pos_stride, n);
+    if (rc0) return rc0;
     if (vel) {
-        GVX_CK(gvx_ensure(g->own_vel, (size_t)n * 12));
-        GVX_CK(cudaMemcpy2DAsync(g->own_vel.p, 12, vel, vel_stride, 12, n, cudaMemcpyHostToDevice, g->stream));
+        rc0 = upload_float3(g, g->own_vel, vel, vel_stride, n);
+        if (rc0) return rc0;
     }
     if (weight) {
         GVX_CK(gvx_ensure(g->own_w, (size_t)n * 4));

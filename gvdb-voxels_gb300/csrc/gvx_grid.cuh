@@ -107,6 +107,7 @@ struct gvx_grid {
     // points
     GvxPoints pts;
     DevBuf own_pos, own_vel, own_w, own_r;  // storage of gvx_commit_points_host
+    DevBuf own_stage;                       // strided host records as copied, before packing
 
     // grouping of points by leaf (sorted order)
     DevBuf keys[2], vals[2];
