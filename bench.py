@@ -477,6 +477,60 @@ def run_batched(dev, iters=5):
             "tuning": tun}
 
 
+def run_point_cloud(dev, reps=5):
+    """Point-cloud level set, the sequence gPointCloud runs per frame: RebuildTopology (radius 2r,
+    full) + UpdateAtlas + ClearChannel + InsertPointsSubcell_FP16 (subcell 4, r) +
+    GatherLevelSet_FP16 + UpdateApron(0, 3) + Compute(FUNC_SMOOTH, 0, 1, (1, 0, 0), apron, packed, 3),
+    on the surface points of the 30 fusion frames taken as one cloud (r = 1).  Points on the device
+    before timing; CUDA-event time per stage on the grid's stream, median of `reps` runs."""
+    import numpy as np
+    import torch
+
+    import gvx
+    import workloads
+
+    pos = np.concatenate([p for p, _ in workloads.depth_fusion(frames=30, seed=3)])
+    n = len(pos)
+    pd = torch.from_numpy(pos).to(dev)
+    stream = torch.cuda.Stream(device=dev)
+    g = gvx.Grid(dev.index)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx.T_FLOAT, 1)
+    g.set_stream(stream.cuda_stream)
+    g.set_points(n, pd)
+    names = ("topology", "subcell_fp16", "gather_levelset_fp16", "apron", "smooth")
+    runs = []
+    with torch.cuda.stream(stream):
+        for r in range(reps + 2):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+            ev[0].record(stream)
+            g.rebuild_topology(n, 2.0, mode=gvx.TOPO_FULL)
+            g.update_atlas()
+            g.clear_channel(0)
+            ev[1].record(stream)
+            sc = g.insert_points_subcell_fp16(4, n, 1.0)
+            ev[2].record(stream)
+            g.gather_levelset_fp16(4, n, 1.0, sc, chan=0)
+            ev[3].record(stream)
+            g.update_apron(0, 3.0)
+            ev[4].record(stream)
+            g.compute(gvx.FUNC_SMOOTH, 0, 1, (1.0, 0.0, 0.0), update_apron=True, skip_over_aprons=True, boundval=3.0)
+            ev[5].record(stream)
+            torch.cuda.synchronize()
+            if r >= 2:
+                runs.append([ev[k].elapsed_time(ev[k + 1]) for k in range(len(names))])
+        inf = g.info()
+    g.close()
+    med = np.median(np.asarray(runs), axis=0)
+    total = float(med.sum())
+    return {"workload": "point_cloud: the 30 fusion frames' surface points as one cloud (%d points, 2048^3); "
+                        "RebuildTopology r=2 + UpdateAtlas + ClearChannel + InsertPointsSubcell_FP16(4, r=1) + "
+                        "GatherLevelSet_FP16 + UpdateApron(0, 3) + Compute(FUNC_SMOOTH, 1 iteration)" % n,
+            "points": n, "active_bricks": int(inf["used_leaves"]), "subcell_entries": int(sc),
+            "stage_ms": {k: round(float(v), 4) for k, v in zip(names, med)}, "ms_per_frame": round(total, 4),
+            "mpoints_s": round(n / (total * 1e-3) / 1e6, 1)}
+
+
 def run_fusion(dev, frames=30):
     """Surface-fusion workload: 30 depth frames (640x480, f = 525) of an analytic
     scene in 2048^3, each AccumulateTopology (radius 1) + UpdateAtlas + InsertPoints +
@@ -612,7 +666,7 @@ def main():
     ap.add_argument("--points", type=int, default=0, help="smaller runs for profiling (same density)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the differentiable, batched and fusion workloads")
+                    help="skip the differentiable, batched, fusion and point-cloud workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
@@ -632,6 +686,7 @@ def main():
         out["differentiable"] = run_differentiable(torch.device("cuda", 0))
         out["batched"] = run_batched(torch.device("cuda", 0))
         out["fusion"] = run_fusion(torch.device("cuda", 0))
+        out["point_cloud"] = run_point_cloud(torch.device("cuda", 0))
     if rank == 0:
         if pool is not None:
             out["cpu_baseline"] = cpu_baseline(pool)

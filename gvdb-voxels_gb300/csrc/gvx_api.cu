@@ -177,7 +177,7 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
                       &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp,
-                      &g->sc_q, &g->sc_qclr, &g->own_stage};
+                      &g->sc_q, &g->sc_qclr, &g->own_stage, &g->apron_tab};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);

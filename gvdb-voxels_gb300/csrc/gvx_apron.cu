@@ -8,8 +8,17 @@
 // full root-to-leaf descent per apron voxel; here the 26 neighbours of every
 // leaf are resolved once per topology (gvx_topology.cu, k_neighbors) and one
 // warp copies a brick's 6P^2-12P+8 apron voxels with loads/stores of the
-// channel's native element (float4 for FLOAT3/FLOAT4 channels).
+// channel's native element (float4 for FLOAT3/FLOAT4 channels).  The warp
+// first resolves the brick's 26 neighbour slots into shared memory; the
+// voxels then come from a table, built once per brick shape, of (apron voxel,
+// neighbour, source voxel in that neighbour).
+#include <vector>
+
 #include "gvx_grid.cuh"
+
+namespace {
+constexpr int kApronWarps = 8;
+}
 
 struct ApronArgs {
     int brick, P;
@@ -17,63 +26,71 @@ struct ApronArgs {
     const int* slot_leaf;
     const int* leaf_slot;
     const int* nbr;
+    const uint2* tab;  // per apron voxel: padded index | neighbour << 24, source index in the neighbour
+    int napron;
     void* data;
 };
 
-// apron voxel number e of a padded brick (apron 1) -> padded coordinates
-__device__ __forceinline__ void apron_voxel(int e, int P, int& x, int& y, int& z)
-{
-    const int P2 = P * P;
-    if (e < 2 * P2) {
-        z = e < P2 ? 0 : P - 1;
-        const int r = e % P2;
-        y = r / P;
-        x = r % P;
-        return;
-    }
-    const int ring = 4 * P - 4;
-    const int j = e - 2 * P2;
-    z = 1 + j / ring;
-    const int r = j % ring;
-    if (r < 2 * P) {
-        y = r < P ? 0 : P - 1;
-        x = r % P;
-    } else {
-        const int r2 = r - 2 * P;
-        y = 1 + r2 / 2;
-        x = (r2 & 1) ? P - 1 : 0;
-    }
-}
-
 template <class T>
-__global__ void k_apron(ApronArgs a, T boundval)
+__global__ void __launch_bounds__(kApronWarps * 32) k_apron(ApronArgs a, T boundval)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ int s_ns[kApronWarps][27];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t wglobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int P = a.P, b = a.brick, P3 = P * P * P;
-    const int napron = 6 * P * P - 12 * P + 8;
+    const int P3 = a.P * a.P * a.P;
     T* data = (T*)a.data;
     for (uint32_t s = wglobal; s < a.nslots; s += nwarps) {
         const int leaf = a.slot_leaf[s];
-        const int* nb = a.nbr + (size_t)leaf * 27;
-        T* dst = data + (size_t)s * P3;
-        for (int e = lane; e < napron; e += 32) {
-            int x, y, z;
-            apron_voxel(e, P, x, y, z);
-            const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
-            const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
-            const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
-            const int nl = nb[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
-            const int ns = nl >= 0 ? a.leaf_slot[nl] : -1;
-            T v = boundval;
-            if (ns >= 0) {
-                const int sx = x - dx * b, sy = y - dy * b, sz = z - dz * b;  // padded coords in the neighbour
-                v = data[(size_t)ns * P3 + (sz * P + sy) * P + sx];
-            }
-            dst[(z * P + y) * P + x] = v;
+        if (lane < 27) {
+            const int nl = a.nbr[(size_t)leaf * 27 + lane];
+            s_ns[wid][lane] = nl >= 0 ? a.leaf_slot[nl] : -1;
         }
+        __syncwarp();
+        T* dst = data + (size_t)s * P3;
+#pragma unroll 4
+        for (int e = lane; e < a.napron; e += 32) {
+            const uint2 t = a.tab[e];
+            const int ns = s_ns[wid][t.x >> 24];
+            T v = boundval;
+            if (ns >= 0) v = data[(size_t)ns * P3 + t.y];
+            dst[t.x & 0xFFFFFFu] = v;
+        }
+        __syncwarp();
     }
+}
+
+// the table of k_apron for padded bricks of side P (apron 1)
+static std::vector<uint2> apron_table(int P, int b)
+{
+    const int napron = 6 * P * P - 12 * P + 8;
+    std::vector<uint2> t((size_t)napron);
+    for (int e = 0; e < napron; e++) {
+        int x, y, z;
+        const int P2 = P * P;
+        if (e < 2 * P2) {
+            z = e < P2 ? 0 : P - 1;
+            y = (e % P2) / P;
+            x = (e % P2) % P;
+        } else {
+            const int ring = 4 * P - 4, j = e - 2 * P2, r = j % ring;
+            z = 1 + j / ring;
+            if (r < 2 * P) {
+                y = r < P ? 0 : P - 1;
+                x = r % P;
+            } else {
+                y = 1 + (r - 2 * P) / 2;
+                x = ((r - 2 * P) & 1) ? P - 1 : 0;
+            }
+        }
+        const int dx = x == 0 ? -1 : (x == P - 1 ? 1 : 0);
+        const int dy = y == 0 ? -1 : (y == P - 1 ? 1 : 0);
+        const int dz = z == 0 ? -1 : (z == P - 1 ? 1 : 0);
+        const int k = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
+        const int sx = x - dx * b, sy = y - dy * b, sz = z - dz * b;  // padded coords in the neighbour
+        t[e] = make_uint2((uint32_t)((z * P + y) * P + x) | ((uint32_t)k << 24), (uint32_t)((sz * P + sy) * P + sx));
+    }
+    return t;
 }
 
 gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval)
@@ -87,18 +104,27 @@ gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval)
         gvx_set_error("UpdateApron: no topology/atlas");
         return GVX_ERR_STATE;
     }
+    const int P = g->P;
+    if (g->apron_tab_P != P) {  // (P^3 < 2^24 for bricks up to 2^6: the packing holds)
+        const std::vector<uint2> tab = apron_table(P, g->brick);
+        GVX_CK(gvx_ensure(g->apron_tab, tab.size() * sizeof(uint2)));
+        GVX_CK(cudaMemcpy(g->apron_tab.p, tab.data(), tab.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        g->apron_tab_P = P;
+    }
     ApronArgs a;
     a.brick = g->brick;
     a.P = g->P;
+    a.tab = g->apron_tab.as<uint2>();
+    a.napron = 6 * P * P - 12 * P + 8;
     a.nslots = (uint32_t)g->atlas_used;
     a.slot_leaf = g->slot_leaf.as<int>();
     a.leaf_slot = g->leaf_slot.as<int>();
     a.nbr = g->nbr.as<int>();
     a.data = g->ch[chan].data.p;
     if (a.nslots == 0) return GVX_OK;
-    const unsigned threads = 256;
+    const unsigned threads = kApronWarps * 32;
     const uint64_t warps_needed = a.nslots;
-    unsigned blocks = (unsigned)std::min<uint64_t>((warps_needed + 7) / 8, 152ull * 16ull);
+    unsigned blocks = (unsigned)std::min<uint64_t>((warps_needed + kApronWarps - 1) / kApronWarps, 152ull * 16ull);
     switch (g->ch[chan].type) {
     case GVX_T_FLOAT:
         k_apron<float><<<blocks, threads, 0, g->stream>>>(a, boundval);

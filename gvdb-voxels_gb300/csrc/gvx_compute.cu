@@ -47,10 +47,13 @@ __device__ __forceinline__ size_t atlas_index(const AtlasShape& s, int X, int Y,
     return ((slot * s.P + (Z - bz * s.P)) * s.P + (Y - by * s.P)) * s.P + (X - bx * s.P);
 }
 
-// the reference's arithmetic: float sum, then v / (p1 + 6.0) + p2 in double (OP.cuh:397)
+// v / (p1 + 6) + p2 after the float sum.  The reference divides in double
+// (OP.cuh:397: a double literal); FP32 here, correctly rounded, is within one
+// float rounding of it and keeps the FP64 units (a small fraction of GB300's
+// throughput) off the stencil
 __device__ __forceinline__ float smooth_value(float v, float p1, float p2)
 {
-    return (float)((double)v / ((double)p1 + 6.0) + (double)p2);
+    return __fadd_rn(__fdiv_rn(v, __fadd_rn(p1, 6.0f)), p2);
 }
 
 }  // namespace

@@ -236,14 +236,23 @@ __global__ void k_gather_fp16(GatherQArgs a)
                 dist[q] = 3.0f;
                 c4[q][0] = c4[q][1] = c4[q][2] = c4[q][3] = 0.0f;
             }
-            for (uint32_t j = jb; j < je; j++) {
-                const uint2 qq = a.q[j];
-                const uint32_t u[3] = {qq.x & 0xFFFFu, qq.x >> 16, qq.y};
-                float p[3];
+            for (uint32_t j0 = jb; j0 < je; j0 += 32u) {
+                // 32 entries at a time: lane k reads back entry j0 + k once, the warp shares it
+                float4 mine = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j0 + lane < je) {
+                    const uint2 qq = a.q[j0 + lane];
+                    const uint32_t u[3] = {qq.x & 0xFFFFu, qq.x >> 16, qq.y};
+                    float p[3];
 #pragma unroll
-                for (int k = 0; k < 3; k++)
-                    p[k] = __fadd_rn(__fmul_rn(__fdiv_rn((float)u[k], 65535.0f), a.qrange[k]), a.qmin[k]);
-                const uint32_t cu = a.clr_out ? a.qclr[j] : 0u;
+                    for (int k = 0; k < 3; k++)
+                        p[k] = __fadd_rn(__fmul_rn(__fdiv_rn((float)u[k], 65535.0f), a.qrange[k]), a.qmin[k]);
+                    mine = make_float4(p[0], p[1], p[2], __uint_as_float(a.clr_out ? a.qclr[j0 + lane] : 0u));
+                }
+                const int cnt = (int)min(32u, je - j0);
+                for (int e = 0; e < cnt; e++) {
+                const float p[3] = {__shfl_sync(0xFFFFFFFFu, mine.x, e), __shfl_sync(0xFFFFFFFFu, mine.y, e),
+                                    __shfl_sync(0xFFFFFFFFu, mine.z, e)};
+                const uint32_t cu = __float_as_uint(__shfl_sync(0xFFFFFFFFu, mine.w, e));
 #pragma unroll
                 for (int q = 0; q < VPL; q++) {
                     const float dx = __fsub_rn(p[0], wx[q]), dy = __fsub_rn(p[1], wy[q]), dz = __fsub_rn(p[2], wz[q]);
@@ -255,6 +264,7 @@ __global__ void k_gather_fp16(GatherQArgs a)
                         for (int k = 0; k < 4; k++)
                             c4[q][k] = __fadd_rn(c4[q][k], __fdiv_rn(__fdiv_rn((float)((cu >> (8 * k)) & 255u), 255.0f), c));
                     }
+                }
                 }
             }
 #pragma unroll

@@ -102,6 +102,8 @@ struct gvx_grid {
     int64_t atlas_used = 0;
     GvxChannel ch[GVX_MAXCH];
     DevBuf amap;       // 4 ints per slot
+    DevBuf apron_tab;  // apron voxel table of the apron kernel, for bricks of side apron_tab_P
+    int apron_tab_P = 0;
     DevBuf atlas_tmp;  // second atlas of the unpacked (Jacobi) smoothing
 
     // points
