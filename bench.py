@@ -667,8 +667,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiable, batched, fusion and point-cloud workloads")
+    ap.add_argument("--extra", choices=["differentiable", "batched", "fusion", "point_cloud"],
+                    help="run only this workload and print its JSON (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.extra:
+        import torch
+
+        fn = {"differentiable": run_differentiable, "batched": run_batched, "fusion": run_fusion,
+              "point_cloud": run_point_cloud}[args.extra]
+        print(json.dumps(fn(torch.device("cuda", 0))))
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":
