@@ -222,7 +222,7 @@ __global__ void k_gather_fp16(GatherQArgs a)
         const int so[3] = {(loc % a.scdim) * sc, ((loc / a.scdim) % a.scdim) * sc, (loc / a.scdim / a.scdim) * sc};
         const uint32_t jb = a.beg[s], je = a.end[s];
         for (int v0 = 0; v0 < nv; v0 += 32 * VPL) {
-            float dist[VPL], wx[VPL], wy[VPL], wz[VPL], c4[VPL][4];
+            float m2[VPL], wx[VPL], wy[VPL], wz[VPL], c4[VPL][4];
             size_t idx[VPL];
 #pragma unroll
             for (int q = 0; q < VPL; q++) {
@@ -233,7 +233,7 @@ __global__ void k_gather_fp16(GatherQArgs a)
                 wy[q] = (float)(nd.pos[1] + ly);
                 wz[q] = (float)(nd.pos[2] + lz);
                 idx[q] = (((size_t)slot * a.P + (lz + a.apron)) * a.P + (ly + a.apron)) * a.P + (lx + a.apron);
-                dist[q] = 3.0f;
+                m2[q] = __int_as_float(0x7f800000);  // +inf: the smallest squared distance so far
                 c4[q][0] = c4[q][1] = c4[q][2] = c4[q][3] = 0.0f;
             }
             for (uint32_t j0 = jb; j0 < je; j0 += 32u) {
@@ -257,9 +257,9 @@ __global__ void k_gather_fp16(GatherQArgs a)
                 for (int q = 0; q < VPL; q++) {
                     const float dx = __fsub_rn(p[0], wx[q]), dy = __fsub_rn(p[1], wy[q]), dz = __fsub_rn(p[2], wz[q]);
                     const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    const float c = __fsqrt_rn(s2);
-                    dist[q] = fminf(dist[q], __fsub_rn(c, a.radius));
+                    m2[q] = fminf(m2[q], s2);
                     if (a.clr_out) {
+                        const float c = __fsqrt_rn(s2);
 #pragma unroll
                         for (int k = 0; k < 4; k++)
                             c4[q][k] = __fadd_rn(c4[q][k], __fdiv_rn(__fdiv_rn((float)((cu >> (8 * k)) & 255u), 255.0f), c));
@@ -270,7 +270,8 @@ __global__ void k_gather_fp16(GatherQArgs a)
 #pragma unroll
             for (int q = 0; q < VPL; q++) {
                 if (v0 + q * 32 + lane >= nv) continue;
-                a.out[idx[q]] = dist[q];
+                // min_j (sqrt(s2_j) - R) = sqrt(min_j s2_j) - R: rounded sqrt and subtraction are monotone
+                a.out[idx[q]] = fminf(3.0f, __fsub_rn(__fsqrt_rn(m2[q]), a.radius));
                 if (!a.clr_out) continue;
                 uint32_t u = 0u;
 #pragma unroll
@@ -320,14 +321,23 @@ __global__ void k_gather(GatherArgs a)
                 val[q] = a.levelset ? 3.0f : 0.0f;
                 if (a.accum && v < nv) val[q] = a.out[idx[q]];
             }
+            // the nearest listed point decides: min_j (c_j - R) and max_j (R - c_j) are the values at the
+            // smallest squared distance, rounded sqrt and subtraction being monotone
+            float m2[VPL];
+#pragma unroll
+            for (int q = 0; q < VPL; q++) m2[q] = __int_as_float(0x7f800000);
             for (uint32_t j = jb; j < je; j++) {
                 const float4 p = a.pts[j];
 #pragma unroll
                 for (int q = 0; q < VPL; q++) {
                     const float dx = p.x - wx[q], dy = p.y - wy[q], dz = p.z - wz[q];
-                    const float c = sqrtf(dx * dx + dy * dy + dz * dz);
-                    val[q] = a.levelset ? fminf(val[q], c - a.radius) : fmaxf(val[q], a.radius - c);
+                    m2[q] = fminf(m2[q], dx * dx + dy * dy + dz * dz);
                 }
+            }
+#pragma unroll
+            for (int q = 0; q < VPL; q++) {
+                const float c = sqrtf(m2[q]);  // +inf without points: the start value stays
+                val[q] = a.levelset ? fminf(val[q], c - a.radius) : fmaxf(val[q], a.radius - c);
             }
 #pragma unroll
             for (int q = 0; q < VPL; q++) {
