@@ -288,6 +288,35 @@ def run_ours(args, rank, world, pool):
         nb = inf["used_leaves"]
         P = inf["brick_res"] + 2 * inf["apron"]
 
+        # ---- the reference's default rebuild semantics (RebuildTopology's state machine, VG.cpp:1195-1217):
+        # after one full build, frames extend the tree incrementally; outside the timed region
+        incremental = None
+        if not args.no_extras and world == 1:
+            g.request_full_rebuild(True)
+            inc_ms, modes = [], []
+            for f in range(min(FRAMES, 12)):
+                flush.fill_(float(f))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                p = frames[f % FRAMES]
+                g.set_points(n, p, 0, 12, vel_d, 0, 12)
+                e0.record(stream)
+                g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_AUTO)
+                g.finish_topology()
+                g.update_atlas()
+                g.insert_points(n)
+                g.splat(gvx.SPLAT_CUBIC, n, RADIUS, chan_density=0, chan_vel=1)
+                g.update_apron(0, 0.0)
+                g.update_apron(1, 0.0)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                inc_ms.append(e0.elapsed_time(e1))
+                modes.append(g.info()["last_rebuild"])
+            steady = [t for t, m in zip(inc_ms, modes) if m == 2]
+            incremental = {"frames": len(inc_ms), "rebuilds": modes,
+                           "ms_per_incremental_frame": round(sum(steady) / max(len(steady), 1), 4),
+                           "mpoints_s": round(n / (sum(steady) / max(len(steady), 1) * 1e-3) / 1e6, 1) if steady else None,
+                           "active_bricks_last": int(g.info()["used_leaves"])}
+
         # ---- end to end through the C ABI with host buffers (pinned)
         e2e_steps = 0 if args.no_e2e else max(3, min(args.steps, 10))
         e2e_wall, d2h = 1.0, 0
@@ -336,6 +365,7 @@ def run_ours(args, rank, world, pool):
         "config": config_dict(n),
         "wall_s_timed_region": wall,
         "stage_ms": stage_ms,
+        "incremental": incremental,
         "hbm_gbs_step": (b_topo + b_pts + b_atlas + b_apron) / (ms * 1e-3) / 1e9,
         "active_bricks": nb,
         "roofline": {"kernel": "k_splat (cubic, density+velocity)", "bound": "hbm", "achieved": achieved,

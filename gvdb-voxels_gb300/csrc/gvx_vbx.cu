@@ -36,6 +36,16 @@ constexpr unsigned char kMajor = 1, kMinor = 11;  // MAJOR_VERSION / MINOR_VERSI
 struct File {
     FILE* f = nullptr;
     bool ok = true;
+    // bytes from the current position to the end (sizes read from a file are checked against it
+    // before anything is allocated)
+    int64_t left()
+    {
+        const long here = ftell(f);
+        if (here < 0 || fseek(f, 0, SEEK_END) != 0) return -1;
+        const long end = ftell(f);
+        if (fseek(f, here, SEEK_SET) != 0) return -1;
+        return (int64_t)end - (int64_t)here;
+    }
     ~File()
     {
         if (f) fclose(f);
@@ -283,6 +293,15 @@ extern "C" gvx_status gvx_load_vbx(gvx_grid* g, const char* path, int force_majo
                 return GVX_ERR_IO;
             }
         }
+        {
+            int64_t need = 0;
+            for (int l = 0; l < levels; l++) need += (int64_t)cnt0[l] * w0[l] + (int64_t)cnt1[l] * w1[l];
+            if (need > fp.left()) {
+                gvx_set_error("LoadVBX: %s: the topology tables need %lld bytes, the file holds fewer", path,
+                              (long long)need);
+                return GVX_ERR_IO;
+            }
+        }
         // Configure (VG.cpp:598): the file's levels and dimensions
         gvx_status rc = gvx_configure(g, levels, ld, nullptr);
         if (rc) return rc;
@@ -350,6 +369,12 @@ extern "C" gvx_status gvx_load_vbx(gvx_grid* g, const char* path, int force_majo
             if (!fp.ok || file_voxel_bytes(types[c]) == 0 || strides[c] != file_voxel_bytes(types[c])) {
                 gvx_set_error("LoadVBX: %s: channel %d of type %d, %d bytes a voxel", path, c, types[c], strides[c]);
                 return GVX_ERR_UNSUPPORTED;
+            }
+            if (axisres[0] <= 0 || axisres[1] <= 0 || axisres[2] <= 0 ||
+                (int64_t)axisres[0] * axisres[1] * axisres[2] * strides[c] > fp.left()) {
+                gvx_set_error("LoadVBX: %s: atlas %d x %d x %d of channel %d exceeds the file", path, axisres[0],
+                              axisres[1], axisres[2], c);
+                return GVX_ERR_IO;
             }
             dense[c].resize((size_t)axisres[0] * axisres[1] * axisres[2] * (size_t)strides[c]);
             fp.get(dense[c].data(), dense[c].size());

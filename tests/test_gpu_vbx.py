@@ -141,3 +141,23 @@ def test_vbx_through_the_drop_in_class(gvx_mod, tmp_path):
     r = subprocess.run([exe, str(inp), str(tmp_path / "grid.vbx")], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr + r.stdout
     assert "bricks identical" in r.stdout and not r.stdout.startswith("0 ")
+
+
+def test_vbx_counts_beyond_the_file_are_rejected(gvx_mod, tmp_path):
+    """a header whose tables would need more bytes than the file holds fails before allocating"""
+    import struct
+
+    hdr = struct.pack("<BB", 1, 11) + struct.pack("<12f", 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0)
+    hdr += struct.pack("<i", 1) + struct.pack("<Q", 2 + 48 + 4 + 8)
+    hdr += b"\0" * 256 + struct.pack("<BBB", ord("f"), 1, 0) + struct.pack("<3f", 1, 1, 1)
+    hdr += struct.pack("<i3iiiQBiB3i3i", 1, 8, 8, 8, 1, 1, 0, 2, 0, 0, 16, 16, 1, 160, 160, 10)
+    hdr += struct.pack("<iQ", 5, 0x200)
+    for lev, ld in enumerate((3, 3, 3, 3, 5)):
+        r = 1 << ld
+        hdr += struct.pack("<ii3iiiii", ld, r, r, r, r, 1 << 30, 64, (1 << 30) if lev else 0, 8 * r ** 3 if lev else 0)
+    path = tmp_path / "huge.vbx"
+    path.write_bytes(hdr + b"\0" * 1024)
+    h = gvx_mod.Grid(0)
+    with pytest.raises(gvx_mod.GvxError) as e:
+        h.load_vbx(str(path))
+    assert e.value.status == 9
