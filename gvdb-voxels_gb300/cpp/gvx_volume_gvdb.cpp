@@ -204,6 +204,20 @@ void VolumeGVDB::UpdateApron()
     check(gvx_update_apron_all(g_));
 }
 
+// UpdateApronFaces (VG.cpp:4461-4496): face aprons between face neighbours, float channels
+void VolumeGVDB::UpdateApronFaces(uchar chan)
+{
+    need_grid();
+    check(gvx_update_apron_faces(g_, chan));
+}
+
+// UpdateNeighbors (VG.cpp:2527-2556): the neighbour table comes with every topology
+void VolumeGVDB::UpdateNeighbors()
+{
+    need_grid();
+    check(gvx_update_neighbors(g_));
+}
+
 // UpdateApron(chan, boundval) (VG.cpp:4418-4457)
 void VolumeGVDB::UpdateApron(uchar chan, float boundval, bool changeCtx)
 {

@@ -553,6 +553,22 @@ gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval)
     return update_apron_one(g, chan, boundval);
 }
 
+gvx_status gvx_update_apron_faces(gvx_grid* g, int chan)
+{
+    GVX_GUARD(g);
+    return gvx_apron_faces_run(g, chan);
+}
+
+gvx_status gvx_update_neighbors(gvx_grid* g)
+{
+    GVX_GUARD(g);
+    if (g->root_level < 0 || !g->nbr_valid) {
+        gvx_set_error("UpdateNeighbors: no topology");
+        return GVX_ERR_STATE;
+    }
+    return GVX_OK;  // the neighbour table is built with every topology
+}
+
 gvx_status gvx_update_apron_all(gvx_grid* g)
 {
     GVX_GUARD(g);

@@ -12,6 +12,8 @@
 // first resolves the brick's 26 neighbour slots into shared memory; the
 // voxels then come from a table, built once per brick shape, of (apron voxel,
 // neighbour, source voxel in that neighbour).
+#include <string.h>
+
 #include <vector>
 
 #include "gvx_grid.cuh"
@@ -91,6 +93,74 @@ static std::vector<uint2> apron_table(int P, int b)
         t[e] = make_uint2((uint32_t)((z * P + y) * P + x) | ((uint32_t)k << 24), (uint32_t)((sz * P + sy) * P + sx));
     }
     return t;
+}
+
+// UpdateApronFaces (VG.cpp:4461-4496, gvdbUpdateApronFacesF OP.cuh:27-63): per active brick and
+// each of its -x, -y, -z face neighbours, the b^2 voxel pairs across the shared face: the
+// neighbour's +side apron takes the brick's first interior layer, the brick's -side apron the
+// neighbour's last.  Every apron voxel has one writer and only interior voxels are read.
+__global__ void __launch_bounds__(kApronWarps * 32) k_apron_faces(ApronArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t wglobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int P = a.P, b = a.brick, P3 = P * P * P;
+    float* data = (float*)a.data;
+    for (uint32_t s = wglobal; s < a.nslots; s += nwarps) {
+        const int leaf = a.slot_leaf[s];
+#pragma unroll 1
+        for (int side = 0; side < 3; side++) {
+            const int k = side == 0 ? 12 : (side == 1 ? 10 : 4);  // (-1,0,0), (0,-1,0), (0,0,-1) in the 27 table
+            const int nl = a.nbr[(size_t)leaf * 27 + k];
+            const int ns = nl >= 0 ? a.leaf_slot[nl] : -1;
+            if (ns < 0) continue;
+            float* self = data + (size_t)s * P3;
+            float* nbr = data + (size_t)ns * P3;
+            const int st[3] = {1, P, P * P};  // padded strides of x, y, z
+            const int ax = side, au = side == 0 ? 1 : 0, av = side == 2 ? 1 : 2;
+            for (int e = lane; e < b * b; e += 32) {
+                const int u = 1 + e % b, v = 1 + e / b;
+                const int base = u * st[au] + v * st[av];
+                const float v1 = self[base + 1 * st[ax]];  // the brick's first interior layer
+                const float v2 = nbr[base + b * st[ax]];   // the neighbour's last interior layer
+                nbr[base + (b + 1) * st[ax]] = v1;
+                self[base] = v2;
+            }
+        }
+    }
+}
+
+gvx_status gvx_apron_faces_run(gvx_grid* g, int chan)
+{
+    if (chan < 0 || chan >= GVX_MAXCH || !g->ch[chan].used) {
+        gvx_set_error("UpdateApronFaces: channel %d does not exist", chan);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (g->apron == 0) return GVX_OK;  // VG.cpp:4463
+    if (g->ch[chan].type != GVX_T_FLOAT) {
+        gvx_set_error("UpdateApronFaces: float channels only (the reference's one kernel, OP.cuh:27)");
+        return GVX_ERR_UNSUPPORTED;
+    }
+    if (g->root_level < 0 || !g->atlas_valid || !g->nbr_valid) {
+        gvx_set_error("UpdateApronFaces: no topology/atlas");
+        return GVX_ERR_STATE;
+    }
+    ApronArgs a;
+    memset(&a, 0, sizeof(a));
+    a.brick = g->brick;
+    a.P = g->P;
+    a.nslots = (uint32_t)g->atlas_used;
+    a.slot_leaf = g->slot_leaf.as<int>();
+    a.leaf_slot = g->leaf_slot.as<int>();
+    a.nbr = g->nbr.as<int>();
+    a.data = g->ch[chan].data.p;
+    if (a.nslots == 0) return GVX_OK;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((a.nslots + kApronWarps - 1) / kApronWarps, 152ull * 16ull);
+    k_apron_faces<<<blocks, kApronWarps * 32, 0, g->stream>>>(a);
+    g->launches++;
+    GVX_CK(cudaGetLastError());
+    g->ch[chan].apron_valid = false;  // edges and corners are not updated
+    return GVX_OK;
 }
 
 gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval)

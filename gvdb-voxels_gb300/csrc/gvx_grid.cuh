@@ -183,6 +183,7 @@ gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, 
 
 // apron (gvx_apron.cu)
 gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval);
+gvx_status gvx_apron_faces_run(gvx_grid* g, int chan);
 
 // channel storage (gvx_api.cu)
 gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need_slots);

@@ -86,6 +86,7 @@ def load(path=None):
         "gvx_gather_levelset_fp16": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_convert_and_transform": ([vp, vp, i, vp, i, i, fp, fp, fp, fp], i),
         "gvx_channel_type": ([vp, i, ip], i),
+        "gvx_update_apron_faces": ([vp, i], i), "gvx_update_neighbors": ([vp], i),
         "gvx_clear": ([vp], i), "gvx_activate_space": ([vp, fp, ctypes.POINTER(ctypes.c_uint64)], i),
         "gvx_rebuild_topology_cpu": ([vp, i, fp, vp], i),
         "gvx_save_vbx": ([vp, ctypes.c_char_p], i), "gvx_load_vbx": ([vp, ctypes.c_char_p, i, i], i),
@@ -269,6 +270,12 @@ class Grid:
         """ConvertAndTransform: device uint16x3 (src_bits 2) or float3 (4) points -> device float3"""
         self._check(self.lib.gvx_convert_and_transform(self.h, _ptr(src), src_bits, _ptr(dst), 4, n, _f3(wmin),
                                                        _f3(wdelta), _f3(trans), _f3(scal)))
+
+    def update_apron_faces(self, chan):
+        self._check(self.lib.gvx_update_apron_faces(self.h, chan))
+
+    def update_neighbors(self):
+        self._check(self.lib.gvx_update_neighbors(self.h))
 
     def clear(self):
         self._check(self.lib.gvx_clear(self.h))

@@ -247,6 +247,15 @@ gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const 
 /* UpdateApron(chan, boundval) / UpdateApron() (VG.h:407-408, VG.cpp:4411-4457) */
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
 gvx_status gvx_update_apron_all(gvx_grid* g);
+/* UpdateApronFaces (VG.h:409, VG.cpp:4461-4496, kernel OP.cuh:27-63): float
+ * channels only; per brick and face neighbour (-x, -y, -z), the apron voxels
+ * across the shared face take each other's interior layer.  Edges, corners
+ * and faces without a neighbour keep their values. */
+gvx_status gvx_update_apron_faces(gvx_grid* g, int chan);
+/* UpdateNeighbors (VG.h:448, VG.cpp:2527-2556): the face-neighbour table of
+ * UpdateApronFaces.  Every topology build makes the 26-neighbour table here,
+ * so this only checks that a topology exists. */
+gvx_status gvx_update_neighbors(gvx_grid* g);
 
 /* Compute(effect, channel, num_iterations, parameters, bUpdateApron,
  * skipOverAprons, boundval) (VG.h:355, VG.cpp:4532-4558) for the operators

@@ -147,6 +147,8 @@ public:
     void UpdateAtlas();
     void UpdateApron();
     void UpdateApron(uchar chan, float boundval = 0.0f, bool changeCtx = true);
+    void UpdateApronFaces(uchar chan);
+    void UpdateNeighbors();
     void AtlasRetrieveBrickXYZ(uchar channel, Vector3DI minimumCorner, DataPtr& dest);
     void RebuildTopology(int pNumPnts, float pRadius, Vector3DF pOrig);
     void RebuildTopologyCPU(int pNumPnts, Vector3DF pOrig, Vector3DF* pPos);

@@ -1404,6 +1404,50 @@ int orc_update_apron(orc_grid* g, int chan, double boundval)
     return g->degenerate ? ORC_ERR_DEGENERATE : ORC_OK;
 }
 
+/* UpdateNeighbors (VG.cpp:2527-2556) + UpdateApronFaces (VG.cpp:4461-4496,
+ * gvdbUpdateApronFacesF OP.cuh:27-63): per leaf, its -x, -y, -z face
+ * neighbours (the leaf covering the centre minus one brick), and for each
+ * the b^2 voxel pairs across the shared face: the neighbour's +side apron
+ * takes the leaf's first layer, the leaf's -side apron the neighbour's last
+ * layer.  Edges, corners and faces without a neighbour are not written.
+ * Float channels only, as the reference's kernel. */
+int orc_update_apron_faces(orc_grid* g, int chan)
+{
+    if (!g || chan < 0 || chan >= MAXCH || !g->ch[chan] || g->ncomp[chan] != 1) return ORC_ERR_ARG;
+    if (g->apron == 0) return ORC_OK;
+    pool* p0 = &g->pools[0];
+    const int b = g->brick;
+    for (int i = 0; i < p0->cnt; i++) {
+        orc_node* nd = &p0->nodes[i];
+        if (!nd->flags || nd->value[0] < 0) continue;
+        for (int side = 0; side < 3; side++) {
+            float ct[3] = {(float)nd->pos[0] + 0.5f * b, (float)nd->pos[1] + 0.5f * b, (float)nd->pos[2] + 0.5f * b};
+            ct[side] -= (float)b;
+            int64_t nid = get_node_at_point(g, ct);
+            if (nid < 0) continue;
+            orc_node* nb = &p0->nodes[nid];
+            if (nb->value[0] < 0) continue;
+            for (int u = 0; u < b; u++)
+                for (int v = 0; v < b; v++) {
+                    int self[3], other[3];
+                    if (side == 0) { self[0] = 0; self[1] = u; self[2] = v; }
+                    else if (side == 1) { self[0] = u; self[1] = 0; self[2] = v; }
+                    else { self[0] = u; self[1] = v; self[2] = 0; }
+                    for (int a = 0; a < 3; a++) other[a] = self[a];
+                    other[side] = b - 1;
+                    double v1 = *vox_ptr(g, chan, nd->value, self[0], self[1], self[2]);
+                    double v2 = *vox_ptr(g, chan, nb->value, other[0], other[1], other[2]);
+                    int na[3] = {other[0], other[1], other[2]}, sa[3] = {self[0], self[1], self[2]};
+                    na[side] = b;   /* the neighbour's apron across the face */
+                    sa[side] = -1;  /* the leaf's apron across the face */
+                    *vox_ptr(g, chan, nb->value, na[0], na[1], na[2]) = v1;
+                    *vox_ptr(g, chan, nd->value, sa[0], sa[1], sa[2]) = v2;
+                }
+        }
+    }
+    return ORC_OK;
+}
+
 /* ------------------------------------------------------------------ */
 /* atlas voxel (X, Y, Z) of a channel, brick-major storage */
 static double* atlas_voxel(orc_grid* g, int chan, int X, int Y, int Z)

@@ -126,6 +126,8 @@ int orc_cpu_tree_count(void* h, int lev);
 int64_t orc_cpu_tree_root(void* h);
 int orc_cpu_tree_nodes(void* h, int lev, orc_node* out, int cap);
 int orc_cpu_tree_childlist(void* h, int lev, uint64_t* out, int64_t cap);
+/* UpdateNeighbors + UpdateApronFaces (VG.cpp:2527-2556, 4461-4496): face aprons of float channels */
+int orc_update_apron_faces(orc_grid* g, int chan);
 /* ConvertAndTransform (VG.cpp:5668-5682) on host arrays */
 int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, const float wmin[3],
                               const float wdelta[3], const float trans[3], const float scal[3]);

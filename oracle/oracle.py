@@ -61,6 +61,7 @@ def load():
         "orc_gather_fp16": ([vp, i, vp, i, vp, f, f, vp, i, i, i, vp], i), "orc_pos_bounds": ([vp, vp], None),
         "orc_scatter_density": ([vp, i, vp, i, vp, f, vp, i, i], i),
         "orc_convert_and_transform": ([i, vp, i, vp, vp, vp, vp, vp], i),
+        "orc_update_apron_faces": ([vp, i], i),
         "orc_cpu_tree_new": ([i, vp], vp), "orc_cpu_tree_free": ([vp], None),
         "orc_cpu_tree_activate": ([vp, i, vp, i, vp], i), "orc_cpu_tree_count": ([vp, i], i),
         "orc_cpu_tree_root": ([vp], i64), "orc_cpu_tree_nodes": ([vp, i, vp, i], i),
@@ -236,6 +237,9 @@ class Oracle:
 
     def update_apron(self, chan, boundval=0.0):
         self._ck(self.lib.orc_update_apron(self.h, chan, float(boundval)), "update_apron")
+
+    def update_apron_faces(self, chan):
+        self._ck(self.lib.orc_update_apron_faces(self.h, chan), "update_apron_faces")
 
     def write_channel(self, chan, data):
         data = np.ascontiguousarray(data, np.float64).ravel()

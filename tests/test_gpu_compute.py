@@ -1,6 +1,6 @@
 """GPU parity of Compute (FUNC_SMOOTH, FUNC_FILL_F/C/C4) against the oracle on
 the same channel contents: smoothing within FP32 rounding (a float sum and
-the reference's double division against an FP64 restatement), fills bit for
+division against an FP64 restatement), fills and UpdateApronFaces bit for
 bit, over the whole atlas (aprons and unused slots included)."""
 import numpy as np
 import pytest
@@ -129,3 +129,28 @@ def test_unsupported_operator(gvx_mod, orc):
         g.compute(gvx_mod.FUNC_SMOOTH, 1, 1, (4.0, 0.0, 0.0), update_apron=False, skip_over_aprons=True)
     with pytest.raises(gvx_mod.GvxError):
         g.compute(gvx_mod.FUNC_FILL_C4, 0, 1, (1.0, 1.0, 1.0), update_apron=False, skip_over_aprons=True)
+
+
+def test_update_apron_faces_matches_oracle(gvx_mod, orc):
+    """UpdateApronFaces: face aprons exchanged between face neighbours; edges, corners and faces
+    without a neighbour keep their values (bit for bit against the oracle)"""
+    g, o = build(gvx_mod, orc)
+    data = seeded(g, 0, 9)
+    g.write_channel(0, data)
+    o.write_channel(0, data)
+    g.update_neighbors()
+    g.update_apron_faces(0)
+    o.update_apron_faces(0)
+    a, b = g.read_channel(0), o.read_channel(0)
+    assert np.array_equal(a.astype(np.float64), b)
+    changed = a != data
+    assert changed.any()
+    # only apron voxels of faces change: no interior voxel, no edge or corner
+    P = a.shape[1]
+    on = np.zeros((P, P, P), int)
+    for ax in range(3):
+        sl = [slice(None)] * 3
+        for end in (0, P - 1):
+            sl[ax] = end
+            on[tuple(sl)] += 1
+    assert not changed[:, on != 1].any()
