@@ -297,3 +297,25 @@ def test_radix_sort_entry_point(gvx_mod):
         assert np.array_equal(ko.cpu().numpy().view(np.uint32), keys[order])
         assert np.array_equal(vo.cpu().numpy().view(np.uint32), vals[order])
         g.close()
+
+
+def test_plain_small_32_cubed_bricks(gvx_mod, orc):
+    """the secondary C1 row: the samples' literal Configure(3,3,3,3,5) -- 32^3 bricks (padded 34^3, slab
+    tiles clamped to shared memory): topology, trilinear splat with its fused aprons, then UpdateApron.
+    In 256^3 the first pass holds one level-1 node, the reference's top_lev quirk (VG.cpp:3957-3968)
+    that the oracle reports as degenerate; this slab spans two level-1 nodes along x."""
+    rng = np.random.default_rng(0)
+    pos = (rng.random((60_000, 3)) * np.array([400.0, 90.0, 90.0]) + 1.0).astype(np.float32)
+    w = np.ones(len(pos), np.float32)
+    logdim = (5, 3, 3, 3, 3)
+    g, o = make_pair(gvx_mod, orc, pos, 1.0, logdim=logdim)
+    compare_topology(g, o)
+    g.commit_points_host(pos, weight=w)
+    g.insert_points(len(pos))
+    g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+    o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w, chan_density=0)
+    used = o.used_leaves()
+    assert rel_error(g.read_channel(0)[:used], o.read_channel(0)[:used]) <= DENSITY_TOL
+    g.update_apron(0, 0.5)
+    o.update_apron(0, 0.5)
+    assert rel_error(g.read_channel(0)[:used], o.read_channel(0)[:used]) <= DENSITY_TOL
