@@ -659,6 +659,36 @@ def reference_cuda(frames=3):
                     "orchestration, thrust sort/unique; ScatterDensity + UpdateApron of density"}
 
 
+def host_topology(frames=2):
+    """The reference's host-side topology path (ActivateSpace per point, then
+    FinishTopology; gvdb_volume_gvdb.cpp:2766-2855, 1579-1593) as the oracle
+    restates it, on the full 4M-point frame: single-threaded, as the reference's
+    host code is.  Points with a negative coordinate are left out, as the GPU path
+    drops them."""
+    import numpy as np
+    import workloads
+
+    sys.path.insert(0, ORACLE)
+    import oracle as O
+
+    pos0, vel = workloads.sph_slab(n=N_POINTS, seed=0, box=BOX)
+    times, npts, leaves = [], 0, 0
+    for f in range(frames):
+        pos = workloads.advect(pos0, vel, DT * f)
+        pos = pos[(pos >= 0.0).all(axis=1)]
+        t0 = time.perf_counter()
+        t = O.CpuTree(LOGDIM)
+        t.activate(pos)
+        leaves = int(t.lib.orc_cpu_tree_count(t.h, 0))
+        times.append(time.perf_counter() - t0)
+        npts = pos.shape[0]
+        del t
+    s = sum(times) / len(times)
+    return {"value": npts / s / 1e6, "unit": UNIT, "ms_per_frame": 1e3 * s, "points": int(npts), "leaves": leaves,
+            "frames": frames, "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
+            "path": "host ActivateSpace per point into the host pools (the oracle's restatement), one thread"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return None
@@ -683,6 +713,7 @@ def run_reference(args, world, rank):
                              "sample": "%d independent sub-boxes of 1/128 of the slab per step (%d points, same "
                                        "density), one per host core" % (workers, pts)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "host_topology": host_topology() if not args.no_extras else None,
             "reference_cuda": reference_cuda() if not args.no_extras else None}
 
 

@@ -120,14 +120,17 @@ template <bool HAS_DEN, bool HAS_VEL>
 struct Tile {
     static constexpr bool VEC = HAS_VEL;
     static __host__ __device__ size_t bytes(int P3) { return (size_t)P3 * (VEC ? 16 : 4); }
+    // The velocity sums are explicit fused multiply-adds: left to the compiler,
+    // `o.x += wgt * ux` may be fused in one kernel (or one unrolled copy) and not
+    // in another, and every brick must add a voxel's terms with the same rounding.
     __device__ static void add(unsigned char* t, int i, float wgt, float ux, float uy, float uz)
     {
         if (VEC) {
             float4* v = (float4*)t;
             float4 o = v[i];
-            o.x += wgt * ux;
-            o.y += wgt * uy;
-            o.z += wgt * uz;
+            o.x = __fmaf_rn(wgt, ux, o.x);
+            o.y = __fmaf_rn(wgt, uy, o.y);
+            o.z = __fmaf_rn(wgt, uz, o.z);
             if (HAS_DEN) o.w += wgt;
             v[i] = o;
         } else {
@@ -143,14 +146,213 @@ struct Tile {
     }
 };
 
+// The footprint cells of a batch of hit points (lane i holds the i-th point of
+// the batch in sorted order; lanes without a point have ncell 0), dealt to the
+// lanes 32 at a time.  Lanes whose cells share a row apply their updates one
+// after another in lane order, which is the points' sorted order (the cells of
+// one point lie in distinct rows or distinct chunks of a row); rows apart apply
+// together.  So every voxel sums its contributions in the same order in every
+// brick that holds it.
+//
+// SMALL footprints (trilinear, and cubic of a uniform radius <= 2) span at most
+// 4 voxels on every axis: a cell is one row of the box, and of a cubic box
+// only the rows that can reach the sphere are dealt.  Their decode is a table
+// of 5 bits per layer k of the box, at bit 5k: the first row (2 bits, counted
+// from yl) and the number of rows (3 bits).  Other footprints deal every row
+// of the box in chunks of up to 4 voxels, decoded by division with multipliers
+// m = ceil(2^32 / n) (umulhi(c, m) == c / n for every c < 2^32 / n; 0 stands
+// for n = 1).
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
+__device__ __forceinline__ void deal_cells(unsigned char* tile, const float4 p, const float4 uv, uint32_t box0,
+                                           const uint32_t box1, int ncell, const int P, const int Ox, const int Oy,
+                                           const int Zlo, const float R0, const float h0, const float inv_h0,
+                                           const float norm0, const float r2h0, const float r2l0, const int lane)
+{
+    using T = Tile<HAS_DEN, HAS_VEL>;
+    constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
+    uint32_t aux1 = 0u, aux2 = 0u;  // SMALL: the row table; else the multipliers of the chunk and row counts
+    if (ncell > 0) {
+        const int yl = (int)((box0 >> 16) & 255u), yh = (int)(box0 >> 24);
+        if (SMALL) {
+            const int zl = (int)(box1 & 255u), zh = (int)((box1 >> 8) & 255u);
+            // A row whose float dy, dz give dy^2 + dz^2 < R^2 (1 + 1e-6) in float holds every row
+            // with R^2 - dy^2 - dz^2 > 0 exactly (the rows the weights below can reach), with a
+            // margin of several roundings; the rows of one layer that pass form one run.
+            const float lim = r2h0 * 1.000001f;
+            int cnt = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (zl + k > zh) break;
+                int first = 0, n = yh - yl + 1;
+                if (CUBIC) {
+                    const float dz = (float)(zl + k + Zlo) - p.z;
+                    const float dz2 = dz * dz;
+                    first = -1;
+                    n = 0;
+#pragma unroll
+                    for (int yy = 0; yy < 4; yy++) {
+                        if (yl + yy > yh) break;
+                        const float dy = (float)(yl + yy + Oy) - p.y;
+                        if (dy * dy + dz2 < lim) {
+                            if (first < 0) first = yy;
+                            n++;
+                        }
+                    }
+                    first = max(first, 0);
+                }
+                aux1 |= (uint32_t)(first | (n << 2)) << (5 * k);
+                cnt += n;
+            }
+            // a point whose box reaches the slab but whose sphere does not keeps one (empty) row,
+            // so that every point of the batch owns a cell
+            if (cnt == 0) {
+                aux1 = 1u << 2;
+                cnt = 1;
+            }
+            ncell = cnt;
+            box0 = (box0 & 0x00FFFFFFu) | ((uint32_t)zl << 24);  // xl, xh, yl, zl
+        } else {
+            const uint32_t nch = (((box0 >> 8) & 255u) - (box0 & 255u) + 4u) >> 2;
+            const uint32_t ny = (uint32_t)(yh - yl + 1);
+            aux1 = nch > 1u ? 0xFFFFFFFFu / nch + 1u : 0u;
+            aux2 = ny > 1u ? 0xFFFFFFFFu / ny + 1u : 0u;
+        }
+    }
+    // inclusive scan of the cell counts over the lanes
+    int cend = ncell;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, cend, o);
+        if (lane >= o) cend += t;
+    }
+    const int ctot = __shfl_sync(kFull, cend, 31);
+    const int cstart = cend - ncell;
+    for (int g0 = 0; g0 < ctot; g0 += 32) {
+        const int g = g0 + lane;
+        const bool act = g < ctot;
+        // the point dealing this cell: the points are lanes 0 .. nb-1, each with a cell at least,
+        // so it is the number of points that start at or before g, less one
+        const bool own = ncell > 0;
+        const uint32_t starts =
+            __reduce_or_sync(kFull, own && cstart >= g0 && cstart < g0 + 32 ? 1u << (cstart - g0) : 0u);
+        const int before = __popc(__ballot_sync(kFull, own && cstart < g0));
+        const int j = before - 1 + __popc(starts & (kFull >> (31 - lane)));
+        const float px = __shfl_sync(kFull, p.x, j), py = __shfl_sync(kFull, p.y, j);
+        const float pz = __shfl_sync(kFull, p.z, j), pw = __shfl_sync(kFull, p.w, j);
+        float ux = 0.f, uy = 0.f, uz = 0.f;
+        if (HAS_VEL) {
+            ux = __shfl_sync(kFull, uv.x, j);
+            uy = __shfl_sync(kFull, uv.y, j);
+            uz = __shfl_sync(kFull, uv.z, j);
+        }
+        const uint32_t b0 = __shfl_sync(kFull, box0, j);
+        const uint32_t a1 = __shfl_sync(kFull, aux1, j);
+        const int cell = g - __shfl_sync(kFull, cstart, j);
+        const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
+        const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
+        int lx, ly, lz;
+        if (SMALL) {
+            const int s1 = (int)((a1 >> 2) & 7u), s2 = s1 + (int)((a1 >> 7) & 7u), s3 = s2 + (int)((a1 >> 12) & 7u);
+            const int k = (cell >= s1) + (cell >= s2) + (cell >= s3);
+            const int pre = k == 0 ? 0 : (k == 1 ? s1 : (k == 2 ? s2 : s3));
+            lx = xl;
+            ly = yl + (int)((a1 >> (5 * k)) & 3u) + (cell - pre);
+            lz = (int)(b0 >> 24) + k;
+        } else {
+            const uint32_t b1 = __shfl_sync(kFull, box1, j), m2 = __shfl_sync(kFull, aux2, j);
+            const int zl = (int)(b1 & 255u);
+            const int nch = (xh - xl + 4) >> 2, ny = (int)(b0 >> 24) - yl + 1;
+            const int r = a1 ? (int)__umulhi((uint32_t)cell, a1) : cell;  // cell / nch
+            const int zz = m2 ? (int)__umulhi((uint32_t)r, m2) : r;       // r / ny
+            lx = xl + 4 * (cell - r * nch);
+            ly = yl + (r - zz * ny);
+            lz = zl + zz;
+        }
+        // the lane's voxels lx .. min(lx + 3, xh) of row (ly, lz): values, and a bit per voxel touched
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+        uint32_t vm = 0u;
+        const int t0 = (lz * P + ly) * P + lx;
+        if (act) {
+            if (!CUBIC) {
+                const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
+                const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
+                const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
+                const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
+                w[0] = pw * wxa * wyz;
+                vm = 1u;
+                if (lx + 1 <= xh) {
+                    w[1] = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
+                    vm |= 2u;
+                }
+            } else {
+                // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
+                // support R = 2h.  Along the row R^2 - d^2 is formed from an error-free
+                // c = R^2 - dy^2 - dz^2 (two-product, two-sum) so that the outer branch
+                // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
+                // accuracy up to the edge of the support.
+                float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
+                if (PPR) {
+                    R = pR;
+                    h = 0.5f * R;
+                    inv_h = 1.0f / h;
+                    norm = kInvPi * inv_h * inv_h * inv_h;
+                    r2h = R * R;
+                    r2l = fmaf(R, R, -r2h);
+                }
+                norm *= pw;
+                const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
+                const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
+                const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
+                const float syz = qy + qz;
+                float bv = syz - qy;
+                const float e1 = (qy - (syz - bv)) + (qz - bv);
+                const float c1 = r2h - syz;
+                bv = c1 - r2h;
+                const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
+                const float cl = e2 + r2l - ((ey + ez) + e1);
+                if (c1 + cl > 0.0f) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        if (lx + k > xh) break;
+                        const float dx = (float)(lx + k + Ox) - px;
+                        const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
+                        if (t <= 0.0f) continue;
+                        const float d2 = fmaf(dx, dx, syz);
+                        const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                        const float q = d * inv_h;
+                        const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
+                        const float uu = __fdividef(t, h * (R + d));               // 2 - q
+                        w[k] = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
+                        vm |= 1u << k;
+                    }
+                }
+            }
+        }
+        // lanes sharing a row apply in lane order (the cells of one point lie in distinct rows
+        // or distinct chunks of a row); rows apart apply together
+        const int key = act ? (lz * P + ly) : -1 - lane;
+        const uint32_t grp = __match_any_sync(kFull, key);
+        const int rank = __popc(grp & ((1u << lane) - 1u));
+        const int nph = (int)__reduce_max_sync(kFull, (uint32_t)rank) + 1;
+        for (int ph = 0; ph < nph; ph++) {
+            if (rank == ph && vm) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if ((vm >> k) & 1u) T::add(tile, t0 + k, w[k], ux, uy, uz);
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // One warp per (brick, z-slab): the padded brick's layers are split into
 // slabs of a.slab_layers layers, each with its own shared tile, so a warp's
 // tile is a fraction of the brick and more warps stay resident.  Every slab
 // sees the same candidate points in the same order, so a voxel's sum does not
 // depend on the split.  splat_unit processes work unit u = slot * slabs + slab.
-template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
 __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u, unsigned char* tile, uint64_t* bar,
-                                           int* s_rs_w, int* s_ro_w, const uint16_t* s_magic, uint32_t& phase,
+                                           int* s_rs_w, int* s_ro_w, uint32_t& phase,
                                            const int lane)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
@@ -236,12 +438,17 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
 
     // ---- candidates, 32 at a time, in sorted order.  Each lane tests one
     // candidate and sizes the cells of its footprint in the slab (a cell = up
-    // to 4 consecutive x voxels of one (y, z) row); the cells of all hits are
-    // then dealt to the lanes 32 at a time.  Lanes whose cells share a row
-    // apply their updates one after another in lane order, which is the
-    // points' sorted order, so every voxel sums its contributions in the same
-    // order in every brick that holds it.
-    for (int base = 0; base < total; base += 32) {
+    // to 4 consecutive x voxels of one (y, z) row).  Most candidates miss the
+    // slab, so the hits are first gathered, in order, into a batch of up to 32
+    // points (lane i holds the i-th); a batch that the next round's hits would
+    // overflow, and the last one, has its cells dealt (deal_cells).  Batches
+    // are dealt in order, so the order of every voxel's sum is the points'
+    // sorted order.
+    float4 bp = make_float4(0.f, 0.f, 0.f, 0.f), buv = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t bb0 = 0u, bb1 = 0u;
+    int bnc = 0, nb = 0;  // this lane's cell count; points in the batch (warp-uniform)
+    for (int base = 0;; base += 32) {
+        const bool done = base >= total;  // one more pass deals the last batch
         const int v = base + lane;
         int idx = -1;
         if (v < total) {
@@ -256,7 +463,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             idx = s_rs_w[lo] + (v - s_ro_w[lo]);
         }
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f), uv = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t box0 = 0u, box1 = 0u, magic = 0u;  // footprint in slab-tile coordinates, 8 bits a bound
+        uint32_t box0 = 0u, box1 = 0u;  // footprint in slab-tile coordinates, 8 bits a bound
         int ncell = 0;
         if (idx >= 0) {
             p = a.spos[idx];
@@ -280,127 +487,50 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
                 ncell = nch * ny * (zh - zl + 1);
                 box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
                 box1 = (uint32_t)zl | ((uint32_t)zh << 8);
-                // ceil(2^15 / n) from the table: (c * magic) >> 15 == c / n for c < 2^15 / n
-                // (a footprint has at most 3 chunks x 14 rows x 14 layers of cells here)
-                magic = (uint32_t)s_magic[nch] | ((uint32_t)s_magic[ny] << 16);
             }
         }
-        // inclusive scan of the cell counts over the lanes
-        int cend = ncell;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(kFull, cend, o);
-            if (lane >= o) cend += t;
+        const uint32_t hm = __ballot_sync(kFull, ncell > 0);
+        const int h = __popc(hm);
+        if (done ? nb > 0 : nb + h > 32) {
+            deal_cells<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(tile, bp, buv, bb0, bb1, bnc, P, Ox, Oy, Zlo, R0, h0, inv_h0,
+                                                    norm0, r2h0, r2l0, lane);
+            bnc = 0;
+            nb = 0;
         }
-        const int ctot = __shfl_sync(kFull, cend, 31);
-        const int cstart = cend - ncell;
-        for (int g0 = 0; g0 < ctot; g0 += 32) {
-            const int g = g0 + lane;
-            const bool act = g < ctot;
-            // the point dealing this cell: the first lane whose cells end after g
+        if (done) break;
+        if (h == 0) continue;
+        // lane nb + i takes the i-th hit of this round: the lane of the (i+1)-th set bit of hm
+        const int d = lane - nb;
+        const bool take = d >= 0 && d < h;
+        int src = lane;
+        if (take) {
             int lo = 0, hi = 31;
 #pragma unroll
             for (int it = 0; it < 5; it++) {
                 const int mid = (lo + hi) >> 1;
-                if (__shfl_sync(kFull, cend, mid) > g)
+                if (__popc(hm & (kFull >> (31 - mid))) > d)
                     hi = mid;
                 else
                     lo = mid + 1;
             }
-            const int j = lo;
-            const float px = __shfl_sync(kFull, p.x, j), py = __shfl_sync(kFull, p.y, j);
-            const float pz = __shfl_sync(kFull, p.z, j), pw = __shfl_sync(kFull, p.w, j);
-            float ux = 0.f, uy = 0.f, uz = 0.f;
-            if (HAS_VEL) {
-                ux = __shfl_sync(kFull, uv.x, j);
-                uy = __shfl_sync(kFull, uv.y, j);
-                uz = __shfl_sync(kFull, uv.z, j);
-            }
-            const uint32_t b0 = __shfl_sync(kFull, box0, j), b1 = __shfl_sync(kFull, box1, j);
-            const uint32_t mg = __shfl_sync(kFull, magic, j);
-            const int cell = g - __shfl_sync(kFull, cstart, j);
-            const float pR = PPR ? __shfl_sync(kFull, uv.w, j) : 0.0f;
-            const int xl = (int)(b0 & 255u), xh = (int)((b0 >> 8) & 255u), yl = (int)((b0 >> 16) & 255u);
-            const int zl = (int)(b1 & 255u);
-            const int nch = (xh - xl + 4) >> 2, ny = (int)(b0 >> 24) - yl + 1;
-            const int r = (int)(((uint32_t)cell * (mg & 0xFFFFu)) >> 15);
-            const int zz = (int)(((uint32_t)r * (mg >> 16)) >> 15);
-            const int lx = xl + 4 * (cell - r * nch), ly = yl + (r - zz * ny), lz = zl + zz;
-            // the lane's voxels lx .. min(lx + 3, xh) of row (ly, lz): values, and a bit per voxel touched
-            float w[4] = {0.f, 0.f, 0.f, 0.f};
-            uint32_t vm = 0u;
-            const int t0 = (lz * P + ly) * P + lx;
-            if (act) {
-                if (!CUBIC) {
-                    const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
-                    const float fx = px - fx0, fy = py - fy0, fz = pz - fz0;
-                    const float wyz = ((float)(ly + Oy) == fy0 ? 1.f - fy : fy) * ((float)(lz + Zlo) == fz0 ? 1.f - fz : fz);
-                    const float wxa = (float)(lx + Ox) == fx0 ? 1.f - fx : fx;
-                    w[0] = pw * wxa * wyz;
-                    vm = 1u;
-                    if (lx + 1 <= xh) {
-                        w[1] = pw * fx * wyz;  // lx + 1 is floor(px) + 1 here
-                        vm |= 2u;
-                    }
-                } else {
-                    // M4 cubic spline (Monaghan & Lattanzio 1985), 3D normalisation 1/(pi h^3),
-                    // support R = 2h.  Along the row R^2 - d^2 is formed from an error-free
-                    // c = R^2 - dy^2 - dz^2 (two-product, two-sum) so that the outer branch
-                    // 0.25 (2-q)^3 = 0.25 ((R^2-d^2) / (h (R+d)))^3 keeps FP32 relative
-                    // accuracy up to the edge of the support.
-                    float R = R0, h = h0, inv_h = inv_h0, norm = norm0, r2h = r2h0, r2l = r2l0;
-                    if (PPR) {
-                        R = pR;
-                        h = 0.5f * R;
-                        inv_h = 1.0f / h;
-                        norm = kInvPi * inv_h * inv_h * inv_h;
-                        r2h = R * R;
-                        r2l = fmaf(R, R, -r2h);
-                    }
-                    norm *= pw;
-                    const float dy = (float)(ly + Oy) - py, dz = (float)(lz + Zlo) - pz;
-                    const float qy = dy * dy, ey = fmaf(dy, dy, -qy);
-                    const float qz = dz * dz, ez = fmaf(dz, dz, -qz);
-                    const float syz = qy + qz;
-                    float bv = syz - qy;
-                    const float e1 = (qy - (syz - bv)) + (qz - bv);
-                    const float c1 = r2h - syz;
-                    bv = c1 - r2h;
-                    const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
-                    const float cl = e2 + r2l - ((ey + ez) + e1);
-                    if (c1 + cl > 0.0f) {
-#pragma unroll
-                        for (int k = 0; k < 4; k++) {
-                            if (lx + k > xh) break;
-                            const float dx = (float)(lx + k + Ox) - px;
-                            const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
-                            if (t <= 0.0f) continue;
-                            const float d2 = fmaf(dx, dx, syz);
-                            const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                            const float q = d * inv_h;
-                            const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
-                            const float uu = __fdividef(t, h * (R + d));               // 2 - q
-                            w[k] = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
-                            vm |= 1u << k;
-                        }
-                    }
-                }
-            }
-            // lanes sharing a row apply in lane order (the cells of one point lie in distinct rows
-            // or distinct chunks of a row); rows apart apply together
-            const int key = act ? (lz * P + ly) : -1 - lane;
-            const uint32_t grp = __match_any_sync(kFull, key);
-            const int rank = __popc(grp & ((1u << lane) - 1u));
-            const int nph = (int)__reduce_max_sync(kFull, (uint32_t)rank) + 1;
-            for (int ph = 0; ph < nph; ph++) {
-                if (rank == ph && vm) {
-#pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        if ((vm >> k) & 1u) T::add(tile, t0 + k, w[k], ux, uy, uz);
-                }
-                __syncwarp();
-            }
+            src = lo;
         }
+        const float4 np = make_float4(__shfl_sync(kFull, p.x, src), __shfl_sync(kFull, p.y, src),
+                                      __shfl_sync(kFull, p.z, src), __shfl_sync(kFull, p.w, src));
+        float4 nuv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (HAS_VEL || PPR)
+            nuv = make_float4(__shfl_sync(kFull, uv.x, src), __shfl_sync(kFull, uv.y, src),
+                              __shfl_sync(kFull, uv.z, src), __shfl_sync(kFull, uv.w, src));
+        const uint32_t n0 = __shfl_sync(kFull, box0, src), n1 = __shfl_sync(kFull, box1, src);
+        const int nn = __shfl_sync(kFull, ncell, src);
+        if (take) {
+            bp = np;
+            buv = nuv;
+            bb0 = n0;
+            bb1 = n1;
+            bnc = nn;
+        }
+        nb += h;
     }
 
     // ---- apron voxels with no neighbouring brick take the boundary value (0):
@@ -448,7 +578,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     }
 }
 
-template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
 __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(SplatArgs a)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
@@ -458,8 +588,6 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
     __shared__ int s_rs[kSlabWarps][28];
     __shared__ int s_ro[kSlabWarps][28];
-    __shared__ uint16_t s_magic[32];
-    if (threadIdx.x < 32) s_magic[threadIdx.x] = (uint16_t)(threadIdx.x ? (32767u + threadIdx.x) / threadIdx.x : 0u);
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
@@ -469,15 +597,14 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     const uint32_t units = a.nslots * (uint32_t)a.slabs;
     const uint32_t nw = gridDim.x * kSlabWarps;
     for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw)
-        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], s_magic, phase,
-                                                lane);
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], phase, lane);
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
 
 // The same work over many grids in one persistent launch: the units of grid
 // k are [ustart[k], ustart[k+1]) of one global range, dealt to the warps in
 // stride; every grid has the same brick and tile shape (slab_layers, P).
-template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR>
+template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
 __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     k_splat_batch(const SplatArgs* __restrict__ args, const uint32_t* __restrict__ ustart, int ngrids)
 {
@@ -489,9 +616,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     __shared__ int s_rs[kSlabWarps][28];
     __shared__ int s_ro[kSlabWarps][28];
     __shared__ uint32_t s_us[kBatchMaxGrids + 1];
-    __shared__ uint16_t s_magic[32];
     for (int i = threadIdx.x; i <= ngrids; i += blockDim.x) s_us[i] = ustart[i];
-    if (threadIdx.x < 32) s_magic[threadIdx.x] = (uint16_t)(threadIdx.x ? (32767u + threadIdx.x) / threadIdx.x : 0u);
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
@@ -509,8 +634,8 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
             else
                 hi = mid - 1;
         }
-        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid], s_ro[wid],
-                                                s_magic, phase, lane);
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid], s_ro[wid],
+                                                phase, lane);
     }
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
@@ -691,9 +816,10 @@ static int sm_count(int device)
 struct SplatKind {
     bool has_d, has_v, ppr;
     int mode;
+    bool small;  // footprint within 4 voxels a side: trilinear, or cubic of a uniform radius <= 2
     bool operator==(const SplatKind& o) const
     {
-        return has_d == o.has_d && has_v == o.has_v && ppr == o.ppr && mode == o.mode;
+        return has_d == o.has_d && has_v == o.has_v && ppr == o.ppr && mode == o.mode && small == o.small;
     }
 };
 
@@ -701,11 +827,16 @@ template <bool D, bool V>
 static void* pick_kernel(const SplatKind& k, bool batch)
 {
     if (k.mode == GVX_SPLAT_TRILINEAR)
-        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_TRILINEAR, false>
-                     : (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR, false>;
+        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_TRILINEAR, false, true>
+                     : (void*)k_splat_slab<D, V, GVX_SPLAT_TRILINEAR, false, true>;
     if (k.ppr)
-        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, true> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, true>;
-    return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, false> : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false>;
+        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, true, false>
+                     : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, true, false>;
+    if (k.small)
+        return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, false, true>
+                     : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false, true>;
+    return batch ? (void*)k_splat_batch<D, V, GVX_SPLAT_CUBIC, false, false>
+                 : (void*)k_splat_slab<D, V, GVX_SPLAT_CUBIC, false, false>;
 }
 
 static void* splat_kernel(const SplatKind& k, bool batch)
@@ -798,6 +929,7 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
     kind->has_v = has_v;
     kind->ppr = ppr;
     kind->mode = mode;
+    kind->small = mode == GVX_SPLAT_TRILINEAR || (!ppr && radius <= 2.0f);
     return GVX_OK;
 }
 
@@ -893,8 +1025,8 @@ static std::string tune_key(int device, const SplatArgs& a, const SplatKind& k)
     memset(&prop, 0, sizeof(prop));
     cudaGetDeviceProperties(&prop, device);
     char buf[512];
-    snprintf(buf, sizeof(buf), "%s|%d|P%d|m%d|d%d|v%d|r%d", prop.name, device, a.P, k.mode, (int)k.has_d,
-             (int)k.has_v, (int)k.ppr);
+    snprintf(buf, sizeof(buf), "%s|%d|P%d|m%d|d%d|v%d|r%d|s%d", prop.name, device, a.P, k.mode, (int)k.has_d,
+             (int)k.has_v, (int)k.ppr, (int)k.small);
     return buf;
 }
 
