@@ -169,6 +169,7 @@ gvx_status gvx_destroy(gvx_grid* g)
     cudaSetDevice(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
     DevBuf* bufs[] = {&g->bm_a, &g->bm_a_prefix, &g->bm_b, &g->bm_b_prefix, &g->remap, &g->leaf_key, &g->leaf_range,
+                      &g->leaf_oct,
                       &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos, &g->own_vel, &g->own_w,
                       &g->own_r, &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,

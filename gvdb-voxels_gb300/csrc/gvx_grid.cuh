@@ -90,6 +90,9 @@ struct gvx_grid {
     // per-leaf data
     DevBuf leaf_key;     // compact level-0 key per leaf (pool order)
     DevBuf leaf_range;   // int2 [start, end) in the sorted point order
+    DevBuf leaf_oct;     // 8 ints per leaf: first sorted index of each octant of the leaf's points
+    bool oct_valid = false;  // the sorted points are in octant order inside every leaf, leaf_oct filled
+    uint32_t oct_leaves = 0;
     DevBuf leaf_slot;    // atlas slot per leaf, -1 if inactive
     DevBuf slot_leaf;    // leaf per atlas slot (active slots only)
     DevBuf nbr;          // 27 leaf indices per leaf
@@ -115,6 +118,7 @@ struct gvx_grid {
     DevBuf keys[2], vals[2];
     int sorted_buf = 0;
     uint32_t n_sorted = 0;
+    float sort_trans[3] = {0, 0, 0};  // translation of the positions the sorted keys were made from
     bool group_valid = false;
     float group_trans[3] = {0, 0, 0};
     const void* group_pos = nullptr;
@@ -168,6 +172,7 @@ void gvx_host_tree_free(gvx_grid* g);
 gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
                            const uint64_t* const* clists);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
+gvx_status gvx_topo_octants(gvx_grid* g);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
 // InsertPoints: grouping + sorted attribute arrays

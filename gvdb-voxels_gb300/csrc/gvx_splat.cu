@@ -37,6 +37,7 @@ constexpr int kSlabWarps = 4;        // warps (brick slabs) per block of the spl
 constexpr int kSlabMinBlocks = 6;    // resident blocks per SM the register budget is sized for
 constexpr size_t kSlabTileMax = 48 * 1024;  // shared tile bytes of one warp at most
 constexpr int kBatchMaxGrids = 256;         // grids of one batched launch
+constexpr int kMaxRanges = 27 * 4;          // candidate ranges of a slab: at most 4 octant runs per neighbour
 constexpr float kInvPi = 0.318309886183790671538f;
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 }  // namespace
@@ -98,6 +99,7 @@ struct SplatArgs {
     const GvxNode* nodes0;
     const int* nbr;
     const int2* leaf_range;
+    const int* leaf_oct;  // 8 per leaf: first sorted index of each octant of its points
     const float4* spos;
     const float4* svel;  // nullptr when no velocity and no per-point radius
     bool per_point_radius;
@@ -375,39 +377,96 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
     const int Zlo = Oz + z0, Zhi = Oz + z0 + nl - 1;                          // world z of the slab
 
-    // ---- the 27 neighbour ranges that can reach the slab, ordered by their place in the sorted points
-    int2 rg = make_int2(0, 0);
+    // ---- candidate ranges: the octants of the 27 neighbours (the brick itself included) whose
+    // points can reach the slab, in the sorted order of the points -- neighbours by key, i.e. by
+    // (dx, dy, dz), and inside a brick by octant 4 hx + 2 hy + hz.  Lane r < 27 takes the
+    // neighbour (dx, dy, dz) = (r / 9, r / 3 % 3, r % 3) - 1.  Along each axis a half of a brick
+    // (floor coordinates [c, c + b/2)) is read when its points, whose footprints reach `reach`
+    // voxels from their own, can touch the slab's padded extent.  A lane's octants are merged
+    // into runs of adjacent octants: at most 4 ranges a lane.
     bool has_nb = false;
+    uint32_t need = 0u;  // octants to read
+    int oc[9];           // first index of each octant, and the end of the brick's points
+#pragma unroll
+    for (int o = 0; o < 9; o++) oc[o] = 0;
     if (lane < 27) {
-        const int nl_ = a.nbr[(size_t)leaf * 27 + lane];
+        const int dx = lane / 9 - 1, dy = (lane / 3) % 3 - 1, dz = lane % 3 - 1;
+        const int nl_ = a.nbr[(size_t)leaf * 27 + (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
         if (nl_ >= 0) {
             has_nb = a.leaf_slot[nl_] >= 0;
-            const int bz = nd->pos[2] + (lane / 9 - 1) * b;  // the neighbour's world z range [bz, bz + b)
-            if (bz - a.reach <= Zhi && bz + b - 1 + a.reach >= Zlo) rg = a.leaf_range[nl_];
+            const int hb = b >> 1;
+            const int cx = nd->pos[0] + dx * b, cy = nd->pos[1] + dy * b, cz = nd->pos[2] + dz * b;
+            uint32_t mx = 0u, my = 0u, mz = 0u;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int x0 = cx + h * hb, y0 = cy + h * hb, z0h = cz + h * hb;
+                mx |= (uint32_t)(x0 - a.reach <= Ox + P - 1 && x0 + hb - 1 + a.reach >= Ox) << h;
+                my |= (uint32_t)(y0 - a.reach <= Oy + P - 1 && y0 + hb - 1 + a.reach >= Oy) << h;
+                mz |= (uint32_t)(z0h - a.reach <= Zhi && z0h + hb - 1 + a.reach >= Zlo) << h;
+            }
+#pragma unroll
+            for (int o = 0; o < 8; o++) need |= ((mx >> (o >> 2)) & (my >> ((o >> 1) & 1)) & (mz >> (o & 1)) & 1u) << o;
+            if (need) {
+                const int4* q = (const int4*)(a.leaf_oct + (size_t)nl_ * 8);
+                const int4 q0 = q[0], q1 = q[1];
+                oc[0] = q0.x, oc[1] = q0.y, oc[2] = q0.z, oc[3] = q0.w;
+                oc[4] = q1.x, oc[5] = q1.y, oc[6] = q1.z, oc[7] = q1.w;
+                oc[8] = a.leaf_range[nl_].y;
+            }
         }
     }
-    const uint32_t nbmask = __ballot_sync(kFull, has_nb);
-    const int len = max(0, rg.y - rg.x);
-    // Points are sorted by their brick's key, which orders bricks by (x, y, z),
-    // so the ranges lie in the order of the neighbours' (dx, dy, dz): lane t
-    // takes the t-th neighbour in that order, and a scan gives the offsets.
-    const int src = (lane % 3) * 9 + ((lane / 3) % 3) * 3 + lane / 9;  // nbr-table lane of (dx, dy, dz)
-    const int rs = __shfl_sync(kFull, rg.x, src);
-    const int rl_all = __shfl_sync(kFull, len, src);  // every lane takes part in the shuffle
-    const int rl = lane < 27 ? rl_all : 0;
-    int incl = rl;
+    const uint32_t nbmask = __ballot_sync(kFull, has_nb);  // bit r: neighbour r (key order) is active
+    // runs of needed octants: their count and points
+    int nr = 0, len = 0;
+    {
+        bool in = false;
+        int rs0 = 0;
+#pragma unroll
+        for (int o = 0; o <= 8; o++) {
+            const bool nd_o = o < 8 && ((need >> o) & 1u);
+            if (nd_o && !in) {
+                rs0 = oc[o];
+                in = true;
+            } else if (!nd_o && in) {
+                if (oc[o] > rs0) {
+                    nr++;
+                    len += oc[o] - rs0;
+                }
+                in = false;
+            }
+        }
+    }
+    int incl = len, rincl = nr;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
+        const int t = __shfl_up_sync(kFull, incl, o), u = __shfl_up_sync(kFull, rincl, o);
+        if (lane >= o) {
+            incl += t;
+            rincl += u;
+        }
     }
     const int total = __shfl_sync(kFull, incl, 31);
-    const uint32_t ne = __ballot_sync(kFull, rl > 0);
-    const int m = __popc(ne);
-    if (rl > 0) {
-        const int rank = __popc(ne & ((1u << lane) - 1u));
-        s_rs_w[rank] = rs;
-        s_ro_w[rank] = incl - rl;
+    const int m = __shfl_sync(kFull, rincl, 31);
+    {
+        int rank = rincl - nr, off = incl - len;
+        bool in = false;
+        int rs0 = 0;
+#pragma unroll
+        for (int o = 0; o <= 8; o++) {
+            const bool nd_o = o < 8 && ((need >> o) & 1u);
+            if (nd_o && !in) {
+                rs0 = oc[o];
+                in = true;
+            } else if (!nd_o && in) {
+                if (oc[o] > rs0) {
+                    s_rs_w[rank] = rs0;
+                    s_ro_w[rank] = off;
+                    rank++;
+                    off += oc[o] - rs0;
+                }
+                in = false;
+            }
+        }
     }
     if (lane == 0) s_ro_w[m] = total;
 
@@ -539,7 +598,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
 #pragma unroll 1
         for (int k = 0; k < 27; k++) {
             if (k == 13 || ((nbmask >> k) & 1u)) continue;
-            const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+            const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
             const int xb = dx < 0 ? 0 : (dx > 0 ? P - 1 : 1), yb = dy < 0 ? 0 : (dy > 0 ? P - 1 : 1);
             const int bx = dx == 0 ? a.lb : 0, by = dy == 0 ? a.lb : 0;  // log2 of the region's x, y extents
             const int zlo = max(dz < 0 ? 0 : (dz > 0 ? P - 1 : 1), z0);
@@ -586,8 +645,8 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned char* tile = smem + (size_t)wid * T::bytes(a.slab_layers * a.P * a.P);
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
-    __shared__ int s_rs[kSlabWarps][28];
-    __shared__ int s_ro[kSlabWarps][28];
+    __shared__ int s_rs[kSlabWarps][kMaxRanges + 1];
+    __shared__ int s_ro[kSlabWarps][kMaxRanges + 1];
     if (lane == 0) {
         mbar_init(&s_bar[wid], 1);
         mbar_fence_init();
@@ -613,8 +672,8 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned char* tile = smem + (size_t)wid * T::bytes(args[0].slab_layers * args[0].P * args[0].P);
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
-    __shared__ int s_rs[kSlabWarps][28];
-    __shared__ int s_ro[kSlabWarps][28];
+    __shared__ int s_rs[kSlabWarps][kMaxRanges + 1];
+    __shared__ int s_ro[kSlabWarps][kMaxRanges + 1];
     __shared__ uint32_t s_us[kBatchMaxGrids + 1];
     for (int i = threadIdx.x; i <= ngrids; i += blockDim.x) s_us[i] = ustart[i];
     if (lane == 0) {
@@ -769,6 +828,8 @@ gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool nee
     const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
     gvx_status rc = gvx_topo_group_points(g, n, t);
     if (rc) return rc;
+    rc = gvx_topo_octants(g);
+    if (rc) return rc;
     if (g->perm_valid && (g->perm_has_svel || !need_svel) && g->perm_vel == g->pts.vel &&
         g->perm_w == g->pts.weight && g->perm_r == g->pts.radius)
         return GVX_OK;
@@ -910,6 +971,7 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
     a.nodes0 = g->nodes[0].as<GvxNode>();
     a.nbr = g->nbr.as<int>();
     a.leaf_range = g->leaf_range.as<int2>();
+    a.leaf_oct = g->leaf_oct.as<int>();
     a.spos = g->spos.as<float4>();
     a.svel = need_svel ? g->svel.as<float4>() : nullptr;
     a.per_point_radius = ppr;

@@ -540,6 +540,79 @@ __global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uin
     if (last) leaf_range[leaf].y = (int)(i + 1);
 }
 
+// Points of every leaf in octant order: a stable partition of the leaf's range
+// of sorted point indices by the half of the brick that each point's voxel
+// (floor of the translated position, as the keys take it) lies in on every
+// axis, octant = 4 hx + 2 hy + hz, and the first index of every octant.  The
+// sorted order becomes (leaf key, octant, point index); the splat reads only
+// the octants of a neighbouring brick whose points can reach its slab.  One
+// warp per leaf; lanes 0-7 keep the octants' counters.
+__global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t nleaves,
+                                   const GvxNode* __restrict__ nodes0, const char* pos, int off, int stride, float ox,
+                                   float oy, float oz, int half, const uint32_t* __restrict__ vin,
+                                   uint32_t* __restrict__ vout, int* __restrict__ leaf_oct)
+{
+    const uint32_t leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (leaf >= nleaves) return;  // whole warps
+    const int2 r = leaf_range[leaf];
+    const int bx = nodes0[leaf].pos[0] + half, by = nodes0[leaf].pos[1] + half, bz = nodes0[leaf].pos[2] + half;
+    auto octant = [&](uint32_t v) {
+        float w[3];
+        load_pos(pos, off, stride, v, w);
+        const int x = (int)floorf(w[0] + ox), y = (int)floorf(w[1] + oy), z = (int)floorf(w[2] + oz);
+        return (x >= bx ? 4 : 0) | (y >= by ? 2 : 0) | (z >= bz ? 1 : 0);
+    };
+    int cnt = 0;  // lane o < 8: points of octant o
+    uint32_t v0 = 0u;  // the first 32 points and their octants, kept for the placement pass
+    int o0 = -1;
+    for (int b = r.x; b < r.y; b += 32) {
+        const int i = b + lane;
+        uint32_t v = 0u;
+        int o = -1;
+        if (i < r.y) {
+            v = vin[i];
+            o = octant(v);
+        }
+        if (b == r.x) {
+            v0 = v;
+            o0 = o;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k);
+            if (lane == k) cnt += __popc(m);
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int s = 1; s < 8; s <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, s);
+        if (lane >= s) incl += t;
+    }
+    int run = r.x + incl - cnt;  // lane o < 8: next index of octant o
+    if (lane < 8) leaf_oct[(size_t)leaf * 8 + lane] = run;
+    for (int b = r.x; b < r.y; b += 32) {
+        const int i = b + lane;
+        uint32_t v = v0;
+        int o = o0;
+        if (b != r.x && i < r.y) {
+            v = vin[i];
+            o = octant(v);
+        } else if (b != r.x) {
+            o = -1;
+        }
+        const uint32_t same = __match_any_sync(0xFFFFFFFFu, o);
+        const int dst = __shfl_sync(0xFFFFFFFFu, run, o < 0 ? 0 : o) + __popc(same & ((1u << lane) - 1u));
+        if (o >= 0) vout[dst] = v;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k);
+            if (lane == k) run += __popc(m);
+        }
+    }
+}
+
 // 27-neighbourhood of every leaf (leaf pool indices, -1 where no leaf; all -1
 // for an inactive leaf, whose key is kNoKey)
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;
@@ -906,21 +979,52 @@ static gvx_status sort_points(gvx_grid* g, int n, const float t[3], const KeySpa
     if (rc) return rc;
     g->sorted_buf = res;
     g->n_sorted = (uint32_t)n;
+    for (int a = 0; a < 3; a++) g->sort_trans[a] = t[a];
     g->perm_valid = false;
+    g->oct_valid = false;
     return GVX_OK;
 }
 
 static gvx_status fill_leaf_ranges(gvx_grid* g, uint32_t nleaves)
 {
     GVX_CK(gvx_ensure(g->leaf_range, (size_t)(nleaves + 1) * sizeof(int2)));
+    GVX_CK(gvx_ensure(g->leaf_oct, (size_t)(nleaves + 1) * 8 * sizeof(int)));
     GVX_CK(cudaMemsetAsync(g->leaf_range.p, 0, (size_t)(nleaves + 1) * sizeof(int2), g->stream));
+    GVX_CK(cudaMemsetAsync(g->leaf_oct.p, 0, (size_t)(nleaves + 1) * 8 * sizeof(int), g->stream));
     if (g->n_sorted) {
         k_group_runs<<<blocks_for(g->n_sorted, 256), 256, 0, g->stream>>>(
             g->keys[g->sorted_buf].as<uint32_t>(), g->n_sorted, 1u << g->lookup.ks.total_bits, g->lookup,
             g->leaf_range.as<int2>());
         g->launches++;
     }
+    g->oct_leaves = nleaves;
+    g->oct_valid = false;
     GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}
+
+// Octant order inside every leaf (k_octant_partition), once per grouping, for
+// the splats: partition into the other value buffer (a copy of the sorted
+// values, so entries outside the leaf ranges keep theirs), then copy back.
+gvx_status gvx_topo_octants(gvx_grid* g)
+{
+    if (g->oct_valid) return GVX_OK;
+    const uint32_t nleaves = g->oct_leaves;
+    if (g->n_sorted && nleaves) {
+        uint32_t* vin = g->vals[g->sorted_buf].as<uint32_t>();
+        uint32_t* vtmp = g->vals[1 - g->sorted_buf].as<uint32_t>();
+        const size_t vb = (size_t)g->n_sorted * sizeof(uint32_t);
+        GVX_CK(cudaMemcpyAsync(vtmp, vin, vb, cudaMemcpyDeviceToDevice, g->stream));
+        k_octant_partition<<<blocks_for((uint64_t)nleaves * 32u, 256), 256, 0, g->stream>>>(
+            g->leaf_range.as<int2>(), nleaves, g->nodes[0].as<GvxNode>(), g->pts.pos, g->pts.pos_off,
+            g->pts.pos_stride, g->sort_trans[0], g->sort_trans[1], g->sort_trans[2], g->brick / 2, vin, vtmp,
+            g->leaf_oct.as<int>());
+        g->launches++;
+        GVX_CK(cudaMemcpyAsync(vin, vtmp, vb, cudaMemcpyDeviceToDevice, g->stream));
+        GVX_CK(cudaGetLastError());
+    }
+    g->oct_valid = true;
+    g->perm_valid = false;  // the sorted attributes follow the new order
     return GVX_OK;
 }
 
