@@ -135,6 +135,7 @@ struct gvx_grid {
     DevBuf d0_bits, d0_prefix, x0_bits, x0_prefix, masks, upper, lists, tmp_scan, d_counts;
     DevBuf inc0, inc_remap;  // incremental build: linked + new level-0 bitmaps, linked rank -> pool index
     DevBuf d_err, d_bbox;
+    DevBuf d_rmax;  // float bits of the largest per-point radius of the last point permute
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index

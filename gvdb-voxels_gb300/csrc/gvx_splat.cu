@@ -68,13 +68,20 @@ __device__ __forceinline__ void apron_voxel_coords(int e, int P, int& x, int& y,
     }
 }
 
-// sorted point attributes: (x, y, z, weight) and (vx, vy, vz, radius)
+// sorted point attributes: (x, y, z, weight) and (vx, vy, vz, radius); with
+// per-point radii also the largest radius (float bits, NaN counted as huge)
 __global__ void k_permute(const uint32_t* __restrict__ svals, uint32_t n, const char* pos, int poff, int pstride,
                           const char* vel, int voff, int vstride, const float* __restrict__ weight,
                           const float* __restrict__ radius, float tx, float ty, float tz, float4* spos,
-                          float4* svel)
+                          float4* svel, unsigned int* rmax)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (radius && rmax) {
+        float r = i < n ? radius[svals[i]] : 0.0f;
+        r = r != r ? 3.0e38f : fmaxf(r, 0.0f);
+        const unsigned int m = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(r));
+        if ((threadIdx.x & 31) == 0 && m) atomicMax(rmax, m);
+    }
     if (i >= n) return;
     const uint32_t j = svals[i];
     const float* p = (const float*)(pos + (size_t)j * pstride + poff);
@@ -108,7 +115,8 @@ struct SplatArgs {
     float4* vel;         // or nullptr
     int slabs, slab_layers;  // z-slabs per padded brick, layers per slab
     int lb;              // log2(brick)
-    int reach;           // voxels a point's footprint reaches beyond its brick (neighbour pruning)
+    int reach;           // voxels a point's footprint reaches beyond its own voxel (neighbour pruning)
+    const unsigned int* rmax;  // per-point radii: float bits of the largest (bounds `reach` on the device)
     float max_radius;    // per-point radii above this reach past the 26 neighbours
     bool accum;
     float boundval;
@@ -384,6 +392,8 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     // (floor coordinates [c, c + b/2)) is read when its points, whose footprints reach `reach`
     // voxels from their own, can touch the slab's padded extent.  A lane's octants are merged
     // into runs of adjacent octants: at most 4 ranges a lane.
+    // with per-point radii the reach is that of the largest radius (ceil R voxels, at most brick - 1)
+    const int reach = PPR && a.rmax ? min(a.reach, (int)ceilf(__uint_as_float(*a.rmax))) : a.reach;
     bool has_nb = false;
     uint32_t need = 0u;  // octants to read
     int oc[9];           // first index of each octant, and the end of the brick's points
@@ -400,9 +410,9 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int x0 = cx + h * hb, y0 = cy + h * hb, z0h = cz + h * hb;
-                mx |= (uint32_t)(x0 - a.reach <= Ox + P - 1 && x0 + hb - 1 + a.reach >= Ox) << h;
-                my |= (uint32_t)(y0 - a.reach <= Oy + P - 1 && y0 + hb - 1 + a.reach >= Oy) << h;
-                mz |= (uint32_t)(z0h - a.reach <= Zhi && z0h + hb - 1 + a.reach >= Zlo) << h;
+                mx |= (uint32_t)(x0 - reach <= Ox + P - 1 && x0 + hb - 1 + reach >= Ox) << h;
+                my |= (uint32_t)(y0 - reach <= Oy + P - 1 && y0 + hb - 1 + reach >= Oy) << h;
+                mz |= (uint32_t)(z0h - reach <= Zhi && z0h + hb - 1 + reach >= Zlo) << h;
             }
 #pragma unroll
             for (int o = 0; o < 8; o++) need |= ((mx >> (o >> 2)) & (my >> ((o >> 1) & 1)) & (mz >> (o & 1)) & 1u) << o;
@@ -838,10 +848,16 @@ gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool nee
     GVX_CK(gvx_ensure(g->spos, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
     if (need_svel) GVX_CK(gvx_ensure(g->svel, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
     if (m) {
+        unsigned int* rmax = nullptr;
+        if (g->pts.radius && need_svel) {
+            GVX_CK(gvx_ensure(g->d_rmax, sizeof(unsigned int)));
+            GVX_CK(cudaMemsetAsync(g->d_rmax.p, 0, sizeof(unsigned int), g->stream));
+            rmax = g->d_rmax.as<unsigned int>();
+        }
         k_permute<<<blocks_for(m, 256), 256, 0, g->stream>>>(
             g->vals[g->sorted_buf].as<uint32_t>(), m, g->pts.pos, g->pts.pos_off, g->pts.pos_stride, g->pts.vel,
             g->pts.vel_off, g->pts.vel_stride, g->pts.weight, g->pts.radius, t[0], t[1], t[2], g->spos.as<float4>(),
-            need_svel ? g->svel.as<float4>() : nullptr);
+            need_svel ? g->svel.as<float4>() : nullptr, rmax);
         g->launches++;
     }
     GVX_CK(cudaGetLastError());
@@ -984,6 +1000,7 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
     while ((1 << a.lb) < g->brick) a.lb++;
     a.max_radius = (float)(g->brick - 1);
     a.reach = mode == GVX_SPLAT_TRILINEAR ? 1 : (ppr ? g->brick - 1 : (int)ceilf(radius));
+    a.rmax = ppr && g->n_sorted ? g->d_rmax.as<unsigned int>() : nullptr;
     a.accum = accum != 0;
     a.boundval = 0.0f;
     a.err = g->d_err.as<uint32_t>();
