@@ -69,6 +69,11 @@ void VolumeGVDB::Configure(int levs, int* r, int* ncnt, bool use_masks)
     levels_ = levs;
     mirror_.assign(levs, std::vector<Node>());
     mirror_gen_.assign(levs, 0);
+    clmirror_.assign(levs, std::vector<uint64>());
+    clmirror_gen_.assign(levs, 0);
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    for (int l = 0; l < levs && l < GVX_MAX_LEVELS; l++) logdim_[l] = inf.logdim[l];
     topology_changed();
 }
 
@@ -130,6 +135,9 @@ bool VolumeGVDB::LoadVBX(const std::string fname, int force_maj, int force_min)
     apron_ = inf.apron;
     mirror_.assign(levels_, std::vector<Node>());
     mirror_gen_.assign(levels_, 0);
+    clmirror_.assign(levels_, std::vector<uint64>());
+    clmirror_gen_.assign(levels_, 0);
+    for (int l = 0; l < levels_ && l < GVX_MAX_LEVELS; l++) logdim_[l] = inf.logdim[l];
     for (int c = 0; c < 32; c++) check(gvx_channel_type(g_, c, &chan_type_[c]));
     topology_changed();
     return true;
@@ -514,6 +522,140 @@ Node* VolumeGVDB::getNode(slong nodeid)
 {
     const uint64 id = (uint64)nodeid;
     return getNode((int)(id & 0xFF), (int)((id >> 8) & 0xFF), (slong)(id >> 16));
+}
+
+// ---- host-side tree queries, on the pools and child lists read back on demand
+
+// child list `listid` = Elem(1, lev, ndx): entries [ndx * res^3, (ndx + 1) * res^3) of level lev's lists
+const uint64* VolumeGVDB::child_list(uint64 listid)
+{
+    if (listid == ID_UNDEFL || listid == ID_UNDEF64 || (listid & 0xFF) != 1) return nullptr;
+    const int lev = (int)((listid >> 8) & 0xFF);
+    if (lev < 1 || lev >= (int)clmirror_.size()) return nullptr;
+    const uint64 vc = (uint64)getRes(lev) * getRes(lev) * getRes(lev);
+    if (clmirror_gen_[lev] != gen_) {
+        const uint64 cnt = getNumTotalNodes(lev) * vc;
+        clmirror_[lev].resize((size_t)cnt);
+        if (cnt) check(gvx_read_childlist(g_, lev, clmirror_[lev].data(), (int64_t)cnt));
+        clmirror_gen_[lev] = gen_;
+    }
+    const uint64 at = (listid >> 16) * vc;
+    return at + vc <= clmirror_[lev].size() ? clmirror_[lev].data() + at : nullptr;
+}
+
+// getRange (VG.h:614-619): index-space extent of a level-lev node
+Vector3DI VolumeGVDB::getRange(int lev)
+{
+    int r = getRes(0);
+    for (int l = 1; l <= lev; l++) r *= getRes(l);
+    return Vector3DI(r, r, r);
+}
+
+uint64 VolumeGVDB::getRootNodeID()
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    if (inf.root_level < 0) return ID_UNDEF64;
+    return (uint64)inf.root_level << 8;  // Elem(0, root level, 0)
+}
+
+// getChildNode (VG.cpp:3079-3092), bitmasks off: entry b of the node's child list
+uint64 VolumeGVDB::getChildNode(slong nodeid, uint b)
+{
+    Node* curr = getNode(nodeid);
+    return curr ? getChildRefAtBit(curr, b) : ID_UNDEF64;
+}
+
+// getChildRefAtBit (VG.cpp:3066-3076)
+uint64 VolumeGVDB::getChildRefAtBit(Node* curr, uint b)
+{
+    const uint64* cl = curr ? child_list(curr->mChildList) : nullptr;
+    if (!cl || b >= (uint)(getRes(curr->mLev) * getRes(curr->mLev) * getRes(curr->mLev))) return ID_UNDEF64;
+    return cl[b];
+}
+
+// getChildAtBit (VG.cpp:3052-3064)
+Node* VolumeGVDB::getChildAtBit(Node* curr, uint b)
+{
+    const uint64 ch = getChildRefAtBit(curr, b);
+    return ch == ID_UNDEF64 ? nullptr : getNode((slong)ch);
+}
+
+// isOn (VG.cpp:2787-2796), bitmasks off
+bool VolumeGVDB::isOn(slong nodeid, uint32 b) { return getChildNode(nodeid, b) != ID_UNDEF64; }
+
+// getPosInNode (VG.cpp:2858-2875): integer position inside the node, and its child bit
+bool VolumeGVDB::getPosInNode(slong curr_id, Vector3DI pos, uint32& bit)
+{
+    bit = 0;
+    Node* curr = getNode(curr_id);
+    if (!curr) return false;
+    const int res = getRes(curr->mLev);
+    const Vector3DI range = getRange(curr->mLev);
+    int p[3] = {pos.x - curr->mPos.x, pos.y - curr->mPos.y, pos.z - curr->mPos.z};
+    const int rg[3] = {range.x, range.y, range.z};
+    for (int a = 0; a < 3; a++)
+        if (p[a] < 0 || p[a] >= rg[a]) return false;
+    for (int a = 0; a < 3; a++) p[a] = p[a] * res / rg[a];
+    bit = (uint32)getBitPos(curr->mLev, Vector3DI(p[0], p[1], p[2]));
+    return true;
+}
+
+// getNodeAtPoint (VG.cpp:4650-4684): the leaf holding an index-space position, by descent
+uint64 VolumeGVDB::getNodeAtPoint(uint64 nodeid, Vector3DF pos)
+{
+    Node* curr = getNode((slong)nodeid);
+    if (!curr) return ID_UNDEFL;
+    const Vector3DI range = getRange(curr->mLev);
+    float p[3] = {pos.x - (float)curr->mPos.x, pos.y - (float)curr->mPos.y, pos.z - (float)curr->mPos.z};
+    const float rg[3] = {(float)range.x, (float)range.y, (float)range.z};
+    if (!(p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && p[0] < rg[0] && p[1] < rg[1] && p[2] < rg[2])) return ID_UNDEFL;
+    const float res = (float)getRes(curr->mLev);
+    for (int a = 0; a < 3; a++) p[a] = p[a] * res / rg[a];
+    if (isLeaf((slong)nodeid)) return nodeid;
+    const uint32 i = (uint32)getBitPos(curr->mLev, Vector3DI((int)p[0], (int)p[1], (int)p[2]));
+    if (!isOn((slong)nodeid, i)) return ID_UNDEFL;
+    return getNodeAtPoint(getChildNode((slong)nodeid, i), pos);
+}
+
+// isActive (VG.cpp:4688-4711): is the integer position inside a leaf of the tree
+bool VolumeGVDB::isActive(Vector3DI wpos)
+{
+    const uint64 root = getRootNodeID();
+    return root != ID_UNDEF64 && isActive(wpos, (slong)root);
+}
+
+bool VolumeGVDB::isActive(Vector3DI pos, slong nodeid)
+{
+    uint32 b = 0;
+    if (!getPosInNode(nodeid, pos, b)) return false;
+    if (isLeaf(nodeid)) return true;
+    if (!isOn(nodeid, b)) return false;
+    return isActive(pos, (slong)getChildNode(nodeid, b));
+}
+
+// getValue (VG.cpp:4713-4755): descend to the leaf, then read the atlas voxel at the leaf's
+// mValue plus the position's offset inside it, from a dense atlas of channel 0
+float VolumeGVDB::getValue(slong nodeid, Vector3DF pos, float* atlas)
+{
+    Node* curr = getNode(nodeid);
+    if (!curr || !atlas) return 0.0f;
+    const Vector3DI range = getRange(curr->mLev);
+    float p[3] = {pos.x - (float)curr->mPos.x, pos.y - (float)curr->mPos.y, pos.z - (float)curr->mPos.z};
+    const float rg[3] = {(float)range.x, (float)range.y, (float)range.z};
+    if (!(p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && p[0] < rg[0] && p[1] < rg[1] && p[2] < rg[2])) return 0.0f;
+    const float res = (float)getRes(curr->mLev);
+    for (int a = 0; a < 3; a++) p[a] = p[a] * res / rg[a];
+    if (isLeaf(nodeid)) {
+        gvx_info inf;
+        check(gvx_get_info(g_, &inf));
+        const float x = p[0] + (float)curr->mValue.x, y = p[1] + (float)curr->mValue.y, z = p[2] + (float)curr->mValue.z;
+        return atlas[((size_t)(int)z * inf.atlas_res[1] + (size_t)(int)y) * inf.atlas_res[0] + (size_t)(int)x];
+    }
+    const uint32 i = (uint32)getBitPos(curr->mLev, Vector3DI((int)p[0], (int)p[1], (int)p[2]));
+    if (!isOn(nodeid, i)) return 0.0f;
+    return getValue((slong)getChildNode(nodeid, i), pos, atlas);
 }
 
 Vector3DF VolumeGVDB::getWorldMin()

@@ -70,6 +70,8 @@ namespace nvdb {
 typedef unsigned char uchar;
 typedef int64_t slong;
 typedef uint64_t uint64;
+typedef uint32_t uint32;
+typedef unsigned int uint;
 typedef unsigned long long CUdeviceptr;  // the driver API's device pointer type
 
 struct Vector3DF {
@@ -201,6 +203,41 @@ public:
     Vector3DF getWorldMin();
     Vector3DF getWorldMax();
 
+    // ---- tree shape (VG.h:592-621) and host-side tree queries (VG.h:449-470) on the pools and
+    //      child lists read back on demand: getChildNode/isOn (VG.cpp:2787-2796, 3079-3092),
+    //      getChildRefAtBit/getChildAtBit (3052-3076), getPosInNode (2858-2875),
+    //      getNodeAtPoint/isActive/getValue (4650-4755)
+    int getRes(int lev) { return (lev >= 0 && lev < levels_) ? (1 << logdim_[lev]) : 0; }
+    Vector3DI getRes3DI(int lev)
+    {
+        const int r = getRes(lev);
+        return Vector3DI(r, r, r);
+    }
+    Vector3DI getRange(int lev);
+    Vector3DF getCover(int lev)
+    {
+        const Vector3DI r = getRange(lev);
+        return Vector3DF((float)r.x, (float)r.y, (float)r.z);
+    }
+    int getBitPos(int lv, Vector3DI pos)
+    {
+        const int res = getRes(lv);
+        return (pos.z * res + pos.y) * res + pos.x;
+    }
+    bool isLeaf(slong nodeid) { return (((uint64)nodeid >> 8) & 0xFF) == 0; }
+    uint64 getChildNode(slong nodeid, uint b);
+    uint64 getChildRefAtBit(Node* curr, uint b);
+    Node* getChildAtBit(Node* curr, uint b);
+    bool isOn(slong nodeid, uint32 b);
+    bool getPosInNode(slong curr_id, Vector3DI pos, uint32& bit);
+    uint64 getNodeAtPoint(uint64 nodeid, Vector3DF pos);
+    bool isActive(Vector3DI wpos);
+    bool isActive(Vector3DI wpos, slong nodeid);
+    // `atlas`: channel 0 in the reference's dense atlas layout (gvx_read_channel_dense)
+    float getValue(slong nodeid, Vector3DF pos, float* atlas);
+    // no reference counterpart (the reference keeps mRoot protected): Elem id of the root node
+    uint64 getRootNodeID();
+
     // ---- no reference counterpart
     // TRILINEAR / CUBIC splat of weight (and velocity) into channels (gvx_splat)
     void Splat(int mode, int num_pnts, float radius, Vector3DF trans, int chanDensity, int chanVel,
@@ -217,6 +254,7 @@ private:
     void need_grid();
     void topology_changed() { gen_++; }
     Node* mirror(int lev, uint64 ndx);
+    const uint64* child_list(uint64 listid);  // the res^3 entries of a child list (group 1)
 
     gvx_grid* g_ = nullptr;
     int dev_ = 0;
@@ -226,6 +264,9 @@ private:
     uint64 gen_ = 1;
     std::vector<std::vector<Node>> mirror_;
     std::vector<uint64> mirror_gen_;
+    std::vector<std::vector<uint64>> clmirror_;
+    std::vector<uint64> clmirror_gen_;
+    int logdim_[GVX_MAX_LEVELS] = {};
     DataPtr pos_, vel_, clr_, pnode_;
     int last_insert_n_ = 0;
     int chan_type_[32];  // the type each AddChannel gave, -1 for none
