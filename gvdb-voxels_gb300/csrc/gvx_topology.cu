@@ -20,6 +20,7 @@
 // (sorted direct nodes, then sorted extra nodes: the order of the reference's
 // two passes), parent indices and child-list slots are all O(1) rank lookups.
 // The host reads back 24 bytes (bounding box) and the per-level counts.
+#include <limits.h>
 #include <math.h>
 #include <string.h>
 
@@ -65,18 +66,59 @@ __global__ void k_bbox(const char* pos, int off, int stride, uint32_t n, float o
 {
     uint32_t mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
     bool nan = false;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float w[3];
-        load_pos(pos, off, stride, i, w);
-        w[0] += ox;
-        w[1] += oy;
-        w[2] += oz;
+    const uint32_t nt = gridDim.x * blockDim.x, t = blockIdx.x * blockDim.x + threadIdx.x;
+    const char* base = pos + off;
+    if (stride == 12 && ((uintptr_t)base & 15u) == 0 && nt % 3u == 0) {
+        // packed float3, 16-byte aligned: four points in three float4 loads.  Float4 j holds
+        // floats 4j .. 4j+3, whose axes are (j + k) mod 3; the thread count is a multiple of 3,
+        // so j mod 3 = t mod 3 on every iteration and component k keeps one axis throughout.
+        const float4* v = (const float4*)base;
+        const uint64_t nflt = 3ull * n, nv = nflt / 4;
+        const uint32_t ph = t % 3u;
+        const float oc[3] = {ph == 0 ? ox : (ph == 1 ? oy : oz), ph == 0 ? oy : (ph == 1 ? oz : ox),
+                             ph == 0 ? oz : (ph == 1 ? ox : oy)};
+        uint32_t cmn[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, cmx[4] = {0u, 0u, 0u, 0u};
+        for (uint64_t j = t; j < nv; j += nt) {
+            const float4 q = v[j];
+            const float w[4] = {q.x + oc[0], q.y + oc[1], q.z + oc[2], q.w + oc[0]};
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (w[a] != w[a]) nan = true;
-            const uint32_t o = f2ord(w[a]);
-            mn[a] = min(mn[a], o);
-            mx[a] = max(mx[a], o);
+            for (int k = 0; k < 4; k++) {
+                if (w[k] != w[k]) nan = true;
+                const uint32_t o = f2ord(w[k]);
+                cmn[k] = min(cmn[k], o);
+                cmx[k] = max(cmx[k], o);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t a = (ph + (uint32_t)k) % 3u;
+            mn[a] = min(mn[a], cmn[k]);
+            mx[a] = max(mx[a], cmx[k]);
+        }
+        if (t == 0) {  // the floats after the last whole float4
+            const float o3[3] = {ox, oy, oz};
+            for (uint64_t f = nv * 4; f < nflt; f++) {
+                const uint32_t a = (uint32_t)(f % 3u);
+                const float w = ((const float*)base)[f] + o3[a];
+                if (w != w) nan = true;
+                mn[a] = min(mn[a], f2ord(w));
+                mx[a] = max(mx[a], f2ord(w));
+            }
+        }
+    } else {
+        for (uint32_t i = t; i < n; i += nt) {
+            float w[3];
+            load_pos(pos, off, stride, i, w);
+            w[0] += ox;
+            w[1] += oy;
+            w[2] += oz;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (w[a] != w[a]) nan = true;
+                const uint32_t o = f2ord(w[a]);
+                mn[a] = min(mn[a], o);
+                mx[a] = max(mx[a], o);
+            }
         }
     }
 #pragma unroll
@@ -674,11 +716,27 @@ __global__ void k_bounds_init(int* out)
 // ComputeBounds (VG.cpp:1792-1816): bbox of active leaves
 __global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int range, int* out)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !nodes[i].flags) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // whole warps: the grid is a multiple of 32
+    int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
+    if (i < n && nodes[i].flags) {
+        for (int a = 0; a < 3; a++) {
+            mn[a] = nodes[i].pos[a];
+            mx[a] = nodes[i].pos[a] + range;
+        }
+    }
+    // one atomic per warp and bound
+#pragma unroll
     for (int a = 0; a < 3; a++) {
-        atomicMin(&out[a], nodes[i].pos[a]);
-        atomicMax(&out[3 + a], nodes[i].pos[a] + range);
+        for (int s = 16; s > 0; s >>= 1) {
+            mn[a] = min(mn[a], __shfl_xor_sync(0xFFFFFFFFu, mn[a], s));
+            mx[a] = max(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], s));
+        }
+    }
+    if ((threadIdx.x & 31) == 0 && mn[0] != INT_MAX) {
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&out[a], mn[a]);
+            atomicMax(&out[3 + a], mx[a]);
+        }
     }
 }
 
@@ -1642,7 +1700,8 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     // ---- GetBoundingBox: one reduction, 24 bytes to the host
     uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
     GVX_CK(cudaMemcpyAsync(g->d_bbox.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
-    const unsigned bb = std::min(blocks_for(n, 256), 152u * 8u);
+    // a multiple of 3 blocks (of 256 threads): the packed path needs the thread count divisible by 3
+    const unsigned bb = (std::min(blocks_for(n, 256), 152u * 8u) + 2u) / 3u * 3u;
     k_bbox<<<bb, 256, 0, st>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, o[0], o[1], o[2],
                                g->d_bbox.as<uint32_t>(), g->d_err.as<uint32_t>());
     g->launches++;

@@ -319,3 +319,40 @@ def test_plain_small_32_cubed_bricks(gvx_mod, orc):
     g.update_apron(0, 0.5)
     o.update_apron(0, 0.5)
     assert rel_error(g.read_channel(0)[:used], o.read_channel(0)[:used]) <= DENSITY_TOL
+
+
+@pytest.mark.parametrize("mode", ["trilinear", "cubic"])
+def test_dense_cluster_against_oracle(gvx_mod, orc, mode):
+    """many points per voxel (a Gaussian cluster of sigma 2.5 voxels next to a sparse background):
+    long hit batches, many cells per batch and deep same-row ordering in every slab"""
+    rng = np.random.default_rng(41)
+    dense = rng.normal(0.0, 2.5, (40_000, 3)) + np.array([40.0, 36.0, 44.0])
+    sparse = rng.random((5_000, 3)) * np.array([80.0, 72.0, 88.0]) + 2.0
+    pos = np.concatenate([dense, sparse]).astype(np.float32)
+    pos = pos[(pos > 1.0).all(axis=1)]
+    vel = rng.normal(0, 1, pos.shape).astype(np.float32)
+    w = (0.5 + rng.random(len(pos))).astype(np.float32)
+    if mode == "trilinear":
+        g, o = make_pair(gvx_mod, orc, pos, 1.0, weight=w)
+        g.splat(gvx_mod.SPLAT_TRILINEAR, len(pos), 1.0, chan_density=0)
+        o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=w)
+        assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
+    else:
+        g, o = make_pair(gvx_mod, orc, pos, 2.0, weight=w, vel=vel, channels=((0, 3), (1, 4)))
+        g.splat(gvx_mod.SPLAT_CUBIC, len(pos), 2.0, chan_density=0, chan_vel=1)
+        o.splat(orc.SPLAT_CUBIC, pos, 2.0, weight=w, vel=vel, chan_vel=1)
+        assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
+        v, vr = g.read_channel(1), o.read_channel(1)
+        assert np.abs(v[..., :3] - vr[..., :3]).max() <= 1e-5 * np.abs(vr).max()
+
+
+@pytest.mark.parametrize("radius", [1.0, 1.5, 2.0])
+def test_cubic_lattice_points_on_support_edges(gvx_mod, orc, radius):
+    """points on integer and half-integer coordinates, brick faces included: voxels exactly at
+    distance R (weight 0, excluded) and rows exactly at dy^2 + dz^2 = R^2"""
+    g1 = np.arange(2.0, 60.0, 1.5)
+    pos = np.stack(np.meshgrid(g1, g1[:24], g1[:30], indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    g, o = make_pair(gvx_mod, orc, pos, radius)
+    g.splat(gvx_mod.SPLAT_CUBIC, len(pos), radius, chan_density=0)
+    o.splat(orc.SPLAT_CUBIC, pos, radius)
+    assert rel_error(g.read_channel(0), o.read_channel(0)) <= DENSITY_TOL
