@@ -128,6 +128,16 @@ __global__ void k_pnode(const uint32_t* __restrict__ skeys, const uint32_t* __re
     pnode[svals[i]] = leaf;
 }
 
+// the grid's stream waits for attribute uploads still in flight on the side stream
+gvx_status gvx_wait_attributes(gvx_grid* g)
+{
+    if (g->attr_pending) {
+        GVX_CK(cudaStreamWaitEvent(g->stream, g->ev_attr_ready, 0));
+        g->attr_pending = false;
+    }
+    return GVX_OK;
+}
+
 extern "C" {
 
 const char* gvx_last_error(void) { return t_err; }
@@ -168,6 +178,7 @@ gvx_status gvx_destroy(gvx_grid* g)
     if (!g) return GVX_OK;
     cudaSetDevice(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->aux_stream) cudaStreamSynchronize(g->aux_stream);
     DevBuf* bufs[] = {&g->bm_a, &g->bm_a_prefix, &g->bm_b, &g->bm_b_prefix, &g->remap, &g->leaf_key, &g->leaf_range,
                       &g->leaf_oct,
                       &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos, &g->own_vel, &g->own_w,
@@ -187,6 +198,9 @@ gvx_status gvx_destroy(gvx_grid* g)
     for (int c = 0; c < GVX_MAXCH; c++) gvx_free(g->ch[c].data);
     gvx_host_tree_free(g);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
+    if (g->ev_attr_free) cudaEventDestroy(g->ev_attr_free);
+    if (g->ev_attr_ready) cudaEventDestroy(g->ev_attr_ready);
     delete g;
     return GVX_OK;
 }
@@ -204,6 +218,7 @@ gvx_status gvx_set_stream(gvx_grid* g, void* stream)
 gvx_status gvx_sync(gvx_grid* g)
 {
     GVX_GUARD(g);
+    if (g->aux_stream) GVX_CK(cudaStreamSynchronize(g->aux_stream));
     GVX_CK(cudaStreamSynchronize(g->stream));
     return gvx_check_device_error(g, "sync");
 }
@@ -394,11 +409,12 @@ __global__ void k_pack_float3(const unsigned char* __restrict__ src, int stride,
 
 // one host -> device copy of n float3 records with a byte stride: packed records in one flat copy;
 // strided ones as the raw bytes, packed by a kernel (a 2D copy of 12-byte rows is one DMA row a point)
-static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int stride, int n)
+static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int stride, int n,
+                                cudaStream_t st = nullptr)
 {
     GVX_CK(gvx_ensure(dst, (size_t)n * 12));
     if (stride == 12) {
-        GVX_CK(cudaMemcpyAsync(dst.p, src, (size_t)n * 12, cudaMemcpyHostToDevice, g->stream));
+        GVX_CK(cudaMemcpyAsync(dst.p, src, (size_t)n * 12, cudaMemcpyHostToDevice, st ? st : g->stream));
         return GVX_OK;
     }
     if (stride & 3) {
@@ -424,17 +440,38 @@ gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_s
     }
     gvx_status rc0 = upload_float3(g, g->own_pos, pos, pos_stride, n);
     if (rc0) return rc0;
+    // The attributes (packed velocities, weights, radii) go up on the side stream, so that their
+    // copies overlap the topology build, which needs only positions.  The side stream first waits
+    // for the work already queued on the grid's stream (earlier readers of these buffers); the
+    // point permute waits for the copies (gvx_wait_attributes).  Strided velocities share the
+    // staging buffer with the positions and stay on the grid's stream.
+    const bool side = (vel && vel_stride == 12) || weight || radius;
+    cudaStream_t as = g->stream;
+    if (side) {
+        if (!g->aux_stream) {
+            GVX_CK(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
+            GVX_CK(cudaEventCreateWithFlags(&g->ev_attr_free, cudaEventDisableTiming));
+            GVX_CK(cudaEventCreateWithFlags(&g->ev_attr_ready, cudaEventDisableTiming));
+        }
+        GVX_CK(cudaEventRecord(g->ev_attr_free, g->stream));
+        GVX_CK(cudaStreamWaitEvent(g->aux_stream, g->ev_attr_free, 0));
+        as = g->aux_stream;
+    }
     if (vel) {
-        rc0 = upload_float3(g, g->own_vel, vel, vel_stride, n);
+        rc0 = upload_float3(g, g->own_vel, vel, vel_stride, n, vel_stride == 12 ? as : g->stream);
         if (rc0) return rc0;
     }
     if (weight) {
         GVX_CK(gvx_ensure(g->own_w, (size_t)n * 4));
-        GVX_CK(cudaMemcpyAsync(g->own_w.p, weight, (size_t)n * 4, cudaMemcpyHostToDevice, g->stream));
+        GVX_CK(cudaMemcpyAsync(g->own_w.p, weight, (size_t)n * 4, cudaMemcpyHostToDevice, as));
     }
     if (radius) {
         GVX_CK(gvx_ensure(g->own_r, (size_t)n * 4));
-        GVX_CK(cudaMemcpyAsync(g->own_r.p, radius, (size_t)n * 4, cudaMemcpyHostToDevice, g->stream));
+        GVX_CK(cudaMemcpyAsync(g->own_r.p, radius, (size_t)n * 4, cudaMemcpyHostToDevice, as));
+    }
+    if (side) {
+        GVX_CK(cudaEventRecord(g->ev_attr_ready, g->aux_stream));
+        g->attr_pending = true;
     }
     gvx_status rc = gvx_set_points(g, n, g->own_pos.p, 0, 12, vel ? g->own_vel.p : nullptr, 0, 12, nullptr, 0, 0);
     if (rc) return rc;

@@ -55,6 +55,11 @@ struct gvx_grid {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // host uploads of the point attributes run on a side stream, overlapping the topology
+    // build; the point permute, the only device reader of them, waits for ev_attr_ready
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_attr_free = nullptr, ev_attr_ready = nullptr;
+    bool attr_pending = false;
 
     // configuration (Configure)
     bool configured = false;
@@ -174,6 +179,7 @@ gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, c
                            const uint64_t* const* clists);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
 gvx_status gvx_topo_octants(gvx_grid* g);
+gvx_status gvx_wait_attributes(gvx_grid* g);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
 // InsertPoints: grouping + sorted attribute arrays

@@ -836,7 +836,9 @@ static inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n
 gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel)
 {
     const float t[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
-    gvx_status rc = gvx_topo_group_points(g, n, t);
+    gvx_status rc = gvx_wait_attributes(g);
+    if (rc) return rc;
+    rc = gvx_topo_group_points(g, n, t);
     if (rc) return rc;
     rc = gvx_topo_octants(g);
     if (rc) return rc;
