@@ -485,7 +485,10 @@ gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float or
         gvx_set_error("RebuildTopology: mode %d", mode);
         return GVX_ERR_INVALID_ARG;
     }
-    return gvx_topo_rebuild(g, n, radius, orig, mode, min_depth);
+    gvx_status rc = gvx_topo_rebuild(g, n, radius, orig, mode, min_depth);
+    // the topology build is queued: from here the grid's stream also covers the attribute uploads
+    gvx_status rw = gvx_wait_attributes(g);
+    return rc ? rc : rw;
 }
 
 gvx_status gvx_request_full_rebuild(gvx_grid* g, int on)

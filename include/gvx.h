@@ -117,7 +117,11 @@ gvx_status gvx_set_points(gvx_grid* g, int n, const void* pos, int pos_offset, i
 gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* radius);
 /* CommitData of host points (VG.cpp:532-538): copies n host points (and optional
  * velocities, weights, radii) into library-owned device buffers and binds them
- * as by gvx_set_points.  Strides are in bytes. */
+ * as by gvx_set_points.  Strides are in bytes.  The copies are asynchronous:
+ * the host arrays may be reused once the grid's stream has passed the next call
+ * that takes points (gvx_rebuild_topology, gvx_insert_points, a splat), or after
+ * gvx_sync.  (The attribute copies run on a side stream beside the topology
+ * build; those calls make the grid's stream wait for them.) */
 gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_stride,
                                   const void* vel, int vel_stride, const float* weight,
                                   const float* radius);
