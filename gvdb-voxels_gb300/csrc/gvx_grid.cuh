@@ -178,7 +178,17 @@ void gvx_host_tree_free(gvx_grid* g);
 gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
                            const uint64_t* const* clists);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
-gvx_status gvx_topo_octants(gvx_grid* g);
+// sorted point attributes written together with the octant partition (spos null: none)
+struct GvxSortedAttr {
+    const char* vel;
+    int vel_off, vel_stride;
+    const float* weight;
+    const float* radius;
+    float4* spos;          // (x, y, z, weight) of the translated positions
+    float4* svel;          // (vx, vy, vz, radius), or null
+    unsigned int* rmax;    // float bits of the largest radius, or null
+};
+gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr);
 gvx_status gvx_wait_attributes(gvx_grid* g);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);

@@ -840,34 +840,61 @@ gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool nee
     if (rc) return rc;
     rc = gvx_topo_group_points(g, n, t);
     if (rc) return rc;
-    rc = gvx_topo_octants(g);
-    if (rc) return rc;
+    const bool want_svel = need_svel || g->pts.vel || g->pts.radius;
+    const uint32_t m = g->n_sorted;
+    auto attr_buffers = [&](unsigned int** rmax) -> gvx_status {
+        GVX_CK(gvx_ensure(g->spos, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
+        if (want_svel) GVX_CK(gvx_ensure(g->svel, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
+        *rmax = nullptr;
+        if (g->pts.radius && want_svel) {
+            GVX_CK(gvx_ensure(g->d_rmax, sizeof(unsigned int)));
+            GVX_CK(cudaMemsetAsync(g->d_rmax.p, 0, sizeof(unsigned int), g->stream));
+            *rmax = g->d_rmax.as<unsigned int>();
+        }
+        return GVX_OK;
+    };
+    auto mark_permuted = [&]() {
+        g->perm_valid = true;
+        g->perm_has_svel = want_svel;
+        g->perm_vel = g->pts.vel;
+        g->perm_w = g->pts.weight;
+        g->perm_r = g->pts.radius;
+    };
+    if (!g->oct_valid) {
+        // a new grouping: octant order and the sorted attributes in one pass over the points
+        unsigned int* rmax = nullptr;
+        rc = attr_buffers(&rmax);
+        if (rc) return rc;
+        GvxSortedAttr A;
+        A.vel = g->pts.vel;
+        A.vel_off = g->pts.vel_off;
+        A.vel_stride = g->pts.vel_stride;
+        A.weight = g->pts.weight;
+        A.radius = g->pts.radius;
+        A.spos = g->spos.as<float4>();
+        A.svel = want_svel ? g->svel.as<float4>() : nullptr;
+        A.rmax = rmax;
+        rc = gvx_topo_octants(g, &A);
+        if (rc) return rc;
+        mark_permuted();
+        return GVX_OK;
+    }
     if (g->perm_valid && (g->perm_has_svel || !need_svel) && g->perm_vel == g->pts.vel &&
         g->perm_w == g->pts.weight && g->perm_r == g->pts.radius)
         return GVX_OK;
-    need_svel = need_svel || g->pts.vel || g->pts.radius;
-    const uint32_t m = g->n_sorted;
-    GVX_CK(gvx_ensure(g->spos, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
-    if (need_svel) GVX_CK(gvx_ensure(g->svel, (size_t)std::max<uint32_t>(m, 1u) * sizeof(float4)));
+    // the same grouping with other attributes: the permute alone
+    unsigned int* rmax = nullptr;
+    rc = attr_buffers(&rmax);
+    if (rc) return rc;
     if (m) {
-        unsigned int* rmax = nullptr;
-        if (g->pts.radius && need_svel) {
-            GVX_CK(gvx_ensure(g->d_rmax, sizeof(unsigned int)));
-            GVX_CK(cudaMemsetAsync(g->d_rmax.p, 0, sizeof(unsigned int), g->stream));
-            rmax = g->d_rmax.as<unsigned int>();
-        }
         k_permute<<<blocks_for(m, 256), 256, 0, g->stream>>>(
             g->vals[g->sorted_buf].as<uint32_t>(), m, g->pts.pos, g->pts.pos_off, g->pts.pos_stride, g->pts.vel,
             g->pts.vel_off, g->pts.vel_stride, g->pts.weight, g->pts.radius, t[0], t[1], t[2], g->spos.as<float4>(),
-            need_svel ? g->svel.as<float4>() : nullptr, rmax);
+            want_svel ? g->svel.as<float4>() : nullptr, rmax);
         g->launches++;
     }
     GVX_CK(cudaGetLastError());
-    g->perm_valid = true;
-    g->perm_has_svel = need_svel;
-    g->perm_vel = g->pts.vel;
-    g->perm_w = g->pts.weight;
-    g->perm_r = g->pts.radius;
+    mark_permuted();
     return GVX_OK;
 }
 

@@ -588,11 +588,14 @@ __global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uin
 // axis, octant = 4 hx + 2 hy + hz, and the first index of every octant.  The
 // sorted order becomes (leaf key, octant, point index); the splat reads only
 // the octants of a neighbouring brick whose points can reach its slab.  One
-// warp per leaf; lanes 0-7 keep the octants' counters.
+// warp per leaf; lanes 0-7 keep the octants' counters.  With A.spos the sorted
+// point attributes of the leaves' points are written in the same pass (as
+// k_permute writes them); entries outside the leaf ranges are not, and no
+// reader takes them (a point is splatted only when its own leaf exists).
 __global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t nleaves,
                                    const GvxNode* __restrict__ nodes0, const char* pos, int off, int stride, float ox,
                                    float oy, float oz, int half, const uint32_t* __restrict__ vin,
-                                   uint32_t* __restrict__ vout, int* __restrict__ leaf_oct)
+                                   uint32_t* __restrict__ vout, int* __restrict__ leaf_oct, GvxSortedAttr A)
 {
     const uint32_t leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -647,6 +650,30 @@ __global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t
         const uint32_t same = __match_any_sync(0xFFFFFFFFu, o);
         const int dst = __shfl_sync(0xFFFFFFFFu, run, o < 0 ? 0 : o) + __popc(same & ((1u << lane) - 1u));
         if (o >= 0) vout[dst] = v;
+        if (A.spos) {
+            float rr = 0.0f;
+            if (o >= 0) {
+                float w[3];
+                load_pos(pos, off, stride, v, w);
+                A.spos[dst] = make_float4(w[0] + ox, w[1] + oy, w[2] + oz, A.weight ? A.weight[v] : 1.0f);
+                if (A.radius) rr = A.radius[v];
+                if (A.svel) {
+                    float4 q = make_float4(0.f, 0.f, 0.f, rr);
+                    if (A.vel) {
+                        const float* u = (const float*)(A.vel + (size_t)v * A.vel_stride + A.vel_off);
+                        q.x = u[0];
+                        q.y = u[1];
+                        q.z = u[2];
+                    }
+                    A.svel[dst] = q;
+                }
+                rr = rr != rr ? 3.0e38f : fmaxf(rr, 0.0f);
+            }
+            if (A.rmax) {
+                const unsigned int mm = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(rr));
+                if (lane == 0 && mm) atomicMax(A.rmax, mm);
+            }
+        }
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k);
@@ -1064,9 +1091,11 @@ static gvx_status fill_leaf_ranges(gvx_grid* g, uint32_t nleaves)
 // Octant order inside every leaf (k_octant_partition), once per grouping, for
 // the splats: partition into the other value buffer (a copy of the sorted
 // values, so entries outside the leaf ranges keep theirs), then copy back.
-gvx_status gvx_topo_octants(gvx_grid* g)
+gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr)
 {
     if (g->oct_valid) return GVX_OK;
+    GvxSortedAttr none;
+    memset(&none, 0, sizeof(none));
     const uint32_t nleaves = g->oct_leaves;
     if (g->n_sorted && nleaves) {
         uint32_t* vin = g->vals[g->sorted_buf].as<uint32_t>();
@@ -1076,13 +1105,13 @@ gvx_status gvx_topo_octants(gvx_grid* g)
         k_octant_partition<<<blocks_for((uint64_t)nleaves * 32u, 256), 256, 0, g->stream>>>(
             g->leaf_range.as<int2>(), nleaves, g->nodes[0].as<GvxNode>(), g->pts.pos, g->pts.pos_off,
             g->pts.pos_stride, g->sort_trans[0], g->sort_trans[1], g->sort_trans[2], g->brick / 2, vin, vtmp,
-            g->leaf_oct.as<int>());
+            g->leaf_oct.as<int>(), attr ? *attr : none);
         g->launches++;
         GVX_CK(cudaMemcpyAsync(vin, vtmp, vb, cudaMemcpyDeviceToDevice, g->stream));
         GVX_CK(cudaGetLastError());
     }
     g->oct_valid = true;
-    g->perm_valid = false;  // the sorted attributes follow the new order
+    g->perm_valid = false;  // the sorted attributes follow the new order (the caller sets it when attr wrote them)
     return GVX_OK;
 }
 
