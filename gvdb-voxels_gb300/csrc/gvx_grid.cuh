@@ -141,6 +141,7 @@ struct gvx_grid {
     DevBuf inc0, inc_remap;  // incremental build: linked + new level-0 bitmaps, linked rank -> pool index
     DevBuf d_err, d_bbox;
     DevBuf d_rmax;  // float bits of the largest per-point radius of the last point permute
+    DevBuf d_next;  // work-unit counter of the splat launch
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index

@@ -121,6 +121,7 @@ struct SplatArgs {
     bool accum;
     float boundval;
     uint32_t* err;
+    uint32_t* next;  // work-unit counter of the single-grid launch
 };
 
 // Shared-memory tile of one padded brick.  Density only: float per voxel.
@@ -664,18 +665,23 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t units = a.nslots * (uint32_t)a.slabs;
-    const uint32_t nw = gridDim.x * kSlabWarps;
-    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < units; u += nw)
+    // units one at a time from a counter (zeroed before the launch): bricks differ widely in cost
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(a.next, 1u);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= units) break;
         splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], phase, lane);
+    }
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
 
 // The same work over many grids in one persistent launch: the units of grid
-// k are [ustart[k], ustart[k+1]) of one global range, dealt to the warps in
-// stride; every grid has the same brick and tile shape (slab_layers, P).
+// k are [ustart[k], ustart[k+1]) of one global range, taken by the warps from
+// a counter; every grid has the same brick and tile shape (slab_layers, P).
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
 __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
-    k_splat_batch(const SplatArgs* __restrict__ args, const uint32_t* __restrict__ ustart, int ngrids)
+    k_splat_batch(const SplatArgs* __restrict__ args, uint32_t* __restrict__ ustart, int ngrids)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -693,8 +699,15 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t total = s_us[ngrids];
-    const uint32_t nw = gridDim.x * kSlabWarps;
-    for (uint32_t u = blockIdx.x * kSlabWarps + wid; u < total; u += nw) {
+    // units are taken one at a time from a counter (ustart[ngrids + 1], zeroed before every
+    // launch): a brick of a dense cloud costs many times a sparse one, and a fixed stride
+    // would leave the warps that drew the dense ones running alone at the end
+    uint32_t* next = ustart + ngrids + 1;
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(next, 1u);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= total) break;
         int lo = 0, hi = ngrids - 1;  // the grid k with ustart[k] <= u < ustart[k+1]
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -1079,6 +1092,9 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         const uint64_t ctas_needed = (units + kSlabWarps - 1) / kSlabWarps;
         const uint32_t grid =
             (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g->device) * std::max(per_sm, 1));
+        GVX_CK(gvx_ensure(g->d_next, sizeof(uint32_t)));
+        GVX_CK(cudaMemsetAsync(g->d_next.p, 0, sizeof(uint32_t), g->stream));
+        a.next = g->d_next.as<uint32_t>();
         void* args[] = {&a};
         GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kSlabWarps * 32), args, smem, g->stream));
         g->launches++;
@@ -1144,7 +1160,8 @@ static gvx_status batch_launch(gvx_batch* b, const SplatKind& k, const SplatArgs
     const size_t smem = splat_smem(a0, k);
     void* kern = splat_kernel(k, true);
     const SplatArgs* dargs = b->d_args.as<SplatArgs>();
-    const uint32_t* dus = b->d_ustart.as<uint32_t>();
+    uint32_t* dus = b->d_ustart.as<uint32_t>();
+    GVX_CK(cudaMemsetAsync(dus + ngrids + 1, 0, sizeof(uint32_t), b->stream));  // the unit counter
     void* args[] = {(void*)&dargs, (void*)&dus, (void*)&ngrids};
     GVX_CK(cudaLaunchKernel(kern, dim3(blocks), dim3(kSlabWarps * 32), args, smem, b->stream));
     b->launches++;
@@ -1185,7 +1202,7 @@ static gvx_status batch_tables(gvx_batch* b, int mode, float radius, int chan_d,
 static gvx_status batch_upload(gvx_batch* b, const std::vector<SplatArgs>& args, const std::vector<uint32_t>& ustart)
 {
     GVX_CK(gvx_ensure(b->d_args, args.size() * sizeof(SplatArgs)));
-    GVX_CK(gvx_ensure(b->d_ustart, ustart.size() * sizeof(uint32_t)));
+    GVX_CK(gvx_ensure(b->d_ustart, (ustart.size() + 1) * sizeof(uint32_t)));  // + the unit counter
     GVX_CK(cudaMemcpyAsync(b->d_args.p, args.data(), args.size() * sizeof(SplatArgs), cudaMemcpyHostToDevice,
                            b->stream));
     GVX_CK(cudaMemcpyAsync(b->d_ustart.p, ustart.data(), ustart.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
