@@ -41,6 +41,7 @@ struct BackArgs {
     float* gw;
     float* gr;                // or null
     uint32_t* err;
+    uint32_t* next;           // point counter (zeroed before the launch)
 };
 
 }  // namespace
@@ -49,10 +50,13 @@ template <int MODE>
 __global__ void __launch_bounds__(kBackThreads) k_splat_backward(BackArgs a)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const int P = a.P, P3 = P * P * P, ap = a.apron, b = a.brick, lb = a.lb;
-    for (uint32_t i = warp0; i < a.n; i += nwarps) {
+    // points one at a time from a counter: their supports differ in size
+    for (;;) {
+        uint32_t i = 0;
+        if (lane == 0) i = atomicAdd(a.next, 1u);
+        i = __shfl_sync(0xFFFFFFFFu, i, 0);
+        if (i >= a.n) break;
         const uint32_t key = a.skeys[i];
         const uint32_t orig = a.svals[i];
         // the point takes part iff its own brick is in the lookup (as in the forward)
@@ -235,6 +239,9 @@ extern "C" gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float rad
     a.gr = grad_r;
     a.err = g->d_err.as<uint32_t>();
     if (a.n) {
+        GVX_CK(gvx_ensure(g->d_next, sizeof(uint32_t)));
+        GVX_CK(cudaMemsetAsync(g->d_next.p, 0, sizeof(uint32_t), g->stream));
+        a.next = g->d_next.as<uint32_t>();
         const unsigned blocks = std::min<unsigned>(blocks_for((uint64_t)a.n * 32u, kBackThreads), 152u * 16u);
         if (mode == GVX_SPLAT_CUBIC)
             k_splat_backward<GVX_SPLAT_CUBIC><<<blocks, kBackThreads, 0, g->stream>>>(a);

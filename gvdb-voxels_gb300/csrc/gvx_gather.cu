@@ -165,6 +165,7 @@ struct GatherArgs {
     int levelset, accum;
     float* out;         // T_FLOAT channel, brick-major padded
     uint32_t* clr_out;  // T_UCHAR4 channel or null
+    uint32_t* next;     // subcell counter (zeroed before the launch)
 };
 
 __device__ __forceinline__ uint32_t clr_to_char(const float c[4])
@@ -192,6 +193,7 @@ struct GatherQArgs {
     float radius;
     float* out;           // T_FLOAT channel
     uint32_t* clr_out;    // any 4-byte channel, or null
+    uint32_t* next;       // subcell counter (zeroed before the launch)
 };
 
 // float -> uint32 as the GPU's conversion does: truncation, saturating, NaN -> 0
@@ -212,10 +214,13 @@ template <int VPL>
 __global__ void k_gather_fp16(GatherQArgs a)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const int sc = a.sc, nv = sc * sc * sc;
-    for (uint32_t s = warp0; s < a.nsub; s += nwarps) {
+    // subcells one at a time from a counter: their lists differ widely in length
+    for (;;) {
+        uint32_t s = 0;
+        if (lane == 0) s = atomicAdd(a.next, 1u);
+        s = __shfl_sync(0xFFFFFFFFu, s, 0);
+        if (s >= a.nsub) break;
         const uint32_t slot = s / (uint32_t)a.spb;
         const int loc = (int)(s - slot * (uint32_t)a.spb);
         const GvxNode& nd = a.nodes0[a.slot_leaf[slot]];
@@ -287,10 +292,13 @@ template <int VPL>
 __global__ void k_gather(GatherArgs a)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const int sc = a.sc, nv = sc * sc * sc;
-    for (uint32_t s = warp0; s < a.nsub; s += nwarps) {
+    // subcells one at a time from a counter: their lists differ widely in length
+    for (;;) {
+        uint32_t s = 0;
+        if (lane == 0) s = atomicAdd(a.next, 1u);
+        s = __shfl_sync(0xFFFFFFFFu, s, 0);
+        if (s >= a.nsub) break;
         const uint32_t slot = s / (uint32_t)a.spb;
         const int loc = (int)(s - slot * (uint32_t)a.spb);
         const GvxNode& nd = a.nodes0[a.slot_leaf[slot]];
@@ -558,6 +566,9 @@ gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radiu
     a.radius = radius;
     a.out = g->ch[cl].data.as<float>();
     a.clr_out = want_clr ? g->ch[chan_clr].data.as<uint32_t>() : nullptr;
+    GVX_CK(gvx_ensure(g->d_next, sizeof(uint32_t)));
+    GVX_CK(cudaMemsetAsync(g->d_next.p, 0, sizeof(uint32_t), g->stream));
+    a.next = g->d_next.as<uint32_t>();
     const unsigned blocks = std::min<unsigned>(blocks_for((uint64_t)a.nsub * 32u, 256), 152u * 16u);
     if (subcell * subcell * subcell <= 64)
         k_gather_fp16<2><<<blocks, 256, 0, g->stream>>>(a);
@@ -610,6 +621,9 @@ gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, 
     a.accum = accum ? 1 : 0;
     a.out = g->ch[chan].data.as<float>();
     a.clr_out = (chan_clr >= 0 && g->sc_has_clr) ? g->ch[chan_clr].data.as<uint32_t>() : nullptr;
+    GVX_CK(gvx_ensure(g->d_next, sizeof(uint32_t)));
+    GVX_CK(cudaMemsetAsync(g->d_next.p, 0, sizeof(uint32_t), g->stream));
+    a.next = g->d_next.as<uint32_t>();
     const unsigned blocks = std::min<unsigned>(blocks_for((uint64_t)a.nsub * 32u, 256), 152u * 16u);
     if (subcell * subcell * subcell <= 64)
         k_gather<2><<<blocks, 256, 0, g->stream>>>(a);
