@@ -480,6 +480,8 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
         }
     }
     if (lane == 0) s_ro_w[m] = total;
+    // an accumulating splat leaves a slab that no point reaches as it is: no load, no store
+    if (a.accum && total == 0) return;
 
     // ---- tile: previous values (accumulate) or zeros
     if (a.accum) {
