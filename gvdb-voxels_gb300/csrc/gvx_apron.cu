@@ -50,13 +50,28 @@ __global__ void __launch_bounds__(kApronWarps * 32) k_apron(ApronArgs a, T bound
         }
         __syncwarp();
         T* dst = data + (size_t)s * P3;
-#pragma unroll 4
-        for (int e = lane; e < a.napron; e += 32) {
-            const uint2 t = a.tab[e];
-            const int ns = s_ns[wid][t.x >> 24];
-            T v = boundval;
-            if (ns >= 0) v = data[(size_t)ns * P3 + t.y];
-            dst[t.x & 0xFFFFFFu] = v;
+        // U values per lane are loaded before any is stored: the sources (neighbours' interiors)
+        // and the destinations (this brick's apron) are the same array, so a load-store loop
+        // would keep one load in flight per lane
+        constexpr int U = sizeof(T) <= 4 ? 16 : 4;
+        for (int e0 = 0; e0 < a.napron; e0 += 32 * U) {
+            T v[U];
+            uint32_t di[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int e = e0 + u * 32 + lane;
+                v[u] = boundval;
+                di[u] = 0xFFFFFFFFu;
+                if (e < a.napron) {
+                    const uint2 t = a.tab[e];
+                    const int ns = s_ns[wid][t.x >> 24];
+                    if (ns >= 0) v[u] = data[(size_t)ns * P3 + t.y];
+                    di[u] = t.x & 0xFFFFFFu;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                if (di[u] != 0xFFFFFFFFu) dst[di[u]] = v[u];
         }
         __syncwarp();
     }
