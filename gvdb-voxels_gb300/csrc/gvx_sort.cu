@@ -66,7 +66,9 @@ __global__ void k_sort_bases(const uint32_t* __restrict__ hist, uint32_t* __rest
     base[p * 256 + t] = s[t] - v;
 }
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(const uint32_t* __restrict__ kin,
+// 4 resident tiles per SM (registers capped at 64): unbounded, the compiler's register use left room
+// for one tile per SM and a 32M-key sort took 1.7 ms instead of 1.0 ms
+__global__ void __launch_bounds__(kThreads, 4) k_onesweep(const uint32_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        uint32_t n, int shift, const uint32_t* __restrict__ base,
