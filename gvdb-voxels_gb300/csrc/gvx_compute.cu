@@ -88,12 +88,17 @@ __global__ void k_fill_op(unsigned char* data, AtlasShape s, int3 hi, int effect
 // staged in shared memory, its interior written back in place
 __global__ void k_smooth_slots(float* data, int P, int apron, size_t nslots, float p1, float p2)
 {
-    extern __shared__ float sb[];
+    extern __shared__ __align__(16) float sb[];
     const int P3 = P * P * P;
     const int b = P - 2 * apron;
     for (size_t s = blockIdx.x; s < nslots; s += gridDim.x) {
         float* g = data + s * (size_t)P3;
-        for (int i = threadIdx.x; i < P3; i += blockDim.x) sb[i] = g[i];
+        if ((P3 & 3) == 0) {  // slots of P^3 floats, P even: 16-byte aligned, moved as float4
+            const float4* g4 = (const float4*)g;
+            for (int i = threadIdx.x; i < P3 / 4; i += blockDim.x) ((float4*)sb)[i] = g4[i];
+        } else {
+            for (int i = threadIdx.x; i < P3; i += blockDim.x) sb[i] = g[i];
+        }
         __syncthreads();
         for (int i = threadIdx.x; i < b * b * b; i += blockDim.x) {
             const int x = apron + i % b, y = apron + (i / b) % b, z = apron + i / (b * b);
