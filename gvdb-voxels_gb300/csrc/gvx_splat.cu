@@ -24,7 +24,9 @@
 #include <string.h>
 
 #include <map>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -1341,6 +1343,48 @@ gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count)
     }
     b->grids.assign(grids, grids + count);
     batch_drop_graph(b);
+    return GVX_OK;
+}
+
+// Topology of every grid from a pool of host threads: each grid is driven by one
+// thread at a time (a grid handle is not shared between threads), and builds of
+// grids on different streams overlap on the GPU.  A build is mostly small kernels
+// and two host readbacks, so one thread alone leaves the GPU idle most of the time.
+gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    const size_t n = b->grids.size();
+    if (n == 0) return GVX_OK;
+    const size_t nt = std::min<size_t>(n, (size_t)std::max(1, threads > 0 ? threads : 8));
+    std::atomic<size_t> next{0};
+    std::vector<gvx_status> st(n, GVX_OK);
+    std::vector<std::string> msg(n);
+    const int device = b->device;
+    auto work = [&]() {
+        if (cudaSetDevice(device) != cudaSuccess) return;
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            gvx_grid* g = b->grids[i];
+            gvx_status r = gvx_rebuild_topology(g, g->pts.n, radius, nullptr, mode, 1);
+            if (r == GVX_OK) r = gvx_update_atlas(g);
+            if (r == GVX_OK) r = gvx_insert_points(g, g->pts.n, nullptr, nullptr);
+            st[i] = r;
+            if (r != GVX_OK) msg[i] = gvx_last_error();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (std::thread& t : pool) t.join();
+    for (size_t i = 0; i < n; i++)
+        if (st[i] != GVX_OK) {
+            gvx_set_error("BatchTopology: grid %zu: %s", i, msg[i].c_str());
+            return st[i];
+        }
     return GVX_OK;
 }
 

@@ -104,6 +104,7 @@ def load(path=None):
         "gvx_batch_set_stream": ([vp, vp], i), "gvx_batch_set_grids": ([vp, ctypes.POINTER(vp), i], i),
         "gvx_batch_splat": ([vp, i, f, i, i, i, i], i),
         "gvx_batch_get_tuning": ([vp, ip, ip, fp], i),
+        "gvx_batch_topology": ([vp, f, i, i], i),
         "gvx_batch_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
     }
     for name, (args, res) in sig.items():
@@ -442,6 +443,12 @@ class Batch:
     def splat(self, mode, radius, chan_density=0, chan_vel=-1, accum=False, graph=True, tune=False):
         flags = (BATCH_GRAPH if graph else 0) | (BATCH_TUNE if tune else 0)
         self._check(self.lib.gvx_batch_splat(self.h, mode, float(radius), chan_density, chan_vel, int(accum), flags))
+
+    def topology(self, radius, mode=None, threads=0):
+        """gvx_batch_topology: RebuildTopology + UpdateAtlas + InsertPoints of every grid, from a
+        pool of host threads"""
+        self._check(self.lib.gvx_batch_topology(self.h, float(radius), TOPO_FULL if mode is None else mode,
+                                                int(threads)))
 
     def tuning(self):
         la, bp, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0)

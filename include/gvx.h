@@ -367,6 +367,13 @@ gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count);
 gvx_status gvx_batch_splat(gvx_batch* b, int mode, float radius, int chan_density, int chan_vel, int accum,
                            int flags);
 gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_sm, float* ms);
+/* Topology of every grid of the batch (no reference counterpart): per grid, the
+ * calls gvx_rebuild_topology(radius, no origin, mode), gvx_update_atlas and
+ * gvx_insert_points over its bound points, as a caller would make them, made
+ * from `threads` host threads at once (0: 8) so that the grids' builds overlap
+ * on the GPU.  Grids that share a stream still build one after another.  The
+ * first failing grid's status is returned, its index in gvx_last_error(). */
+gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads);
 gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* count);
 
 #ifdef __cplusplus

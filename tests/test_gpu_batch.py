@@ -104,3 +104,35 @@ def test_batch_autotune_keeps_results(gvx_mod):
     assert t["slab_layers"] >= 1 and t["blocks_per_sm"] >= 1 and t["ms"] > 0
     assert same(read_all(grids, (0,)), ref)
     b.close()
+
+
+def test_batch_topology_matches_per_grid_builds(gvx_mod):
+    """gvx_batch_topology from 4 host threads, grids on their own streams: the same pools, child lists,
+    atlas maps and point groupings (checked through a splat) as one-by-one builds"""
+    cl = clouds(9, 11)
+    ref = make_grids(gvx_mod, cl, radius=1.0)
+    grids = []
+    for p, w in cl:
+        g = gvx_mod.Grid(0)
+        g.configure(LOGDIM)
+        g.add_channel(0, gvx_mod.T_FLOAT, 1)
+        g.commit_points_host(p, weight=w)
+        grids.append(g)
+    b = gvx_mod.Batch(0)
+    b.set_grids(grids)
+    b.topology(1.0, threads=4)
+    for g in grids:
+        g.sync()
+    for g, r, (p, _) in zip(grids, ref, cl):
+        gi, ri = g.info(), r.info()
+        assert gi["root_level"] == ri["root_level"] and gi["used_leaves"] == ri["used_leaves"]
+        for lev in range(ri["root_level"] + 1):
+            assert np.array_equal(g.read_nodes(lev), r.read_nodes(lev))
+            if lev > 0:
+                assert np.array_equal(g.read_childlist(lev), r.read_childlist(lev))
+        g.splat(gvx_mod.SPLAT_TRILINEAR, len(p), 1.0, chan_density=0)
+        r.splat(gvx_mod.SPLAT_TRILINEAR, len(p), 1.0, chan_density=0)
+    assert same(read_all(grids, (0,)), read_all(ref, (0,)))
+    b.close()
+    for g in grids + ref:
+        g.close()
