@@ -621,6 +621,25 @@ gvx_status gvx_update_apron_all(gvx_grid* g)
     return GVX_OK;
 }
 
+// test hook: a sort pass whose first tile never reports (bounded look-back, error status, usable context)
+gvx_status gvx_test_sort_withheld_tile(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in,
+                                       uint32_t* keys_out, uint32_t* vals_out, uint32_t n)
+{
+    GVX_GUARD(g);
+    if (!keys_in || !vals_in || !keys_out || !vals_out) {
+        gvx_set_error("test_sort_withheld_tile: null buffer");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(gvx_ensure(g->d_err, 64));
+    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));
+    gvx_status rc = gvx_sort_pass_withheld_tile(keys_in, vals_in, keys_out, vals_out, n, g->sort, g->stream,
+                                                g->d_err.as<uint32_t>(), &g->launches);
+    if (rc) return rc;
+    rc = gvx_check_device_error(g, "test_sort_withheld_tile");
+    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));  // the grid goes on with a clean error word
+    return rc;
+}
+
 gvx_status gvx_radix_sort(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                           uint32_t* vals_out, uint32_t n, int bits)
 {

@@ -112,6 +112,10 @@ struct SortScratch {
     DevBuf lookback;  // tiles * 256 status words
     DevBuf counter;   // tile counters, one per pass
 };
+// one sort pass with its first tile withheld: the bounded look-back times out (a test hook)
+gvx_status gvx_sort_pass_withheld_tile(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
+                                       uint32_t n, SortScratch& s, cudaStream_t st, uint32_t* d_err,
+                                       int64_t* launches);
 // Sorts (keys, vals) by the low `bits` bits of the keys, stable.  The keys
 // must already be in keys[0]/vals[0]; the result ends in buffer index *result
 // (0 or 1).  If the histogram of the pass digits was accumulated by the

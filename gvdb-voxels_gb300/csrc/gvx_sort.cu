@@ -246,3 +246,35 @@ gvx_status gvx_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], uint32_t n, int 
     *result = cur;
     return GVX_OK;
 }
+
+// One pass of the sort with its first tile withheld (a test of the bounded
+// look-back): the tile counter starts at 1 and tiles - 1 blocks run, so every
+// block takes a tile in range, and the tile after the withheld one waits for a
+// flag that nothing sets.  Its wait gives up after kSpinCycles and records
+// GVX_DERR_TIMEOUT; it then publishes the prefix it has (a lower bound of the
+// true one, so every scatter index stays below n) and the later tiles finish.
+gvx_status gvx_sort_pass_withheld_tile(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
+                                       uint32_t n, SortScratch& s, cudaStream_t st, uint32_t* d_err,
+                                       int64_t* launches)
+{
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    if (tiles < 2) {
+        gvx_set_error("sort test: %u keys make one tile; at least two are needed", n);
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(gvx_ensure(s.hist, 4 * 256 * sizeof(uint32_t)));
+    GVX_CK(gvx_ensure(s.base, 4 * 256 * sizeof(uint32_t)));
+    GVX_CK(gvx_ensure(s.lookback, (size_t)tiles * 256 * sizeof(uint32_t)));
+    GVX_CK(gvx_ensure(s.counter, 4 * sizeof(uint32_t)));
+    GVX_CK(cudaMemsetAsync(s.hist.p, 0, 4 * 256 * sizeof(uint32_t), st));
+    k_sort_hist<<<tiles < 1024 ? tiles : 1024, 256, 0, st>>>(kin, n, 1, s.hist.as<uint32_t>());
+    k_sort_bases<<<1, 256, 0, st>>>(s.hist.as<uint32_t>(), s.base.as<uint32_t>());
+    GVX_CK(cudaMemsetAsync(s.lookback.p, 0, (size_t)tiles * 256 * sizeof(uint32_t), st));
+    static const uint32_t one = 1u;
+    GVX_CK(cudaMemcpyAsync(s.counter.p, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+    k_onesweep<<<tiles - 1, kThreads, 0, st>>>(kin, vin, kout, vout, n, 0, s.base.as<uint32_t>(),
+                                               s.lookback.as<uint32_t>(), s.counter.as<uint32_t>(), d_err);
+    *launches += 3;
+    GVX_CK(cudaGetLastError());
+    return GVX_OK;
+}

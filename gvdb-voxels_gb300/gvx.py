@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "libgvx.so")
 OK = 0
 ERR_NAMES = {1: "INVALID_ARG", 2: "NOT_CONFIGURED", 3: "CAPACITY", 4: "DEVICE", 5: "TIMEOUT",
              6: "UNSUPPORTED", 7: "DEPTH", 8: "STATE", 9: "IO"}
+ERR_TIMEOUT = 5
 
 T_UCHAR, T_UCHAR4, T_FLOAT, T_FLOAT3, T_FLOAT4 = 0, 2, 3, 4, 5
 TOPO_AUTO, TOPO_FULL, TOPO_ACCUMULATE = 0, 1, 2
@@ -105,6 +106,7 @@ def load(path=None):
         "gvx_batch_splat": ([vp, i, f, i, i, i, i], i),
         "gvx_batch_get_tuning": ([vp, ip, ip, fp], i),
         "gvx_batch_topology": ([vp, f, i, i], i),
+        "gvx_test_sort_withheld_tile": ([vp, vp, vp, vp, vp, ctypes.c_uint32], i),
         "gvx_batch_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
     }
     for name, (args, res) in sig.items():

@@ -374,6 +374,14 @@ gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_
  * on the GPU.  Grids that share a stream still build one after another.  The
  * first failing grid's status is returned, its index in gvx_last_error(). */
 gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads);
+
+/* Test hook (no reference counterpart): one pass of the radix sort over n > 4096
+ * keys with its first tile withheld, so the decoupled look-back of the second
+ * tile waits for a flag that nothing sets.  The wait gives up after about two
+ * seconds and the call returns GVX_ERR_TIMEOUT; the outputs are undefined, and
+ * the grid and the CUDA context stay usable. */
+gvx_status gvx_test_sort_withheld_tile(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in,
+                                       uint32_t* keys_out, uint32_t* vals_out, uint32_t n);
 gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* count);
 
 #ifdef __cplusplus
