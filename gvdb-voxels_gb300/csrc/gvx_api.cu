@@ -21,6 +21,9 @@ void gvx_set_error(const char* fmt, ...)
 gvx_status gvx_cuda_fail(cudaError_t e, const char* what)
 {
     gvx_set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    // the runtime keeps the last error until it is read: read it here, so that a failure that
+    // leaves the context usable (an allocation) is not reported again by a later call's launch check
+    (void)cudaGetLastError();
     return GVX_ERR_DEVICE;
 }
 

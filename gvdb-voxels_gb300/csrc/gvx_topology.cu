@@ -1010,6 +1010,7 @@ gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
     uint32_t e = 0;
     GVX_CK(cudaMemcpyAsync(&e, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
     GVX_CK(cudaStreamSynchronize(g->stream));
+    if (e) GVX_CK(cudaMemsetAsync(g->d_err.p, 0, sizeof(uint32_t), g->stream));  // each error is reported once
     if (e & GVX_DERR_TIMEOUT) {
         gvx_set_error("%s: a device spin-wait timed out", stage);
         return GVX_ERR_TIMEOUT;
