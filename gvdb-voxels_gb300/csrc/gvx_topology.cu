@@ -383,40 +383,27 @@ __global__ void k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words, 
     }
 }
 
-__global__ void k_pfx_top(uint32_t* block_sums, uint32_t nblocks, uint32_t* total)
+template <bool POPC>
+__global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words,
+                            const uint32_t* __restrict__ block_sums, uint32_t* prefix, uint32_t* total)
 {
-    __shared__ uint32_t s_w[32];
-    __shared__ uint32_t s_carry;
-    if (threadIdx.x == 0) s_carry = 0u;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (uint32_t base = 0; base < nblocks; base += blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        const uint32_t v = i < nblocks ? block_sums[i] : 0u;
-        uint32_t x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) s_w[warp] = x;
+    __shared__ uint32_t s_w[kPfxThreads / 32];
+    __shared__ uint32_t s_off;
+    {
+        uint32_t o = 0u;
+        for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kPfxThreads) o += block_sums[i];
+        for (int k = 16; k > 0; k >>= 1) o += __shfl_xor_sync(0xFFFFFFFFu, o, k);
+        if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = o;
         __syncthreads();
-        uint32_t wp = 0u, tot = 0u;
-        for (int k = 0; k < nw; k++) {
-            if (k < warp) wp += s_w[k];
-            tot += s_w[k];
+        if (threadIdx.x == 0) {
+            uint32_t t = 0u;
+            for (int k = 0; k < kPfxThreads / 32; k++) t += s_w[k];
+            s_off = t;
+            if (total && blockIdx.x + 1 == gridDim.x) *total = t + block_sums[blockIdx.x];
         }
-        if (i < nblocks) block_sums[i] = s_carry + wp + x - v;
-        __syncthreads();
-        if (threadIdx.x == 0) s_carry += tot;
         __syncthreads();
     }
-    if (threadIdx.x == 0 && total) *total = s_carry;
-}
-
-template <bool POPC>
-__global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, const uint32_t* __restrict__ block_off,
-                            uint32_t* prefix)
-{
+    const uint32_t block_off = s_off;
     const uint32_t base = blockIdx.x * kPfxChunk + threadIdx.x * kPfxPerThread;
     uint32_t cnt[kPfxPerThread];
     uint32_t s = 0u;
@@ -432,10 +419,10 @@ __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words, c
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
         if (lane >= o) x += y;
     }
-    __shared__ uint32_t s_w[kPfxThreads / 32];
+    __syncthreads();  // s_w is reused
     if (lane == 31) s_w[warp] = x;
     __syncthreads();
-    uint32_t run = block_off[blockIdx.x] + x - s;
+    uint32_t run = block_off + x - s;
     for (int k = 0; k < warp; k++) run += s_w[k];
 #pragma unroll
     for (int k = 0; k < kPfxPerThread; k++) {
@@ -452,9 +439,8 @@ static gvx_status pfx_run(const uint32_t* in, uint32_t* out, uint32_t n, uint32_
     const uint32_t nb = std::max<uint32_t>(1u, (n + kPfxChunk - 1) / kPfxChunk);
     GVX_CK(gvx_ensure(tmp, (size_t)(nb + 1) * sizeof(uint32_t)));
     k_pfx_reduce<POPC><<<nb, kPfxThreads, 0, st>>>(in, n, tmp.as<uint32_t>());
-    k_pfx_top<<<1, 1024, 0, st>>>(tmp.as<uint32_t>(), nb, total);
-    k_pfx_apply<POPC><<<nb, kPfxThreads, 0, st>>>(in, n, tmp.as<uint32_t>(), out);
-    *launches += 3;
+    k_pfx_apply<POPC><<<nb, kPfxThreads, 0, st>>>(in, n, tmp.as<uint32_t>(), out, total);
+    *launches += 2;
     GVX_CK(cudaGetLastError());
     return GVX_OK;
 }
