@@ -234,23 +234,25 @@ __global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t
 __global__ void k_dilate(const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ count, KeySpace ks,
                          const uint32_t* __restrict__ masks, BitRank d0, uint32_t* x0bits, uint32_t* err)
 {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *count) return;
-    const uint32_t m = masks[j] & ~(1u << 13);
-    if (!m) return;
-    int c[3];
-    ks_unpack(ks, dlist[j], 0, c);
+    // grid-stride over the leaves (their count is on the device; the grid is sized for the points)
+    const uint32_t cnt = *count, stride = gridDim.x * blockDim.x;
     bool degen = false;
-    for (int b = 0; b < 27; b++) {
-        if (!((m >> b) & 1u)) continue;
-        const int nx = c[0] + (b % 3) - 1, ny = c[1] + (b / 3) % 3 - 1, nz = c[2] + b / 9 - 1;
-        if (nx < 0 || ny < 0 || nz < 0 || nx >= (1 << ks.bits[0]) || ny >= (1 << ks.bits[1]) ||
-            nz >= (1 << ks.bits[2])) {
-            degen = true;  // the reference descends outside the root here
-            continue;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += stride) {
+        const uint32_t m = masks[j] & ~(1u << 13);
+        if (!m) continue;
+        int c[3];
+        ks_unpack(ks, dlist[j], 0, c);
+        for (int b = 0; b < 27; b++) {
+            if (!((m >> b) & 1u)) continue;
+            const int nx = c[0] + (b % 3) - 1, ny = c[1] + (b / 3) % 3 - 1, nz = c[2] + b / 9 - 1;
+            if (nx < 0 || ny < 0 || nz < 0 || nx >= (1 << ks.bits[0]) || ny >= (1 << ks.bits[1]) ||
+                nz >= (1 << ks.bits[2])) {
+                degen = true;  // the reference descends outside the root here
+                continue;
+            }
+            const uint32_t nk = ks_pack(ks, nx, ny, nz, 0);
+            if (!br_test(d0, nk)) atomicOr(&x0bits[nk >> 5], 1u << (nk & 31));
         }
-        const uint32_t nk = ks_pack(ks, nx, ny, nz, 0);
-        if (!br_test(d0, nk)) atomicOr(&x0bits[nk >> 5], 1u << (nk & 31));
     }
     if (degen) atomicOr(err, GVX_DERR_DEGENERATE);
 }
@@ -266,16 +268,20 @@ struct UpperDesc {
 __global__ void k_upper_direct(const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ count, KeySpace ks,
                                UpperDesc ud, uint32_t* upper)
 {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = j < *count;
-    int c[3] = {0, 0, 0};
-    if (valid) ks_unpack(ks, dlist[j], 0, c);
-    for (int l = 1; l <= ud.nlev; l++) {
-        const int t = ud.tshift[l];
-        const uint32_t k = valid ? ks_pack(ks, c[0] >> t, c[1] >> t, c[2] >> t, t) : 0xFFFFFFFFu;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
-        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1)
-            atomicOr(&upper[ud.off[l] + (k >> 5)], 1u << (k & 31));
+    // grid-stride over the leaves in whole warps (the match_any below takes every lane)
+    const uint32_t cnt = *count, stride = gridDim.x * blockDim.x;
+    for (uint32_t j0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); j0 < cnt; j0 += stride) {
+        const uint32_t j = j0 + (threadIdx.x & 31u);
+        const bool valid = j < cnt;
+        int c[3] = {0, 0, 0};
+        if (valid) ks_unpack(ks, dlist[j], 0, c);
+        for (int l = 1; l <= ud.nlev; l++) {
+            const int t = ud.tshift[l];
+            const uint32_t k = valid ? ks_pack(ks, c[0] >> t, c[1] >> t, c[2] >> t, t) : 0xFFFFFFFFu;
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, k);
+            if (valid && (threadIdx.x & 31) == __ffs(peers) - 1)
+                atomicOr(&upper[ud.off[l] + (k >> 5)], 1u << (k & 31));
+        }
     }
 }
 
@@ -1202,7 +1208,7 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
         k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
                                                           g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
                                                           radius, 2.0f, b, g->masks.as<uint32_t>());
-        k_dilate<<<blocks_for(n, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks,
+        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks,
                                                      g->masks.as<uint32_t>(), d0, x0.bits, g->d_err.as<uint32_t>());
         g->launches += 2;
     }
@@ -1211,7 +1217,7 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
 
     // ---- upper levels: parents of D0 (direct) and of X0 (extra)
     if (ud.nlev > 0) {
-        k_upper_direct<<<blocks_for(n, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks, ud,
+        k_upper_direct<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks, ud,
                                                            g->upper.as<uint32_t>());
         k_upper_extra<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, words0, ks, ud, g->upper.as<uint32_t>());
         k_prefix_upper<<<2 * ud.nlev, 256, 0, st>>>(ud, g->upper.as<uint32_t>(), counts);
@@ -1524,12 +1530,12 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
         k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
                                                           g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
                                                           radius, 1.0f, b, g->masks.as<uint32_t>());
-        k_dilate<<<blocks_for(n, 256), 256, 0, st>>>(dlist, counts + kCntD0, ks, g->masks.as<uint32_t>(), d0,
+        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(dlist, counts + kCntD0, ks, g->masks.as<uint32_t>(), d0,
                                                      g->x0_bits.as<uint32_t>(), err);
         g->launches += 2;
     }
     if (ud.nlev > 0) {
-        k_upper_direct<<<blocks_for(n, 256), 256, 0, st>>>(dlist, counts + kCntD0, ks, ud, upper);
+        k_upper_direct<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(dlist, counts + kCntD0, ks, ud, upper);
         k_upper_extra<<<blocks_for(words0, 256), 256, 0, st>>>(g->x0_bits.as<uint32_t>(), words0, ks, ud, upper);
         g->launches += 2;
     }
