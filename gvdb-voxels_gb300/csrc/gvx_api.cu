@@ -202,6 +202,7 @@ gvx_status gvx_destroy(gvx_grid* g)
     gvx_host_tree_free(g);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
+    if (g->h_pin) cudaFreeHost(g->h_pin);
     if (g->ev_attr_free) cudaEventDestroy(g->ev_attr_free);
     if (g->ev_attr_ready) cudaEventDestroy(g->ev_attr_ready);
     delete g;

@@ -142,6 +142,7 @@ struct gvx_grid {
     DevBuf d_err, d_bbox;
     DevBuf d_rmax;  // float bits of the largest per-point radius of the last point permute
     DevBuf d_next;  // work-unit counter of the splat launch
+    void* h_pin = nullptr;  // pinned staging of the topology's small readbacks
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index

@@ -997,12 +997,11 @@ __global__ void k_delink_upper(GvxNode* nodes, uint32_t n, const uint64_t* __res
 
 static inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
-gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
+// decodes a device error word that was read back (and clears it on the device:
+// each error is reported once)
+static gvx_status report_device_error(gvx_grid* g, uint32_t e, const char* stage)
 {
-    uint32_t e = 0;
-    GVX_CK(cudaMemcpyAsync(&e, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
-    GVX_CK(cudaStreamSynchronize(g->stream));
-    if (e) GVX_CK(cudaMemsetAsync(g->d_err.p, 0, sizeof(uint32_t), g->stream));  // each error is reported once
+    if (e) GVX_CK(cudaMemsetAsync(g->d_err.p, 0, sizeof(uint32_t), g->stream));
     if (e & GVX_DERR_TIMEOUT) {
         gvx_set_error("%s: a device spin-wait timed out", stage);
         return GVX_ERR_TIMEOUT;
@@ -1020,6 +1019,32 @@ gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
         return GVX_ERR_UNSUPPORTED;
     }
     return GVX_OK;
+}
+
+gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
+{
+    uint32_t e = 0;
+    GVX_CK(cudaMemcpyAsync(&e, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    return report_device_error(g, e, stage);
+}
+
+// `bytes` (at most 256) of device memory and the device error word in one round
+// trip through pinned staging, then the error word reported as above
+static gvx_status readback_checked(gvx_grid* g, void* dst, const void* src, size_t bytes, const char* stage)
+{
+    if (bytes > 256) {
+        gvx_set_error("%s: readback of %zu bytes", stage, bytes);
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (!g->h_pin) GVX_CK(cudaMallocHost(&g->h_pin, 512));
+    GVX_CK(cudaMemcpyAsync(g->h_pin, src, bytes, cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaMemcpyAsync((char*)g->h_pin + 256, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GVX_CK(cudaStreamSynchronize(g->stream));
+    memcpy(dst, g->h_pin, bytes);
+    uint32_t e = 0;
+    memcpy(&e, (const char*)g->h_pin + 256, sizeof(e));
+    return report_device_error(g, e, stage);
 }
 
 static gvx_status ensure_grid_scratch(gvx_grid* g)
@@ -1227,9 +1252,7 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
 
     // ---- counts to the host (the one mid-build synchronisation)
     uint32_t hc[64];
-    GVX_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
-    GVX_CK(cudaStreamSynchronize(st));
-    rc = gvx_check_device_error(g, "RebuildTopology");
+    rc = readback_checked(g, hc, counts, sizeof(hc), "RebuildTopology");
     if (rc) return rc;
     const uint32_t U0 = hc[0], X0 = hc[1];
     uint32_t Ul[GVX_MAXLEV] = {}, Xl[GVX_MAXLEV] = {};
@@ -1422,9 +1445,10 @@ static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t 
     if (rc) return rc;
     if (read_used) {
         uint32_t used = 0;
-        GVX_CK(cudaMemcpyAsync(&used, counts + kCntActive, 4, cudaMemcpyDeviceToHost, st));
-        GVX_CK(cudaStreamSynchronize(st));
+        gvx_status rc = readback_checked(g, &used, counts + kCntActive, 4, "RebuildTopology");
+        if (rc) return rc;
         g->used_leaves = used;
+        return GVX_OK;
     }
     return gvx_check_device_error(g, "RebuildTopology");
 }
@@ -1582,9 +1606,7 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
 
     // ---- new-node counts to the host
     uint32_t hc[64];
-    GVX_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
-    GVX_CK(cudaStreamSynchronize(st));
-    rc = gvx_check_device_error(g, "RebuildTopology");
+    rc = readback_checked(g, hc, counts, sizeof(hc), "RebuildTopology");
     if (rc) return rc;
     uint32_t nnew[GVX_MAXLEV] = {};
     uint64_t total_new = 0;
@@ -1738,9 +1760,7 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
         g->launches++;
     }
     uint32_t hb[14];
-    GVX_CK(cudaMemcpyAsync(hb, g->d_bbox.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
-    GVX_CK(cudaStreamSynchronize(st));
-    rc = gvx_check_device_error(g, "GetBoundingBox");
+    rc = readback_checked(g, hb, g->d_bbox.p, sizeof(hb), "GetBoundingBox");
     if (rc) return rc;
     float mn[3], mx[3];
     int pmin[3], pmax[3];
