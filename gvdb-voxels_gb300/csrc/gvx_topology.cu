@@ -121,6 +121,7 @@ __global__ void k_bbox(const char* pos, int off, int stride, uint32_t n, float o
             }
         }
     }
+    // warp, then block, then one atomic per block and bound (6 addresses take every atomic)
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         for (int s = 16; s > 0; s >>= 1) {
@@ -128,11 +129,21 @@ __global__ void k_bbox(const char* pos, int off, int stride, uint32_t n, float o
             mx[a] = max(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], s));
         }
     }
-    if ((threadIdx.x & 31) == 0) {
+    __shared__ uint32_t s_b[32][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0)
         for (int a = 0; a < 3; a++) {
-            atomicMin(&out[a], mn[a]);
-            atomicMax(&out[3 + a], mx[a]);
+            s_b[wid][a] = mn[a];
+            s_b[wid][3 + a] = mx[a];
         }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        uint32_t v = s_b[0][threadIdx.x];
+        for (int w = 1; w < nw; w++) v = threadIdx.x < 3 ? min(v, s_b[w][threadIdx.x]) : max(v, s_b[w][threadIdx.x]);
+        if (threadIdx.x < 3)
+            atomicMin(&out[threadIdx.x], v);
+        else
+            atomicMax(&out[threadIdx.x], v);
     }
     if (nan) atomicOr(err, GVX_DERR_BADPOINT);
 }
@@ -743,7 +754,7 @@ __global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int
             mx[a] = nodes[i].pos[a] + range;
         }
     }
-    // one atomic per warp and bound
+    // warp, then block, then one atomic per block and bound
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         for (int s = 16; s > 0; s >>= 1) {
@@ -751,10 +762,21 @@ __global__ void k_leaf_bounds(const GvxNode* __restrict__ nodes, uint32_t n, int
             mx[a] = max(mx[a], __shfl_xor_sync(0xFFFFFFFFu, mx[a], s));
         }
     }
-    if ((threadIdx.x & 31) == 0 && mn[0] != INT_MAX) {
+    __shared__ int s_b[32][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0)
         for (int a = 0; a < 3; a++) {
-            atomicMin(&out[a], mn[a]);
-            atomicMax(&out[3 + a], mx[a]);
+            s_b[wid][a] = mn[a];
+            s_b[wid][3 + a] = mx[a];
+        }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int v = s_b[0][threadIdx.x];
+        for (int w = 1; w < nw; w++) v = threadIdx.x < 3 ? min(v, s_b[w][threadIdx.x]) : max(v, s_b[w][threadIdx.x]);
+        if (threadIdx.x < 3) {
+            if (v != INT_MAX) atomicMin(&out[threadIdx.x], v);
+        } else if (v != INT_MIN) {
+            atomicMax(&out[threadIdx.x], v);
         }
     }
 }
