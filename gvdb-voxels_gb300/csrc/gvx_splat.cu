@@ -82,7 +82,7 @@ __global__ void k_permute(const uint32_t* __restrict__ svals, uint32_t n, const 
         float r = i < n ? radius[svals[i]] : 0.0f;
         r = r != r ? 3.0e38f : fmaxf(r, 0.0f);
         const unsigned int m = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(r));
-        if ((threadIdx.x & 31) == 0 && m) atomicMax(rmax, m);
+        if ((threadIdx.x & 31) == 0 && m && m > *(volatile unsigned int*)rmax) atomicMax(rmax, m);
     }
     if (i >= n) return;
     const uint32_t j = svals[i];

@@ -674,7 +674,8 @@ __global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t
             }
             if (A.rmax) {
                 const unsigned int mm = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(rr));
-                if (lane == 0 && mm) atomicMax(A.rmax, mm);
+                // most warps find the maximum already there: read before the atomic
+                if (lane == 0 && mm && mm > *(volatile unsigned int*)A.rmax) atomicMax(A.rmax, mm);
             }
         }
 #pragma unroll
