@@ -324,19 +324,21 @@ __device__ __forceinline__ void deal_cells(unsigned char* tile, const float4 p, 
                 const float e2 = (r2h - (c1 - bv)) + (-syz - bv);
                 const float cl = e2 + r2l - ((ey + ez) + e1);
                 if (c1 + cl > 0.0f) {
+                    // the four voxels without branches (a slot outside the row or the support
+                    // is computed and masked), so that their independent chains interleave
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
-                        if (lx + k > xh) break;
                         const float dx = (float)(lx + k + Ox) - px;
                         const float t = fmaf(-dx, dx, c1) + cl;  // R^2 - d^2
-                        if (t <= 0.0f) continue;
                         const float d2 = fmaf(dx, dx, syz);
                         const float d = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
                         const float q = d * inv_h;
                         const float wi = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q < 1
                         const float uu = __fdividef(t, h * (R + d));               // 2 - q
-                        w[k] = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
-                        vm |= 1u << k;
+                        const float wk = norm * (q < 1.0f ? wi : 0.25f * uu * uu * uu);
+                        const bool ok = lx + k <= xh && t > 0.0f;
+                        w[k] = ok ? wk : 0.0f;
+                        vm |= ok ? 1u << k : 0u;
                     }
                 }
             }
