@@ -131,12 +131,24 @@ __global__ void k_pnode(const uint32_t* __restrict__ skeys, const uint32_t* __re
     pnode[svals[i]] = leaf;
 }
 
-// the grid's stream waits for attribute uploads still in flight on the side stream
+// the grid's stream waits for the uploads of the last commit still in flight on the
+// side stream: all of them (the attributes are copied after the positions) ...
 gvx_status gvx_wait_attributes(gvx_grid* g)
 {
     if (g->attr_pending) {
         GVX_CK(cudaStreamWaitEvent(g->stream, g->ev_attr_ready, 0));
         g->attr_pending = false;
+        g->pos_pending = false;
+    }
+    return GVX_OK;
+}
+
+// ... or the positions alone (what the topology build and the subcell lists read)
+gvx_status gvx_wait_positions(gvx_grid* g)
+{
+    if (g->pos_pending) {
+        GVX_CK(cudaStreamWaitEvent(g->stream, g->ev_pos_ready, 0));
+        g->pos_pending = false;
     }
     return GVX_OK;
 }
@@ -184,8 +196,8 @@ gvx_status gvx_destroy(gvx_grid* g)
     if (g->aux_stream) cudaStreamSynchronize(g->aux_stream);
     DevBuf* bufs[] = {&g->bm_a, &g->bm_a_prefix, &g->bm_b, &g->bm_b_prefix, &g->remap, &g->leaf_key, &g->leaf_range,
                       &g->leaf_oct,
-                      &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos, &g->own_vel, &g->own_w,
-                      &g->own_r, &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
+                      &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos[0], &g->own_vel[0], &g->own_w[0],
+                      &g->own_r[0], &g->own_pos[1], &g->own_vel[1], &g->own_w[1], &g->own_r[1], &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
                       &g->d_counts, &g->d_err, &g->d_bbox, &g->d_rmax, &g->d_next, &g->host_stage, &g->api_keys[0],
@@ -203,7 +215,9 @@ gvx_status gvx_destroy(gvx_grid* g)
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
     if (g->h_pin) cudaFreeHost(g->h_pin);
-    if (g->ev_attr_free) cudaEventDestroy(g->ev_attr_free);
+    for (int k = 0; k < 2; k++)
+        if (g->ev_set_free[k]) cudaEventDestroy(g->ev_set_free[k]);
+    if (g->ev_pos_ready) cudaEventDestroy(g->ev_pos_ready);
     if (g->ev_attr_ready) cudaEventDestroy(g->ev_attr_ready);
     delete g;
     return GVX_OK;
@@ -413,12 +427,11 @@ __global__ void k_pack_float3(const unsigned char* __restrict__ src, int stride,
 
 // one host -> device copy of n float3 records with a byte stride: packed records in one flat copy;
 // strided ones as the raw bytes, packed by a kernel (a 2D copy of 12-byte rows is one DMA row a point)
-static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int stride, int n,
-                                cudaStream_t st = nullptr)
+static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int stride, int n, cudaStream_t st)
 {
     GVX_CK(gvx_ensure(dst, (size_t)n * 12));
     if (stride == 12) {
-        GVX_CK(cudaMemcpyAsync(dst.p, src, (size_t)n * 12, cudaMemcpyHostToDevice, st ? st : g->stream));
+        GVX_CK(cudaMemcpyAsync(dst.p, src, (size_t)n * 12, cudaMemcpyHostToDevice, st));
         return GVX_OK;
     }
     if (stride & 3) {
@@ -426,8 +439,8 @@ static gvx_status upload_float3(gvx_grid* g, DevBuf& dst, const void* src, int s
         return GVX_ERR_INVALID_ARG;
     }
     GVX_CK(gvx_ensure(g->own_stage, (size_t)n * stride));
-    GVX_CK(cudaMemcpyAsync(g->own_stage.p, src, (size_t)(n - 1) * stride + 12, cudaMemcpyHostToDevice, g->stream));
-    k_pack_float3<<<std::min<unsigned>((unsigned)((n + 255) / 256), 152u * 16u), 256, 0, g->stream>>>(
+    GVX_CK(cudaMemcpyAsync(g->own_stage.p, src, (size_t)(n - 1) * stride + 12, cudaMemcpyHostToDevice, st));
+    k_pack_float3<<<std::min<unsigned>((unsigned)((n + 255) / 256), 152u * 16u), 256, 0, st>>>(
         g->own_stage.as<unsigned char>(), stride, (uint32_t)n, dst.as<float>());
     g->launches++;
     GVX_CK(cudaGetLastError());
@@ -442,44 +455,47 @@ gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_s
         gvx_set_error("CommitData: invalid host points");
         return GVX_ERR_INVALID_ARG;
     }
-    gvx_status rc0 = upload_float3(g, g->own_pos, pos, pos_stride, n);
-    if (rc0) return rc0;
-    // The attributes (packed velocities, weights, radii) go up on the side stream, so that their
-    // copies overlap the topology build, which needs only positions.  The side stream first waits
-    // for the work already queued on the grid's stream (earlier readers of these buffers); the
-    // point permute waits for the copies (gvx_wait_attributes).  Strided velocities share the
-    // staging buffer with the positions and stay on the grid's stream.
-    const bool side = (vel && vel_stride == 12) || weight || radius;
-    cudaStream_t as = g->stream;
-    if (side) {
-        if (!g->aux_stream) {
-            GVX_CK(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
-            GVX_CK(cudaEventCreateWithFlags(&g->ev_attr_free, cudaEventDisableTiming));
-            GVX_CK(cudaEventCreateWithFlags(&g->ev_attr_ready, cudaEventDisableTiming));
-        }
-        GVX_CK(cudaEventRecord(g->ev_attr_free, g->stream));
-        GVX_CK(cudaStreamWaitEvent(g->aux_stream, g->ev_attr_free, 0));
-        as = g->aux_stream;
+    // Two sets of library-owned point buffers, filled in turn: this call fills the set the
+    // previous call did not, on the side stream, after the work that was queued before the
+    // previous call (the last work that read this set).  Its copies therefore overlap the work
+    // queued since (a previous frame), and the calls that read points make the grid's stream
+    // wait for them: the topology build and the subcell lists for the positions, the point
+    // permute for everything (gvx_wait_positions, gvx_wait_attributes).
+    if (!g->aux_stream) {
+        GVX_CK(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) GVX_CK(cudaEventCreateWithFlags(&g->ev_set_free[k], cudaEventDisableTiming));
+        GVX_CK(cudaEventCreateWithFlags(&g->ev_pos_ready, cudaEventDisableTiming));
+        GVX_CK(cudaEventCreateWithFlags(&g->ev_attr_ready, cudaEventDisableTiming));
     }
+    const int cur = g->own_set, nxt = cur ^ 1;
+    GVX_CK(cudaEventRecord(g->ev_set_free[cur], g->stream));  // everything queued so far reads set `cur`
+    if (g->own_set_used[nxt]) GVX_CK(cudaStreamWaitEvent(g->aux_stream, g->ev_set_free[nxt], 0));
+    cudaStream_t as = g->aux_stream;
+    gvx_status rc0 = upload_float3(g, g->own_pos[nxt], pos, pos_stride, n, as);
+    if (rc0) return rc0;
+    GVX_CK(cudaEventRecord(g->ev_pos_ready, as));
     if (vel) {
-        rc0 = upload_float3(g, g->own_vel, vel, vel_stride, n, vel_stride == 12 ? as : g->stream);
+        rc0 = upload_float3(g, g->own_vel[nxt], vel, vel_stride, n, as);
         if (rc0) return rc0;
     }
     if (weight) {
-        GVX_CK(gvx_ensure(g->own_w, (size_t)n * 4));
-        GVX_CK(cudaMemcpyAsync(g->own_w.p, weight, (size_t)n * 4, cudaMemcpyHostToDevice, as));
+        GVX_CK(gvx_ensure(g->own_w[nxt], (size_t)n * 4));
+        GVX_CK(cudaMemcpyAsync(g->own_w[nxt].p, weight, (size_t)n * 4, cudaMemcpyHostToDevice, as));
     }
     if (radius) {
-        GVX_CK(gvx_ensure(g->own_r, (size_t)n * 4));
-        GVX_CK(cudaMemcpyAsync(g->own_r.p, radius, (size_t)n * 4, cudaMemcpyHostToDevice, as));
+        GVX_CK(gvx_ensure(g->own_r[nxt], (size_t)n * 4));
+        GVX_CK(cudaMemcpyAsync(g->own_r[nxt].p, radius, (size_t)n * 4, cudaMemcpyHostToDevice, as));
     }
-    if (side) {
-        GVX_CK(cudaEventRecord(g->ev_attr_ready, g->aux_stream));
-        g->attr_pending = true;
-    }
-    gvx_status rc = gvx_set_points(g, n, g->own_pos.p, 0, 12, vel ? g->own_vel.p : nullptr, 0, 12, nullptr, 0, 0);
+    GVX_CK(cudaEventRecord(g->ev_attr_ready, as));
+    g->pos_pending = true;
+    g->attr_pending = true;
+    g->own_set = nxt;
+    g->own_set_used[nxt] = true;
+    gvx_status rc = gvx_set_points(g, n, g->own_pos[nxt].p, 0, 12, vel ? g->own_vel[nxt].p : nullptr, 0, 12, nullptr,
+                                   0, 0);
     if (rc) return rc;
-    return gvx_set_point_attribs(g, weight ? g->own_w.as<float>() : nullptr, radius ? g->own_r.as<float>() : nullptr);
+    return gvx_set_point_attribs(g, weight ? g->own_w[nxt].as<float>() : nullptr,
+                                 radius ? g->own_r[nxt].as<float>() : nullptr);
 }
 
 gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
@@ -489,7 +505,9 @@ gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float or
         gvx_set_error("RebuildTopology: mode %d", mode);
         return GVX_ERR_INVALID_ARG;
     }
-    gvx_status rc = gvx_topo_rebuild(g, n, radius, orig, mode, min_depth);
+    gvx_status rc = gvx_wait_positions(g);
+    if (rc) return rc;
+    rc = gvx_topo_rebuild(g, n, radius, orig, mode, min_depth);
     // the topology build is queued: from here the grid's stream also covers the attribute uploads
     gvx_status rw = gvx_wait_attributes(g);
     return rc ? rc : rw;

@@ -506,12 +506,20 @@ extern "C" {
 
 gvx_status gvx_insert_points_subcell(gvx_grid* g, int subcell, int n, float radius, const float trans[3], int* sc_len)
 {
+    if (g) {
+        gvx_status rc = gvx_wait_positions(g);
+        if (rc) return rc;
+    }
     return insert_subcell(g, subcell, n, radius, trans, sc_len, false);
 }
 
 gvx_status gvx_insert_points_subcell_fp16(gvx_grid* g, int subcell, int n, float radius, const float trans[3],
                                           int* sc_len)
 {
+    if (g) {
+        gvx_status rc = gvx_wait_positions(g);
+        if (rc) return rc;
+    }
     return insert_subcell(g, subcell, n, radius, trans, sc_len, true);
 }
 

@@ -58,8 +58,9 @@ struct gvx_grid {
     // host uploads of the point attributes run on a side stream, overlapping the topology
     // build; the point permute, the only device reader of them, waits for ev_attr_ready
     cudaStream_t aux_stream = nullptr;
-    cudaEvent_t ev_attr_free = nullptr, ev_attr_ready = nullptr;
-    bool attr_pending = false;
+    cudaEvent_t ev_set_free[2] = {nullptr, nullptr};  // the work queued before a set was last replaced
+    cudaEvent_t ev_pos_ready = nullptr, ev_attr_ready = nullptr;
+    bool pos_pending = false, attr_pending = false;
 
     // configuration (Configure)
     bool configured = false;
@@ -116,7 +117,11 @@ struct gvx_grid {
 
     // points
     GvxPoints pts;
-    DevBuf own_pos, own_vel, own_w, own_r;  // storage of gvx_commit_points_host
+    // storage of gvx_commit_points_host: two sets, filled in turn, so that a commit's copies
+    // overlap the work still reading the other set
+    DevBuf own_pos[2], own_vel[2], own_w[2], own_r[2];
+    int own_set = 0;
+    bool own_set_used[2] = {false, false};
     DevBuf own_stage;                       // strided host records as copied, before packing
 
     // grouping of points by leaf (sorted order)
@@ -192,6 +197,7 @@ struct GvxSortedAttr {
 };
 gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr);
 gvx_status gvx_wait_attributes(gvx_grid* g);
+gvx_status gvx_wait_positions(gvx_grid* g);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
 // InsertPoints: grouping + sorted attribute arrays

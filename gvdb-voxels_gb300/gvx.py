@@ -146,7 +146,7 @@ class Grid:
         self.h = h
         self.device = device
         self._types = {}
-        self._keep = []
+        self._keep = (None, None)
 
     def _check(self, st):
         if st != OK:
@@ -205,7 +205,9 @@ class Grid:
         weight = None if weight is None else np.ascontiguousarray(weight, dtype=np.float32)
         radius = None if radius is None else np.ascontiguousarray(radius, dtype=np.float32)
         arrs += [a for a in (vel, weight, radius) if a is not None]
-        self._keep = arrs
+        # the copies run asynchronously into one of two device buffer sets: hold the arrays of
+        # the last two commits
+        self._keep = (arrs, self._keep[0])
         n = pos.shape[0]
         self._check(self.lib.gvx_commit_points_host(self.h, n, _ptr(pos), pos.strides[0], _ptr(vel),
                                                     vel.strides[0] if vel is not None else 0, _ptr(weight),

@@ -120,8 +120,11 @@ gvx_status gvx_set_point_attribs(gvx_grid* g, const float* weight, const float* 
  * as by gvx_set_points.  Strides are in bytes.  The copies are asynchronous:
  * the host arrays may be reused once the grid's stream has passed the next call
  * that takes points (gvx_rebuild_topology, gvx_insert_points, a splat), or after
- * gvx_sync.  (The attribute copies run on a side stream beside the topology
- * build; those calls make the grid's stream wait for them.) */
+ * gvx_sync.  (The copies run on a side stream into one of two buffer sets, filled
+ * in turn, after the work queued before the previous commit: a commit issued
+ * while the previous frame still runs overlaps it.  Those calls, and
+ * gvx_insert_points_subcell for the positions, make the grid's stream wait for
+ * the copies.) */
 gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_stride,
                                   const void* vel, int vel_stride, const float* weight,
                                   const float* radius);
