@@ -112,30 +112,48 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """start sampling every 50 ms and wait (up to 10 s) for the first sample, so that the
+        sampler is live when the timed region begins"""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
                 text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except Exception:
             self.proc = None
+            return
+        t_end = time.perf_counter() + 10.0
+        while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """the samples taken from 0.1 s before the timed region [t0, t1] to 0.1 s after it (the
+        region of a short run is shorter than the sampling period: the samples that bracket it),
+        after waiting (up to 2 s) for one taken after t1"""
         if not self.proc:
             return None
+        if t1 is not None:
+            t_end = time.perf_counter() + 2.0
+            while time.perf_counter() < t_end and self.proc.poll() is None and \
+                    not any(t > t1 for t, _ in self.lines):
+                time.sleep(0.01)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        lines = list(self.lines)
+        if t0 is not None and t1 is not None:
+            window = [(t, ln) for t, ln in lines if t0 - 0.1 <= t <= t1 + 0.1]
+            lines = window or lines
         sm, mx, reasons = [], 0, set()
-        for ln in self.lines:
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 3:
                 continue
@@ -288,9 +306,10 @@ def run_ours(args, rank, world, pool):
             step(args.warmup + k, sp[k])
             ends[k].record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        wall = t1 - t0
         launches = g.kernel_launches() - launches0
-        clk = clocks.stop()
+        clk = clocks.stop(t0, t1)
         if dist:
             dist.barrier()
         step_ms = [starts[k].elapsed_time(ends[k]) for k in range(args.steps)]
