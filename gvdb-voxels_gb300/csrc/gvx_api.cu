@@ -196,8 +196,9 @@ gvx_status gvx_destroy(gvx_grid* g)
     if (g->aux_stream) cudaStreamSynchronize(g->aux_stream);
     DevBuf* bufs[] = {&g->bm_a, &g->bm_a_prefix, &g->bm_b, &g->bm_b_prefix, &g->remap, &g->leaf_key, &g->leaf_range,
                       &g->leaf_oct,
-                      &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos[0], &g->own_vel[0], &g->own_w[0],
-                      &g->own_r[0], &g->own_pos[1], &g->own_vel[1], &g->own_w[1], &g->own_r[1], &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
+                      &g->leaf_slot, &g->slot_leaf, &g->nbr, &g->amap, &g->own_pos[0], &g->own_vel[0],
+                      &g->own_w[0], &g->own_r[0], &g->own_pos[1], &g->own_vel[1], &g->own_w[1], &g->own_r[1],
+                      &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
                       &g->d_counts, &g->d_err, &g->d_bbox, &g->d_rmax, &g->d_next, &g->host_stage, &g->api_keys[0],
