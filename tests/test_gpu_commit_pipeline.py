@@ -60,7 +60,7 @@ def assert_same(a, b, k):
         assert np.array_equal(a[c].view(np.uint32), b[c].view(np.uint32)), "frame %d channel %d" % (k, c - 2)
 
 
-def commit_pinned(g, host, k, strided):
+def commit_pinned(g, host, k):
     pos, vel, w = host[k]
     lib = g.lib
     n = pos.shape[0]
@@ -69,12 +69,9 @@ def commit_pinned(g, host, k, strided):
     g._check(st)
 
 
-def test_pipelined_commits_match_fresh_frames(gvx_mod):
+def pinned_frames(fr, n, strided_frame):
     import torch
 
-    n = 300_000
-    fr = frames(4, n, seed=11)
-    strided_frame = 2
     host = []
     for k, (pos, vel, w) in enumerate(fr):
         if k == strided_frame:  # float4 records, the fourth float ignored
@@ -89,7 +86,10 @@ def test_pipelined_commits_match_fresh_frames(gvx_mod):
         ww = torch.empty(n, dtype=torch.float32, pin_memory=True)
         ww.copy_(torch.from_numpy(w))
         host.append((p, v, ww))
+    return host
 
+
+def fresh_results(gvx_mod, fr, n):
     expect = []
     for pos, vel, w in fr:
         f = new_grid(gvx_mod)
@@ -97,14 +97,23 @@ def test_pipelined_commits_match_fresh_frames(gvx_mod):
         run_frame(f, gvx_mod, n)
         expect.append(results(f))
         f.close()
+    return expect
+
+
+def test_pipelined_commits_match_fresh_frames(gvx_mod):
+    n = 300_000
+    fr = frames(4, n, seed=11)
+    strided_frame = 2
+    host = pinned_frames(fr, n, strided_frame)
+    expect = fresh_results(gvx_mod, fr, n)
 
     # pipelined: frame k+1 committed after frame k's work is queued, before its readback
     g = new_grid(gvx_mod)
-    commit_pinned(g, host, 0, False)
+    commit_pinned(g, host, 0)
     for k in range(len(fr)):
         run_frame(g, gvx_mod, n)
         if k + 1 < len(fr):
-            commit_pinned(g, host, k + 1, k + 1 == strided_frame)
+            commit_pinned(g, host, k + 1)
         assert_same(results(g), expect[k], k)
     g.close()
 
@@ -112,7 +121,29 @@ def test_pipelined_commits_match_fresh_frames(gvx_mod):
     g = new_grid(gvx_mod)
     for rep in range(2):
         for k in range(len(fr)):
-            commit_pinned(g, host, k, k == strided_frame)
+            commit_pinned(g, host, k)
             run_frame(g, gvx_mod, n)
+            assert_same(results(g), expect[k], k)
+    g.close()
+
+
+def test_pipelined_commits_on_a_caller_stream(gvx_mod):
+    """the same pipelined order with the grid on a caller's stream (gvx_set_stream): the
+    buffer-set events are recorded on that stream"""
+    import torch
+
+    n = 200_000
+    fr = frames(3, n, seed=12)
+    host = pinned_frames(fr, n, -1)
+    expect = fresh_results(gvx_mod, fr, n)
+    s = torch.cuda.Stream()
+    g = new_grid(gvx_mod)
+    g.set_stream(s.cuda_stream)
+    for rep in range(2):
+        commit_pinned(g, host, 0)
+        for k in range(len(fr)):
+            run_frame(g, gvx_mod, n)
+            if k + 1 < len(fr):
+                commit_pinned(g, host, k + 1)
             assert_same(results(g), expect[k], k)
     g.close()
