@@ -169,13 +169,11 @@ void VolumeGVDB::ClearChannel(uchar chan)
 
 // FinishTopology (VG.cpp:1579-1593): space activated on the host is committed
 // to the device (whatever pCommitPool says: the device pools are the tree);
-// the bounds of the active leaves
+// ComputeBounds when pComputeBounds
 void VolumeGVDB::FinishTopology(bool pCommitPool, bool pComputeBounds)
 {
-    (void)pCommitPool;
-    (void)pComputeBounds;
     need_grid();
-    check(gvx_finish_topology(g_));
+    check(gvx_finish_topology_ex(g_, pCommitPool ? 1 : 0, pComputeBounds ? 1 : 0));
     topology_changed();
 }
 
@@ -672,6 +670,22 @@ Vector3DF VolumeGVDB::getWorldMax()
     gvx_info inf;
     check(gvx_get_info(g_, &inf));
     return Vector3DF(inf.obj_max[0], inf.obj_max[1], inf.obj_max[2]);
+}
+
+Vector3DF VolumeGVDB::getVoxRes()
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    return Vector3DF(inf.vox_res[0], inf.vox_res[1], inf.vox_res[2]);
+}
+
+Vector3DF VolumeGVDB::getVoxResMax()
+{
+    need_grid();
+    gvx_info inf;
+    check(gvx_get_info(g_, &inf));
+    return Vector3DF(inf.vox_res_max[0], inf.vox_res_max[1], inf.vox_res_max[2]);
 }
 
 void VolumeGVDB::Splat(int mode, int num_pnts, float radius, Vector3DF trans, int chanDensity, int chanVel,

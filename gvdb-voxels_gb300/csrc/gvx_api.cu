@@ -273,6 +273,9 @@ gvx_status gvx_configure(gvx_grid* g, int levels, const int* logdim, const int* 
     g->configured = true;
     g->topo_gen++;
     g->root_level = -1;
+    g->vox_res_max_reset = true;  // VG.cpp:2428
+    g->bounds_pending = false;
+    for (int a = 0; a < 3; a++) g->obj_min[a] = g->obj_max[a] = g->vox_res_max[a] = 0.f;
     g->rebuild_topo = true;
     g->curr_depth = -1;
     g->lookup_valid = g->group_valid = g->atlas_valid = g->nbr_valid = false;
@@ -521,13 +524,16 @@ gvx_status gvx_request_full_rebuild(gvx_grid* g, int on)
     return GVX_OK;
 }
 
-gvx_status gvx_finish_topology(gvx_grid* g)
+gvx_status gvx_finish_topology_ex(gvx_grid* g, int commit_pool, int compute_bounds)
 {
     GVX_GUARD(g);
+    (void)commit_pool;  // the device pools are the tree: space activated on the host is always committed
     gvx_status rc = gvx_host_tree_commit(g);  // pools grown by ActivateSpace go to the device
     if (rc) return rc;
-    return gvx_topo_compute_bounds(g);
+    return compute_bounds ? gvx_topo_compute_bounds(g) : GVX_OK;
 }
+
+gvx_status gvx_finish_topology(gvx_grid* g) { return gvx_finish_topology_ex(g, 1, 1); }
 
 gvx_status gvx_clear(gvx_grid* g)
 {
@@ -731,6 +737,8 @@ gvx_status gvx_get_info(gvx_grid* g, gvx_info* out)
         out->bbox_max[a] = g->bbox_max[a];
         out->obj_min[a] = g->obj_min[a];
         out->obj_max[a] = g->obj_max[a];
+        out->vox_res[a] = g->obj_max[a] - g->obj_min[a];
+        out->vox_res_max[a] = g->vox_res_max[a];
     }
     int nch = 0;
     for (int c = 0; c < GVX_MAXCH; c++) nch += g->ch[c].used;

@@ -85,7 +85,9 @@ struct gvx_grid {
     DevBuf clist[GVX_MAXLEV];
     float bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
     float obj_min[3] = {0, 0, 0}, obj_max[3] = {0, 0, 0};
+    float vox_res_max[3] = {0, 0, 0};  // mVoxResMax (sticky since Configure)
     bool bounds_pending = false;
+    bool vox_res_max_reset = true;     // the next ComputeBounds zeroes mVoxResMax first
 
     // lookup of leaves by key for the current topology
     LeafLookup lookup{};

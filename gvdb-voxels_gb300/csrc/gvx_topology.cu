@@ -1969,8 +1969,30 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     return GVX_OK;
 }
 
-// ComputeBounds runs on the device; the 24-byte result is read when the host
-// asks for it (gvx_get_info), so FinishTopology adds no synchronisation
+// ComputeBounds (VG.cpp:1792-1816) runs on the device: min and max both start
+// at level-0 pool node 0's position whatever its flags (a delinked node 0
+// still seeds them), then the active leaves lower the minimum to their
+// positions and raise the maximum to position + range.  mVoxResMax (the
+// largest max - min per axis since Configure) is kept on the device beside
+// them.  The result is read when the host asks for it (gvx_get_info), so
+// FinishTopology adds no synchronisation.  host_stage: ints [0..2] min,
+// [3..5] max, [6..8] res max.
+__global__ void k_bounds_seed(const GvxNode* __restrict__ nodes, uint32_t n, int* out, int reset_res_max)
+{
+    const int a = threadIdx.x;
+    if (a < 3) {
+        out[a] = n ? nodes[0].pos[a] : 0x7FFFFFFF;
+        out[3 + a] = n ? nodes[0].pos[a] : (int)0x80000000;
+        if (reset_res_max) out[6 + a] = 0;
+    }
+}
+
+__global__ void k_bounds_res_max(int* out, uint32_t n)
+{
+    const int a = threadIdx.x;
+    if (a < 3 && n) out[6 + a] = max(out[6 + a], out[3 + a] - out[a]);
+}
+
 gvx_status gvx_topo_compute_bounds(gvx_grid* g)
 {
     if (g->root_level < 0) return GVX_OK;
@@ -1978,12 +2000,15 @@ gvx_status gvx_topo_compute_bounds(gvx_grid* g)
     if (rc) return rc;
     const uint32_t L0 = (uint32_t)g->count[0];
     GVX_CK(gvx_ensure(g->host_stage, 64));
-    k_bounds_init<<<1, 32, 0, g->stream>>>(g->host_stage.as<int>());
+    k_bounds_seed<<<1, 32, 0, g->stream>>>(g->nodes[0].as<GvxNode>(), L0, g->host_stage.as<int>(),
+                                          g->vox_res_max_reset ? 1 : 0);
     g->launches++;
+    g->vox_res_max_reset = false;
     if (L0) {
         k_leaf_bounds<<<blocks_for(L0, 256), 256, 0, g->stream>>>(g->nodes[0].as<GvxNode>(), L0, g->range[0],
                                                                    g->host_stage.as<int>());
-        g->launches++;
+        k_bounds_res_max<<<1, 32, 0, g->stream>>>(g->host_stage.as<int>(), L0);
+        g->launches += 2;
     }
     GVX_CK(cudaGetLastError());
     g->bounds_pending = true;
@@ -1993,13 +2018,14 @@ gvx_status gvx_topo_compute_bounds(gvx_grid* g)
 gvx_status gvx_topo_read_bounds(gvx_grid* g)
 {
     if (!g->bounds_pending) return GVX_OK;
-    int hb[6];
+    int hb[9];
     GVX_CK(cudaMemcpyAsync(hb, g->host_stage.p, sizeof(hb), cudaMemcpyDeviceToHost, g->stream));
     GVX_CK(cudaStreamSynchronize(g->stream));
     const bool any = g->count[0] > 0;
     for (int a = 0; a < 3; a++) {
         g->obj_min[a] = any ? (float)hb[a] : 0.f;
         g->obj_max[a] = any ? (float)hb[3 + a] : 0.f;
+        g->vox_res_max[a] = (float)hb[6 + a];
     }
     g->bounds_pending = false;
     return GVX_OK;

@@ -44,7 +44,8 @@ class Info(ctypes.Structure):
                 ("node_count", ctypes.c_int64 * 10), ("used_leaves", ctypes.c_int64),
                 ("atlas_subdim", ctypes.c_int * 3), ("atlas_res", ctypes.c_int * 3), ("channels", ctypes.c_int),
                 ("last_rebuild", ctypes.c_int), ("root_pos", ctypes.c_int * 3), ("bbox_min", ctypes.c_float * 3),
-                ("bbox_max", ctypes.c_float * 3), ("obj_min", ctypes.c_float * 3), ("obj_max", ctypes.c_float * 3)]
+                ("bbox_max", ctypes.c_float * 3), ("obj_min", ctypes.c_float * 3), ("obj_max", ctypes.c_float * 3),
+                ("vox_res", ctypes.c_float * 3), ("vox_res_max", ctypes.c_float * 3)]
 
 
 _lib = None
@@ -73,7 +74,7 @@ def load(path=None):
         "gvx_set_point_attribs": ([vp, vp, vp], i),
         "gvx_commit_points_host": ([vp, i, vp, i, vp, i, vp, vp], i),
         "gvx_rebuild_topology": ([vp, i, f, fp, i, i], i), "gvx_request_full_rebuild": ([vp, i], i),
-        "gvx_finish_topology": ([vp], i), "gvx_update_atlas": ([vp], i),
+        "gvx_finish_topology": ([vp], i), "gvx_finish_topology_ex": ([vp, i, i], i), "gvx_update_atlas": ([vp], i),
         "gvx_insert_points": ([vp, i, fp, vp], i),
         "gvx_scatter_density": ([vp, i, f, f, fp, i, i], i),
         "gvx_insert_points_subcell": ([vp, i, i, f, fp, ip], i),
@@ -101,6 +102,8 @@ def load(path=None):
         "gvx_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
         "gvx_radix_sort": ([vp, vp, vp, vp, vp, ctypes.c_uint32, i], i),
         "gvx_radix_sort_noalloc": ([vp, vp, vp, vp, ctypes.c_uint32, i, vp], i),
+        "gvx_radix_sort_noalloc_status": ([vp], i),
+        "gvx_test_sort_noalloc_withheld_tile": ([vp, vp, vp, vp, ctypes.c_uint32, vp], i),
         "gvx_batch_create": ([i, ctypes.POINTER(vp)], i), "gvx_batch_destroy": ([vp], i),
         "gvx_batch_set_stream": ([vp, vp], i), "gvx_batch_set_grids": ([vp, ctypes.POINTER(vp), i], i),
         "gvx_batch_splat": ([vp, i, f, i, i, i, i], i),
@@ -221,8 +224,8 @@ class Grid:
     def request_full_rebuild(self, on=True):
         self._check(self.lib.gvx_request_full_rebuild(self.h, int(on)))
 
-    def finish_topology(self):
-        self._check(self.lib.gvx_finish_topology(self.h))
+    def finish_topology(self, commit_pool=True, compute_bounds=True):
+        self._check(self.lib.gvx_finish_topology_ex(self.h, int(commit_pool), int(compute_bounds)))
 
     def update_atlas(self):
         self._check(self.lib.gvx_update_atlas(self.h))
@@ -367,6 +370,21 @@ class Grid:
         self._check(self.lib.gvx_read_channel(self.h, chan, _ptr(out), nbytes))
         shp = (-1, P, P, P) + ((nc,) if nc > 1 else ())
         return out.reshape(shp)
+
+    def read_slots(self, chan, slots):
+        """the bricks of the given atlas slots, (len(slots), P, P, P[, ncomp]),
+        copied slot by slot (a sample of a channel too large to read whole)"""
+        inf = self.info()
+        P = inf["brick_res"] + 2 * inf["apron"]
+        dt, nc = _ELEM[self._types[chan]]
+        ptr, nbytes = self.channel_device_ptr(chan)
+        per = P * P * P * nc * np.dtype(dt).itemsize
+        out = np.zeros((len(slots), P, P, P) + ((nc,) if nc > 1 else ()), dt)
+        for k, s in enumerate(np.asarray(slots, np.int64)):
+            if s < 0 or (s + 1) * per > nbytes:
+                raise ValueError("slot %d outside channel %d" % (s, chan))
+            self._check(self.lib.gvx_memcpy(self.device, _ptr(out[k]), ctypes.c_void_p(ptr + int(s) * per), per, 1))
+        return out
 
     def read_channel_dense(self, chan):
         """the reference's 3D-array layout: (Z, Y, X[, ncomp])"""

@@ -80,8 +80,10 @@ typedef struct gvx_info {
     int root_pos[3];
     float bbox_min[3];     /* getBoundMin(), posMin after GetBoundingBox */
     float bbox_max[3];
-    float obj_min[3];      /* ComputeBounds result */
-    float obj_max[3];
+    float obj_min[3];      /* ComputeBounds (VG.cpp:1792-1816) of the last FinishTopology: */
+    float obj_max[3];      /*   mObjMin/mObjMax (= mVoxMin/mVoxMax), seeded by pool node 0 */
+    float vox_res[3];      /* mVoxRes = obj_max - obj_min */
+    float vox_res_max[3];  /* mVoxResMax: largest mVoxRes since Configure */
 } gvx_info;
 
 const char* gvx_last_error(void);
@@ -139,6 +141,10 @@ gvx_status gvx_request_full_rebuild(gvx_grid* g, int on);
  * by gvx_activate_space / gvx_rebuild_topology_cpu to the device, then the
  * bounds of the active leaves */
 gvx_status gvx_finish_topology(gvx_grid* g);
+/* FinishTopology(pCommitPool, pComputeBounds): ComputeBounds only when
+ * compute_bounds != 0; the host-activated space is committed either way
+ * (the device pools are the tree) */
+gvx_status gvx_finish_topology_ex(gvx_grid* g, int commit_pool, int compute_bounds);
 /* Clear (VG.h:327, VG.cpp:2487-2503): empty tree, next rebuild full */
 gvx_status gvx_clear(gvx_grid* g);
 /* ActivateSpace(Vector3DF) (VG.h:398, VG.cpp:2768-2855) and
@@ -304,12 +310,23 @@ gvx_status gvx_radix_sort(gvx_grid* g, const uint32_t* keys_in, const uint32_t* 
  * At most GVX_NOALLOC_SORT_MAX_KEYS pairs (larger n -> GVX_ERR_CAPACITY); the
  * array (about 2.4 MB) stays resident on every GPU that loads the library;
  * calls share it, so calls that overlap on the GPU race -- order them on one
- * stream.  Runs on the current device and the given stream (NULL = legacy
- * default stream); its first call on a device looks up the array's address,
- * so make that first call before any stream capture. */
+ * stream.  Sorting in place is allowed (keys_out == keys_in, vals_out ==
+ * vals_in); keys_out and vals_out must not overlap (GVX_ERR_INVALID_ARG).
+ * Runs on the current device and the given stream (NULL = legacy default
+ * stream); its first call on a device (and the first after the device's
+ * context was replaced, e.g. by cudaDeviceReset) looks up the array's address,
+ * so make that first call before any stream capture.  The call returns before
+ * the sort runs, so it cannot report a device-side failure itself: a bounded
+ * look-back wait that gave up sets a sticky flag in the array, which
+ * gvx_radix_sort_noalloc_status reads. */
 #define GVX_NOALLOC_SORT_MAX_KEYS (1u << 18)
 gvx_status gvx_radix_sort_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                                   uint32_t* vals_out, uint32_t n, int bits, void* stream);
+/* Waits for `stream`, then reads and clears the sticky device flag of
+ * gvx_radix_sort_noalloc on the current device: GVX_ERR_TIMEOUT when a call
+ * since the last query had a look-back wait give up (that call's output is
+ * wrong), else GVX_OK.  Allocates nothing. */
+gvx_status gvx_radix_sort_noalloc_status(void* stream);
 
 /* queries: getNumTotalNodes/getNumUsedNodes (VG.h:637-643), getBoundMin/Max */
 gvx_status gvx_get_info(gvx_grid* g, gvx_info* out);
@@ -385,6 +402,12 @@ gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads)
  * the grid and the CUDA context stay usable. */
 gvx_status gvx_test_sort_withheld_tile(gvx_grid* g, const uint32_t* keys_in, const uint32_t* vals_in,
                                        uint32_t* keys_out, uint32_t* vals_out, uint32_t n);
+/* The same test on gvx_radix_sort_noalloc's static scratch (4096 < n <=
+ * GVX_NOALLOC_SORT_MAX_KEYS, separate input and output buffers): the call
+ * returns GVX_OK at once, and gvx_radix_sort_noalloc_status then reports
+ * GVX_ERR_TIMEOUT. */
+gvx_status gvx_test_sort_noalloc_withheld_tile(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                                               uint32_t* vals_out, uint32_t n, void* stream);
 gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* count);
 
 #ifdef __cplusplus

@@ -200,8 +200,15 @@ public:
     Node* getNodeAtLevel(int n, int lev);
     Node* getNode(int grp, int lev, slong ndx);
     Node* getNode(slong nodeid);
+    // bounds of the last ComputeBounds (VG.cpp:1792-1816, run by FinishTopology):
+    // getWorldMin/Max (VG.cpp:5804-5810) and VolumeBase's getVolMin/Max return mObjMin/mObjMax;
+    // getVoxRes/getVoxResMax stand in for the public members mVoxRes/mVoxResMax
     Vector3DF getWorldMin();
     Vector3DF getWorldMax();
+    Vector3DF getVolMin() { return getWorldMin(); }
+    Vector3DF getVolMax() { return getWorldMax(); }
+    Vector3DF getVoxRes();
+    Vector3DF getVoxResMax();
 
     // ---- tree shape (VG.h:592-621) and host-side tree queries (VG.h:449-470) on the pools and
     //      child lists read back on demand: getChildNode/isOn (VG.cpp:2787-2796, 3079-3092),

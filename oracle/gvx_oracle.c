@@ -47,6 +47,7 @@ struct orc_grid {
     int curr_depth;   /* mCurrDepth */
     int last_mode;
     float pos_min[3], pos_max[3]; /* mPosMin / mPosMax of the last GetBoundingBox */
+    float vox_res_max[3];         /* mVoxResMax: zeroed by Configure (VG.cpp:2428), grown by ComputeBounds */
     int colavg_seen;              /* AUX_COLAVG exists: an avgColor ScatterDensity ran */
     int degenerate;
     /* atlas (shared subdim, as UpdateAtlas resizes every channel together) */
@@ -697,6 +698,19 @@ int orc_add_channel(orc_grid* g, int chan, int type)
     return ORC_OK;
 }
 
+/* the atlas layout (slot assignment, atlas map, mValue) without any channel
+ * storage, for topology and sampled-splat checks at sizes whose FP64 atlas
+ * would not fit; the subdivision starts as AddChannel's would */
+int orc_atlas_layout_only(orc_grid* g)
+{
+    if (!g) return ORC_ERR_ARG;
+    if (!g->have_atlas) {
+        g->sub[0] = g->defsub[0]; g->sub[1] = g->defsub[1]; g->sub[2] = g->defsub[2];
+        g->have_atlas = 1;
+    }
+    return ORC_OK;
+}
+
 int orc_clear_channel(orc_grid* g, int chan)
 {
     if (!g || chan < 0 || chan >= MAXCH || !g->ch[chan]) return ORC_ERR_ARG;
@@ -975,6 +989,151 @@ static int splat_new(orc_grid* g, int mode, int n, const float* pos, int ps, con
     }
     if (!accum) { apron_unowned(g, tab, nt, chan_d, 0.0); apron_unowned(g, tab, nt, chan_v, 0.0); }
     free(tab);
+    return ORC_OK;
+}
+
+static int floor_div(int v, int b) { return v >= 0 ? v / b : -((-v + b - 1) / b); }
+
+/* The trilinear / cubic splat of splat_new restricted to a sample of leaves,
+ * without atlas channels (a 4M-point frame's FP64 atlas would take tens of
+ * GB): the same per-point weights and the same rule for which bricks receive
+ * a contribution (every active leaf whose padded box holds the voxel), so a
+ * sampled leaf's padded P^3 voxels get exactly what splat_new writes there.
+ * Values are ADDED to dens_out[((k*P + lz)*P + ly)*P + lx] and to
+ * vel_out[(...)*3 + c] (k = index in `leaves`; either output may be NULL);
+ * the caller zeroes them for a fresh splat and keeps them to accumulate.  A
+ * listed pool index that is not an active leaf with an atlas slot takes
+ * nothing.  zero_unowned: afterwards the sampled apron voxels whose world
+ * position lies in no active leaf are set to 0, as a non-accumulating splat
+ * leaves them (apron_unowned). */
+int orc_splat_sample(orc_grid* g, int mode, int n, const float* pos, int ps, const float* weight,
+                     const float* rad_pp, const float* vel, int vs, float radius, const float trans[3],
+                     const int* leaves, int nleaves, int zero_unowned, double* dens_out, double* vel_out)
+{
+    if (!g || n < 0 || (n > 0 && !pos) || ps < 3 || nleaves < 0 || (nleaves > 0 && !leaves)) return ORC_ERR_ARG;
+    if (mode != ORC_SPLAT_TRILINEAR && mode != ORC_SPLAT_CUBIC) return ORC_ERR_ARG;
+    if (g->root_level < 0) return ORC_ERR_STATE;
+    const float tr[3] = {trans ? trans[0] : 0.f, trans ? trans[1] : 0.f, trans ? trans[2] : 0.f};
+    const int b = g->brick, a = g->apron, P = g->P;
+    const int64_t P3 = (int64_t)P * P * P;
+    pool* p0 = &g->pools[0];
+    /* dense map brick coordinate -> sample index over the sampled bricks' box */
+    int kmin[3] = {1 << 30, 1 << 30, 1 << 30}, kmax[3] = {-1, -1, -1};
+    int valid = 0;
+    for (int k = 0; k < nleaves; k++) {
+        const int li = leaves[k];
+        if (li < 0 || li >= p0->cnt || !p0->nodes[li].flags || p0->nodes[li].value[0] < 0) continue;
+        for (int c = 0; c < 3; c++) {
+            const int kc = p0->nodes[li].pos[c] / b;
+            if (kc < kmin[c]) kmin[c] = kc;
+            if (kc > kmax[c]) kmax[c] = kc;
+        }
+        valid++;
+    }
+    if (!valid) return ORC_OK;
+    const int64_t ext[3] = {kmax[0] - kmin[0] + 1, kmax[1] - kmin[1] + 1, kmax[2] - kmin[2] + 1};
+    const int64_t cells = ext[0] * ext[1] * ext[2];
+    if (cells > ((int64_t)1 << 27)) return ORC_ERR_NOMEM;
+    int* dmap = (int*)malloc((size_t)cells * sizeof(int));
+    if (!dmap) return ORC_ERR_NOMEM;
+    for (int64_t c = 0; c < cells; c++) dmap[c] = -1;
+    for (int k = 0; k < nleaves; k++) {
+        const int li = leaves[k];
+        if (li < 0 || li >= p0->cnt || !p0->nodes[li].flags || p0->nodes[li].value[0] < 0) continue;
+        const int64_t c = ((int64_t)(p0->nodes[li].pos[2] / b - kmin[2]) * ext[1] +
+                           (p0->nodes[li].pos[1] / b - kmin[1])) * ext[0] + (p0->nodes[li].pos[0] / b - kmin[0]);
+        dmap[c] = k;
+    }
+#define SAMPLE_AT(kx, ky, kz)                                                                              \
+    (((kx) < kmin[0] || (ky) < kmin[1] || (kz) < kmin[2] || (kx) > kmax[0] || (ky) > kmax[1] ||          \
+      (kz) > kmax[2])                                                                                      \
+         ? -1                                                                                              \
+         : dmap[((int64_t)((kz) - kmin[2]) * ext[1] + ((ky) - kmin[1])) * ext[0] + ((kx) - kmin[0])])
+    int nt;
+    kv* tab = active_leaf_table(g, &nt);
+    for (int i = 0; i < n; i++) {
+        float wf[3];
+        for (int c = 0; c < 3; c++) wf[c] = pos[(int64_t)i * ps + c] + tr[c];
+        if (wf[0] < 0 || wf[1] < 0 || wf[2] < 0) continue;
+        if (find_leaf(tab, nt, leaf_key((int)floorf(wf[0]) / b, (int)floorf(wf[1]) / b, (int)floorf(wf[2]) / b)) < 0)
+            continue;
+        double p[3] = {wf[0], wf[1], wf[2]};
+        const double R = rad_pp ? (double)rad_pp[i] : (double)radius;
+        int lo[3], hi[3];
+        for (int c = 0; c < 3; c++) {
+            if (mode == ORC_SPLAT_TRILINEAR) { lo[c] = (int)floor(p[c]); hi[c] = lo[c] + 1; }
+            else { lo[c] = (int)floor(p[c] - R); hi[c] = (int)ceil(p[c] + R); }
+        }
+        /* does the footprint reach a sampled brick at all? */
+        int hit = 0;
+        const int h0[3] = {floor_div(lo[0] - a, b), floor_div(lo[1] - a, b), floor_div(lo[2] - a, b)};
+        const int h1[3] = {floor_div(hi[0] + a, b), floor_div(hi[1] + a, b), floor_div(hi[2] + a, b)};
+        for (int kz = h0[2]; kz <= h1[2] && !hit; kz++)
+            for (int ky = h0[1]; ky <= h1[1] && !hit; ky++)
+                for (int kx = h0[0]; kx <= h1[0] && !hit; kx++)
+                    if (SAMPLE_AT(kx, ky, kz) >= 0) hit = 1;
+        if (!hit) continue;
+        const double w = weight ? (double)weight[i] : 1.0;
+        double u[3] = {0, 0, 0};
+        if (vel) { u[0] = vel[(int64_t)i * vs]; u[1] = vel[(int64_t)i * vs + 1]; u[2] = vel[(int64_t)i * vs + 2]; }
+        double f[3];
+        for (int c = 0; c < 3; c++) f[c] = p[c] - floor(p[c]);
+        const double h = 0.5 * R;
+        const double norm = 1.0 / (3.14159265358979323846 * h * h * h);
+        for (int z = lo[2]; z <= hi[2]; z++)
+            for (int y = lo[1]; y <= hi[1]; y++)
+                for (int x = lo[0]; x <= hi[0]; x++) {
+                    double wt;
+                    if (mode == ORC_SPLAT_TRILINEAR) {
+                        const int dx = x - lo[0], dy = y - lo[1], dz = z - lo[2];
+                        wt = w * ((dx ? f[0] : 1 - f[0]) * (dy ? f[1] : 1 - f[1]) * (dz ? f[2] : 1 - f[2]));
+                    } else {
+                        const double ddx = x - p[0], ddy = y - p[1], ddz = z - p[2];
+                        const double q = sqrt(ddx * ddx + ddy * ddy + ddz * ddz) / h;
+                        if (q >= 2.0) continue;
+                        wt = w * norm * m4(q);
+                    }
+                    if (x < 0 || y < 0 || z < 0) continue;
+                    for (int kz = floor_div(z - a, b); kz <= floor_div(z + a, b); kz++)
+                        for (int ky = floor_div(y - a, b); ky <= floor_div(y + a, b); ky++)
+                            for (int kx = floor_div(x - a, b); kx <= floor_div(x + a, b); kx++) {
+                                if (kx < 0 || ky < 0 || kz < 0) continue;
+                                const int sk = SAMPLE_AT(kx, ky, kz);
+                                if (sk < 0) continue;
+                                const int lx = x - kx * b + a, ly = y - ky * b + a, lz = z - kz * b + a;
+                                const int64_t vi = (int64_t)sk * P3 + ((int64_t)lz * P + ly) * P + lx;
+                                if (dens_out) dens_out[vi] += wt;
+                                if (vel_out && vel) {
+                                    vel_out[vi * 3] += wt * u[0];
+                                    vel_out[vi * 3 + 1] += wt * u[1];
+                                    vel_out[vi * 3 + 2] += wt * u[2];
+                                }
+                            }
+                }
+    }
+    if (zero_unowned && a > 0) {
+        for (int k = 0; k < nleaves; k++) {
+            const int li = leaves[k];
+            if (li < 0 || li >= p0->cnt || !p0->nodes[li].flags || p0->nodes[li].value[0] < 0) continue;
+            const orc_node* nd = &p0->nodes[li];
+            for (int z = -a; z < b + a; z++)
+                for (int y = -a; y < b + a; y++)
+                    for (int x = -a; x < b + a; x++) {
+                        if (x >= 0 && x < b && y >= 0 && y < b && z >= 0 && z < b) continue;
+                        const int wv[3] = {nd->pos[0] + x, nd->pos[1] + y, nd->pos[2] + z};
+                        int li2 = -1;
+                        if (wv[0] >= 0 && wv[1] >= 0 && wv[2] >= 0)
+                            li2 = find_leaf(tab, nt, leaf_key(wv[0] / b, wv[1] / b, wv[2] / b));
+                        if (li2 >= 0) continue;
+                        const int64_t vi = (int64_t)k * P3 + ((int64_t)(z + a) * P + (y + a)) * P + (x + a);
+                        if (dens_out) dens_out[vi] = 0.0;
+                        if (vel_out) vel_out[vi * 3] = vel_out[vi * 3 + 1] = vel_out[vi * 3 + 2] = 0.0;
+                    }
+        }
+    }
+#undef SAMPLE_AT
+    free(tab);
+    free(dmap);
     return ORC_OK;
 }
 
@@ -1336,6 +1495,41 @@ int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, 
                                     : ((const float*)src)[(int64_t)i * 3 + a];
             dst[(int64_t)i * 3 + a] = fmaf(fmaf(p, wdelta[a], wmin[a]), scal[a], trans[a]);
         }
+    }
+    return ORC_OK;
+}
+
+/* ComputeBounds (VG.cpp:1792-1816), run by FinishTopology (VG.cpp:1584):
+ * mVoxMin and mVoxMax both start at the position of level-0 pool node 0,
+ * whatever its flags (a delinked node still seeds them); then every active
+ * leaf lowers the minimum to its position and raises the maximum to its
+ * position + range.  mObjMin/Max = mVoxMin/Max, mVoxRes = max - min, and
+ * mVoxResMax keeps the largest mVoxRes per axis since Configure.  The
+ * reference reads pool node 0 of an empty pool (undefined); here an empty
+ * pool gives zeros.  out: min[3], max[3], res[3], res_max[3]. */
+int orc_compute_bounds(orc_grid* g, float out[12])
+{
+    float mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    const pool* p0 = &g->pools[0];
+    if (p0->cnt > 0) {
+        const int range = g->range[0];
+        for (int a = 0; a < 3; a++) mn[a] = mx[a] = (float)p0->nodes[0].pos[a];
+        for (int n = 0; n < p0->cnt; n++) {
+            const orc_node* c = &p0->nodes[n];
+            if (!c->flags) continue;
+            for (int a = 0; a < 3; a++) {
+                if (c->pos[a] < mn[a]) mn[a] = (float)c->pos[a];
+                if (c->pos[a] + range > mx[a]) mx[a] = (float)(c->pos[a] + range);
+            }
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        const float res = mx[a] - mn[a];
+        if (res > g->vox_res_max[a]) g->vox_res_max[a] = res;
+        out[a] = mn[a];
+        out[3 + a] = mx[a];
+        out[6 + a] = res;
+        out[9 + a] = g->vox_res_max[a];
     }
     return ORC_OK;
 }

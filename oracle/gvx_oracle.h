@@ -79,6 +79,8 @@ int orc_clear_channel(orc_grid* g, int chan);
 int orc_rebuild_topology(orc_grid* g, int n, const float* pos, int stride_floats,
                          float radius, const float orig[3], int mode, int min_depth);
 int orc_update_atlas(orc_grid* g);
+/* the atlas layout without channel storage (UpdateAtlas then assigns slots) */
+int orc_atlas_layout_only(orc_grid* g);
 
 /* queries */
 int orc_root_level(const orc_grid* g);   /* level of the root node, -1 if none */
@@ -100,6 +102,15 @@ int orc_splat(orc_grid* g, int mode, int n, const float* pos, int pos_stride,
               const float* weight, const float* radius_pp, const float* vel, int vel_stride,
               float radius, const float trans[3], int chan_density, int chan_vel,
               int accum, int expand, int subcell, float radius_ins);
+
+/* TRILINEAR / CUBIC splat values of a sample of leaves (level-0 pool
+ * indices) without atlas channels, for checks at sizes whose FP64 atlas
+ * would not fit: ADDED to dens_out[k][P][P][P] and vel_out[k][P][P][P][3]
+ * (either may be NULL); zero_unowned sets the sampled apron voxels that no
+ * active leaf owns to 0 afterwards (a non-accumulating splat). */
+int orc_splat_sample(orc_grid* g, int mode, int n, const float* pos, int pos_stride, const float* weight,
+                     const float* radius_pp, const float* vel, int vel_stride, float radius, const float trans[3],
+                     const int* leaves, int nleaves, int zero_unowned, double* dens_out, double* vel_out);
 
 /* InsertPointsSubcell + GatherDensity / GatherLevelSet with the optional
  * colour average (PT.cuh:696-773): clr holds one uchar4 per point (or NULL),
@@ -131,6 +142,8 @@ int orc_update_apron_faces(orc_grid* g, int chan);
 /* ConvertAndTransform (VG.cpp:5668-5682) on host arrays */
 int orc_convert_and_transform(int n, const void* src, int src_bits, float* dst, const float wmin[3],
                               const float wdelta[3], const float trans[3], const float scal[3]);
+/* ComputeBounds (VG.cpp:1792-1816): out = mVoxMin[3], mVoxMax[3], mVoxRes[3], mVoxResMax[3] */
+int orc_compute_bounds(orc_grid* g, float out[12]);
 /* mPosMin / mPosMax of the last GetBoundingBox */
 void orc_pos_bounds(orc_grid* g, float out[6]);
 

@@ -59,6 +59,8 @@ def load():
         "orc_splat": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, i, i, i, i, i, f], i),
         "orc_gather": ([vp, i, i, vp, i, vp, f, f, vp, i, i, i, i, vp], i),
         "orc_gather_fp16": ([vp, i, vp, i, vp, f, f, vp, i, i, i, vp], i), "orc_pos_bounds": ([vp, vp], None),
+        "orc_compute_bounds": ([vp, vp], i), "orc_atlas_layout_only": ([vp], i),
+        "orc_splat_sample": ([vp, i, i, vp, i, vp, vp, vp, i, f, vp, vp, i, i, vp, vp], i),
         "orc_scatter_density": ([vp, i, vp, i, vp, f, vp, i, i], i),
         "orc_convert_and_transform": ([i, vp, i, vp, vp, vp, vp, vp], i),
         "orc_update_apron_faces": ([vp, i], i),
@@ -132,6 +134,10 @@ class Oracle:
         return self._ck(self.lib.orc_rebuild_topology(self.h, pos.shape[0], _p(pos), 3, float(radius), _p(o),
                                                       mode, min_depth), "rebuild_topology", allow_degenerate)
 
+    def atlas_layout_only(self):
+        """slot assignment without channel storage (for sampled checks of large grids)"""
+        self._ck(self.lib.orc_atlas_layout_only(self.h), "atlas_layout_only")
+
     def update_atlas(self):
         self._ck(self.lib.orc_update_atlas(self.h), "update_atlas")
 
@@ -187,6 +193,30 @@ class Oracle:
                                 _p(t), chan_density, chan_vel, int(accum), int(expand), subcell, float(radius_ins))
         return self._ck(st, "splat", allow_degenerate)
 
+    def splat_sample(self, mode, pos, leaves, radius=1.0, weight=None, radius_pp=None, vel=None, trans=(0, 0, 0),
+                     zero_unowned=True, dens=None, velout=None):
+        """TRILINEAR / CUBIC splat values (FP64) of the padded bricks of the
+        level-0 pool nodes `leaves`, without atlas channels.  Adds into `dens`
+        (k, P, P, P) and `velout` (k, P, P, P, 3) when given (accumulation),
+        else into zeros; returns (dens, velout or None)."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        lv = np.ascontiguousarray(leaves, np.int32)
+        w = None if weight is None else np.ascontiguousarray(weight, np.float32)
+        r = None if radius_pp is None else np.ascontiguousarray(radius_pp, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        t = np.ascontiguousarray(trans, np.float32)
+        P = (1 << self.logdim[0]) + 2 * self.apron
+        if dens is None:
+            dens = np.zeros((len(lv), P, P, P), np.float64)
+        if velout is None and v is not None:
+            velout = np.zeros((len(lv), P, P, P, 3), np.float64)
+        assert dens.flags.c_contiguous and dens.dtype == np.float64
+        st = self.lib.orc_splat_sample(self.h, mode, pos.shape[0], _p(pos), 3, _p(w), _p(r), _p(v), 3,
+                                       float(radius), _p(t), _p(lv), len(lv), int(zero_unowned), _p(dens),
+                                       _p(velout))
+        self._ck(st, "splat_sample")
+        return dens, velout
+
     def gather(self, levelset, pos, radius, radius_ins, subcell=4, chan=0, chan_clr=-1, clr=None,
                trans=(0, 0, 0), accum=False, allow_degenerate=False):
         """InsertPointsSubcell + GatherDensity / GatherLevelSet; returns the
@@ -228,6 +258,12 @@ class Oracle:
         out = np.zeros(6, np.float32)
         self.lib.orc_pos_bounds(self.h, _p(out))
         return out[:3], out[3:]
+
+    def compute_bounds(self):
+        """ComputeBounds (VG.cpp:1792-1816): (mVoxMin, mVoxMax, mVoxRes, mVoxResMax)"""
+        out = np.zeros(12, np.float32)
+        self._ck(self.lib.orc_compute_bounds(self.h, _p(out)), "compute_bounds")
+        return out[:3], out[3:6], out[6:9], out[9:]
 
     def compute(self, effect, chan, iterations, params, update_apron, skip_over_aprons, boundval=0.0):
         """Compute (VG.cpp:4534-4558): FUNC_FILL_F/C/C4 (110-112), FUNC_SMOOTH (113)"""

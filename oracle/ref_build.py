@@ -7,6 +7,7 @@ translation units its library JIT-loads at run time:
   source/gvdb_library/kernels/cuda_gvdb_module.cu    (particles, nodes, apron kernels)
   source/gvdb_library/kernels/cuda_gvdb_copydata.cu  (fill / copy kernels)
 
+from the checkout named by $GVDB_REFERENCE or found beside the repository,
 with the reference's own flags (--use_fast_math, PTX output, see
 source/gvdb_library/CMakeLists.txt:37-60), targeting sm_103a, into
 oracle/_ref/*.ptx.  The PTX is text: it is loaded as is by the harness
@@ -21,7 +22,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = os.environ.get("GVDB_REFERENCE", "/root/reference")
+# the reference checkout: $GVDB_REFERENCE, else a directory named "reference"
+# beside the repository (absent on machines that only run the prebuilt PTX)
+REF = os.environ.get("GVDB_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 KDIR = os.path.join(REF, "source", "gvdb_library", "kernels")
 UNITS = ("cuda_gvdb_module.cu", "cuda_gvdb_copydata.cu")
 

@@ -665,6 +665,10 @@ int rh_rebuild(rh_grid* g, float radius, const float* orig, int mode, int min_de
 
 int rh_update_atlas(rh_grid* g)
 {
+    if (!g->have_atlas || g->sub[0] * g->sub[1] <= 0) {
+        t_err = "UpdateAtlas: the grid has no channel (no atlas to assign)";
+        return -1;
+    }
     int used = g->used0;
     int amax = g->sub[0] * g->sub[1] * g->sub[2];
     if (used > amax) {

@@ -45,3 +45,12 @@ def compare_topology(g, o, check_childlists=True):
             a, b = g.read_childlist(lev), o.childlist(lev)
             assert np.array_equal(a, b), "level %d child lists differ at %d slots" % (lev, int((a != b).sum()))
     assert inf["used_leaves"] == o.used_leaves()
+
+
+def leaf_slots(nodes, subdim, P):
+    """atlas slot of every level-0 node from its mValue (the atlas voxel of its
+    interior corner): slot = (bz * sy + by) * sx + bx, -1 without a slot"""
+    v = np.asarray(nodes["value"], np.int64)
+    b = v // P
+    slot = (b[:, 2] * subdim[1] + b[:, 1]) * subdim[0] + b[:, 0]
+    return np.where(v[:, 0] < 0, -1, slot)

@@ -103,7 +103,7 @@ def make_case(gvx, n, seed, lo, hi, mode):
     order = np.argsort(keys)
     slot_of_brick = (keys[order], np.arange(used, dtype=np.int64)[order])
     return dict(g=g, pos=pos, w=w, R=R, tgt=tgt, used=used, slot_of_brick=slot_of_brick, mode=mode,
-                gpu=(gp.cpu().numpy(), gw.cpu().numpy(), gr.cpu().numpy()), G=G)
+                gpu=(gp.cpu().numpy(), gw.cpu().numpy(), gr.cpu().numpy()), G=G, rho_t=rho_t)
 
 
 def reference_grads(c):
@@ -203,44 +203,47 @@ def test_backward_is_deterministic(gvx_mod):
 
 
 def test_autograd_function_wrapper(gvx_mod):
-    """the adjoint behind a torch.autograd.Function (test harness only)"""
+    """the adjoint behind a torch.autograd.Function (test harness only): the
+    splat of (pos, w, R) as a differentiable op, L = 1/2 |rho - rho*|^2 over
+    the interior voxels, gradients of all three inputs against the FP64
+    restatement's autograd (and identical to a direct gvx_splat_backward)"""
     import torch
 
-    rng = np.random.default_rng(11)
-    n = 5_000
-    pos0 = rng.uniform(8, 60, (n, 3)).astype(np.float32)
-    g = gvx_mod.Grid(0)
-    g.configure(LOGDIM)
-    g.add_channel(0, gvx_mod.T_FLOAT, 1)
-    g.commit_points_host(pos0)
-    g.rebuild_topology(n, 3.0, mode=gvx_mod.TOPO_FULL)
-    g.update_atlas()
+    c = make_case(gvx_mod, 20_000, 4, 8.0, 120.0, "cubic")
+    g, n = c["g"], len(c["pos"])
 
     class Splat(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, pos, w):
-            ctx.save_for_backward(pos, w)
+        def forward(ctx, pos, w, R):
             g.set_points(n, pos.detach())
-            g.set_point_attribs(weight=w.detach())
-            g.splat(gvx_mod.SPLAT_CUBIC, n, 2.0, chan_density=0)
+            g.set_point_attribs(weight=w.detach(), radius=R.detach())
+            g.splat(gvx_mod.SPLAT_CUBIC, n, 1.0, chan_density=0)
             g.sync()
-            return torch.from_numpy(g.read_channel(0).reshape(-1)).cuda()
+            return torch.from_numpy(g.read_channel(0).copy()).cuda()
 
         @staticmethod
         def backward(ctx, grad_out):
             gp = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
             gw = torch.zeros(n, dtype=torch.float32, device="cuda")
-            g.splat_backward(gvx_mod.SPLAT_CUBIC, n, 2.0, grad_out.contiguous(), gp, gw)
+            gr = torch.zeros(n, dtype=torch.float32, device="cuda")
+            g.splat_backward(gvx_mod.SPLAT_CUBIC, n, 1.0, grad_out.contiguous(), gp, gw, gr)
             g.sync()
-            return gp, gw
+            return gp, gw, gr
 
-    pos = torch.from_numpy(pos0).cuda().requires_grad_(True)
-    w = torch.ones(n, device="cuda", requires_grad=True)
-    rho = Splat.apply(pos, w)
-    P = 10
+    pos = torch.from_numpy(c["pos"]).cuda().requires_grad_(True)
+    w = torch.from_numpy(c["w"]).cuda().requires_grad_(True)
+    R = torch.from_numpy(c["R"]).cuda().requires_grad_(True)
+    rho = Splat.apply(pos, w, R)
+    rho_t = torch.from_numpy(c["rho_t"]).cuda()
+    P = rho.shape[1]
     mask = torch.zeros((P, P, P), device="cuda")
     mask[1:-1, 1:-1, 1:-1] = 1.0
-    L = 0.5 * ((rho.view(-1, P, P, P) * mask) ** 2).sum()
+    L = 0.5 * (((rho - rho_t) * mask) ** 2).sum()
     L.backward()
-    # dL/dw_i = sum_v rho_v W_iv: positive for every point with a support
-    assert torch.isfinite(pos.grad).all() and (w.grad > 0).float().mean() > 0.99
+    got = (pos.grad.cpu().numpy(), w.grad.cpu().numpy(), R.grad.cpu().numpy())
+    for a, b in zip(got, c["gpu"]):
+        assert np.array_equal(a, b)
+    gp, gw, gr, _ = reference_grads(c)
+    assert close(got[0], gp), float(np.abs(got[0] - gp).max() / np.abs(gp).max())
+    assert close(got[1], gw)
+    assert close(got[2], gr)

@@ -33,6 +33,18 @@ def step(gvx, orc, g, o, pos, radius, mode, min_depth=1, orig=(0.0, 0.0, 0.0)):
     compare_topology(g, o)
     assert g.info()["last_rebuild"] == o.last_mode()
     assert np.array_equal(g.read_atlas_map(), o.atlas_map())
+    compare_bounds(g, o)
+
+
+def compare_bounds(g, o):
+    """FinishTopology's ComputeBounds (VG.cpp:1792-1816) against the oracle's
+    restatement: mObjMin/Max, mVoxRes and the sticky mVoxResMax, exactly"""
+    vmin, vmax, vres, vres_max = o.compute_bounds()
+    inf = g.info()
+    assert np.array_equal(np.float32(inf["obj_min"]), vmin)
+    assert np.array_equal(np.float32(inf["obj_max"]), vmax)
+    assert np.array_equal(np.float32(inf["vox_res"]), vres)
+    assert np.array_equal(np.float32(inf["vox_res_max"]), vres_max)
 
 
 def moving_slab(n, seed, frames, dt, box=(150.0, 90.0, 180.0)):
@@ -120,3 +132,33 @@ def test_full_request_after_incremental(gvx_mod, orc):
         step(gvx_mod, orc, g, o, pos, 1.0, gvx_mod.TOPO_AUTO)
     step(gvx_mod, orc, g, o, frames[0], 1.0, gvx_mod.TOPO_FULL)
     assert o.last_mode() == 1
+
+
+def test_bounds_seeded_by_inactive_pool_node_zero(gvx_mod, orc):
+    """ComputeBounds seeds min and max with level-0 pool node 0's position even
+    when an incremental build has delinked that leaf (VG.cpp:1795-1797), and
+    mVoxResMax keeps the widest box seen since Configure."""
+    g, o = new_pair(gvx_mod, orc)
+    a = np.array([[10.5, 10.5, 10.5], [300.5, 200.5, 100.5]], np.float32)
+    step(gvx_mod, orc, g, o, a, 0.0, gvx_mod.TOPO_AUTO)
+    step(gvx_mod, orc, g, o, a, 0.0, gvx_mod.TOPO_AUTO)
+    wide = g.info()["vox_res_max"]
+    b = np.array([[300.5, 200.5, 100.5], [120.5, 40.5, 20.5]], np.float32)
+    step(gvx_mod, orc, g, o, b, 0.0, gvx_mod.TOPO_AUTO)
+    n0 = g.read_nodes(0)
+    assert n0["pos"][0].tolist() == [8, 8, 8] and n0["flags"][0] == 0
+    inf = g.info()
+    assert inf["obj_min"] == [8.0, 8.0, 8.0]  # from the delinked node 0, not from an active leaf
+    assert inf["obj_max"] == [304.0, 208.0, 104.0]
+    # a narrower cloud later: mVoxRes shrinks, mVoxResMax does not
+    g2, o2 = new_pair(gvx_mod, orc)
+    step(gvx_mod, orc, g2, o2, a, 0.0, gvx_mod.TOPO_FULL)
+    narrow = np.array([[11.5, 11.5, 11.5], [20.5, 11.5, 11.5]], np.float32)
+    step(gvx_mod, orc, g2, o2, narrow, 0.0, gvx_mod.TOPO_FULL)
+    inf2 = g2.info()
+    assert inf2["vox_res"] == [16.0, 8.0, 8.0] and inf2["vox_res_max"] == wide
+    # FinishTopology(true, false) leaves the bounds as they were
+    g2.commit_points_host(a)
+    g2.rebuild_topology(len(a), 0.0, mode=gvx_mod.TOPO_FULL)
+    g2.finish_topology(compute_bounds=False)
+    assert g2.info()["obj_min"] == inf2["obj_min"] and g2.info()["obj_max"] == inf2["obj_max"]

@@ -407,3 +407,20 @@ def test_cpu_tree_known_answer(orc):
     # a point in an existing leaf adds nothing
     t.activate(np.array([[9.9, 12.0, 15.5]], np.float32))
     assert len(t.nodes(0)) == 2
+
+
+def test_compute_bounds_known_answers(orc):
+    """ComputeBounds (VG.cpp:1792-1816) on the two-point tree: leaves at
+    (8,8,8), (296,200,96), (296,192,96), range 8 -> min (8,8,8), max
+    (304,208,104); mVoxResMax is sticky while mVoxRes follows the last tree."""
+    o = orc.Oracle()
+    o.add_channel(0, orc.T_FLOAT)
+    assert o.rebuild_topology(two_points(), 1.0) == orc.OK
+    vmin, vmax, vres, vres_max = o.compute_bounds()
+    assert vmin.tolist() == [8, 8, 8] and vmax.tolist() == [304, 208, 104]
+    assert vres.tolist() == [296, 200, 96] and vres_max.tolist() == [296, 200, 96]
+    small = np.array([[10.5, 10.5, 10.5], [20.5, 10.5, 10.5]], np.float32)
+    assert o.rebuild_topology(small, 0.0, mode=orc.TOPO_FULL) == orc.OK
+    vmin, vmax, vres, vres_max = o.compute_bounds()
+    assert vmin.tolist() == [8, 8, 8] and vmax.tolist() == [24, 16, 16]
+    assert vres.tolist() == [16, 8, 8] and vres_max.tolist() == [296, 200, 96]
