@@ -186,15 +186,21 @@ def algorithmic_bytes(n, nb, P):
 
 
 def load_traffic():
+    """(DRAM bytes per active brick, per point) of the splat launch, from the summary of an
+    ncu capture of the bench's timed frames (profiles/splat_cubic_sph4m_traffic.txt)"""
     p = os.path.join(ROOT, "profiles", "splat_cubic_sph4m_traffic.txt")
     if not os.path.exists(p):
         return None
+    vals = {}
     for ln in open(p):
-        if ln.startswith("dram_bytes_per_launch:"):
+        if ":" in ln:
+            k, v = ln.split(":", 1)
             try:
-                return float(ln.split(":", 1)[1])
-            except ValueError:
-                return None
+                vals[k.strip()] = float(v.split()[0])
+            except (ValueError, IndexError):
+                pass
+    if "dram_bytes_per_brick" in vals and "dram_bytes_per_point" in vals:
+        return vals["dram_bytes_per_brick"], vals["dram_bytes_per_point"]
     return None
 
 
@@ -317,8 +323,15 @@ def run_ours(args, rank, world, pool):
         ms = max_over_ranks(sum(step_ms) / len(step_ms), dist, dev)
 
         inf = g.info()
-        nb = inf["used_leaves"]
         P = inf["brick_res"] + 2 * inf["apron"]
+        # active bricks of each timed frame (the splat's bytes scale with them): the frames'
+        # topologies rebuilt again outside the timed region
+        nb_frames = []
+        for k in range(args.steps):
+            g.set_points(n, frames[(args.warmup + k) % FRAMES], 0, 12, vel_d, 0, 12)
+            g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_FULL)
+            nb_frames.append(int(g.info()["used_leaves"]))
+        nb = sum(nb_frames) / len(nb_frames)
 
         # ---- the reference's default rebuild semantics (RebuildTopology's state machine, VG.cpp:1195-1217):
         # after one full build, frames extend the tree incrementally; outside the timed region
@@ -393,12 +406,15 @@ def run_ours(args, rank, world, pool):
     splat_bytes = b_pts + b_atlas
     splat_avg = sum(splat_ms) / len(splat_ms)
     achieved = splat_bytes / (splat_avg * 1e-3) / 1e9
+    # per-brick and per-point DRAM bytes of the splat from an ncu capture of the same frames,
+    # applied to this run's bricks and points
+    tr = load_traffic()
+    traffic = tr[0] * nb + tr[1] * n if tr else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
         peak = float(json.load(open(peaks_path))["hbm_gbs"])
         peak_src = "measured"
-    traffic = load_traffic()
     out = {
         "metric": METRIC, "value": job_mpoints_s(world, n, ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -409,13 +425,19 @@ def run_ours(args, rank, world, pool):
         "incremental": incremental,
         "hbm_gbs_step": (b_topo + b_pts + b_atlas + b_apron) / (ms * 1e-3) / 1e9,
         "active_bricks": nb,
-        "roofline": {"kernel": "k_splat (cubic, density+velocity)", "bound": "hbm", "achieved": achieved,
+        "active_bricks_per_frame": nb_frames,
+        "roofline": {"kernel": "k_splat_slab (cubic, density+velocity)", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "algorithmic_bytes": splat_bytes, "launch_ms": splat_avg},
+                     "traffic": traffic, "algorithmic_bytes": splat_bytes, "launch_ms": splat_avg,
+                     "bytes_model": "24 B per point (position, velocity) + P^3 * 20 B per active brick (density "
+                                    "float + velocity float4), bricks averaged over the timed frames; traffic = "
+                                    "ncu DRAM bytes per brick and per point of the same frames, times this run's"},
         "gpu_launches": int(launches),
         "clocks": clk,
         "e2e": {"value": world * n * e2e_steps / e2e_wall / 1e6, "unit": UNIT, "h2d_bytes_per_step": n * 24,
-                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps} if e2e_steps else None,
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                "readback": "the level-1 node pool only: the density and velocity atlases stay in HBM, where "
+                            "GVDB's consumers (raycast, gathers, compute) read them"} if e2e_steps else None,
     }
     if dist:
         dist.destroy_process_group()
@@ -461,9 +483,9 @@ def run_differentiable(dev, iters=5):
         gw = torch.empty(n, dtype=torch.float32, device=dev)
         gr = torch.empty(n, dtype=torch.float32, device=dev)
         G = torch.empty_like(rho_t)
-        fwd, bwd = [], []
+        fwd, bwd, bwd_rc = [], [], []
         for k in range(iters + 3):
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             e[0].record(stream)
             g.splat(gvx.SPLAT_CUBIC, n, 1.0, chan_density=0)
             e[1].record(stream)
@@ -472,17 +494,24 @@ def run_differentiable(dev, iters=5):
                 G.copy_(torch.from_numpy(g.read_channel(0).reshape(-1)) - rho_t.cpu())
             g.splat_backward(gvx.SPLAT_CUBIC, n, 1.0, G, gp, gw, gr)
             e[2].record(stream)
+            # the adjoint with the sorted-key permutation recomputed from the positions
+            g.splat_backward(gvx.SPLAT_CUBIC, n, 1.0, G, gp, gw, gr, recompute=True)
+            e[3].record(stream)
             torch.cuda.synchronize()
             if k >= 3:
                 fwd.append(e[0].elapsed_time(e[1]))
                 bwd.append(e[1].elapsed_time(e[2]))
+                bwd_rc.append(e[2].elapsed_time(e[3]))
         bricks = g.info()["used_leaves"]
     g.close()
-    f, b = sum(fwd) / len(fwd), sum(bwd) / len(bwd)
+    f, b, brc = sum(fwd) / len(fwd), sum(bwd) / len(bwd), sum(bwd_rc) / len(bwd_rc)
     return {"workload": "differentiable: 1M points U[8,504)^3 in 512^3, w~U(0,1), R~U(1,3), cubic density; "
                         "G = rho - rho*, rho* = splat of p + N(0,0.5)",
             "points": n, "active_bricks": bricks, "fwd_ms": round(f, 4), "bwd_ms": round(b, 4),
-            "fwd_plus_bwd_ms": round(f + b, 4), "bwd_over_fwd": round(b / f, 4)}
+            "fwd_plus_bwd_ms": round(f + b, 4), "bwd_over_fwd": round(b / f, 4),
+            "bwd_ms_recomputed": round(brc, 4), "bwd_recomputed_over_fwd": round(brc / f, 4),
+            "bwd_note": "bwd_ms reuses the forward's sorted-key grouping; bwd_ms_recomputed re-keys, re-sorts and "
+                        "re-partitions the points from their positions before the adjoint"}
 
 
 def run_batched(dev, iters=5):
@@ -563,6 +592,57 @@ def run_batched(dev, iters=5):
                      "from a pool of host threads on the grids' own streams, wall-clock timed apart"}
 
 
+def run_scatter_frame(dev, frames=3):
+    """libgvx on the work of the reference arm's `reference_cuda` frame: the same 4M SPH frames
+    (advected 1..3), full RebuildTopology (radius 2), UpdateAtlas, ClearChannel, InsertPoints +
+    ScatterDensity (radius 2, 7-voxel stencil) and UpdateApron of the density channel.  Positions
+    on the device; CUDA-event time per stage on the grid's stream, frame 0 a warm-up."""
+    import torch
+
+    import gvx
+    import workloads
+
+    pos0, vel = workloads.sph_slab(n=N_POINTS, seed=0, box=BOX)
+    stream = torch.cuda.Stream(device=dev)
+    g = gvx.Grid(dev.index)
+    g.configure(LOGDIM)
+    g.add_channel(0, gvx.T_FLOAT, 1)
+    g.set_stream(stream.cuda_stream)
+    names = ("topology", "update_atlas", "clear_channel", "insert_points_scatter_density", "update_apron")
+    tot, stages = [], []
+    with torch.cuda.stream(stream):
+        for f in range(frames + 1):
+            pd = torch.from_numpy(workloads.advect(pos0, vel, DT * f)).to(dev)
+            n = pd.shape[0]
+            torch.cuda.synchronize()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+            e[0].record(stream)
+            g.set_points(n, pd)
+            g.rebuild_topology(n, RADIUS, mode=gvx.TOPO_FULL)
+            e[1].record(stream)
+            g.update_atlas()
+            e[2].record(stream)
+            g.clear_channel(0)
+            e[3].record(stream)
+            g.insert_points(n)
+            g.scatter_density(n, RADIUS)
+            e[4].record(stream)
+            g.update_apron(0, 0.0)
+            e[5].record(stream)
+            torch.cuda.synchronize()
+            if f > 0:
+                tot.append(e[0].elapsed_time(e[-1]))
+                stages.append([e[k].elapsed_time(e[k + 1]) for k in range(len(names))])
+        used = g.info()["used_leaves"]
+    g.close()
+    ms = sum(tot) / len(tot)
+    return {"workload": "the reference arm's reference_cuda frame through libgvx: ScatterDensity (7-voxel "
+                        "stencil, radius 2) + UpdateApron of density on the 4M SPH frames 1..3",
+            "ms_per_frame": round(ms, 4), "mpoints_s": round(N_POINTS / (ms * 1e-3) / 1e6, 1),
+            "active_bricks": int(used),
+            "stage_ms": {k: round(sum(x[i] for x in stages) / len(stages), 4) for i, k in enumerate(names)}}
+
+
 def run_point_cloud(dev, reps=5):
     """Point-cloud level set, the sequence gPointCloud runs per frame: RebuildTopology (radius 2r,
     full) + UpdateAtlas + ClearChannel + InsertPointsSubcell_FP16 (subcell 4, r) +
@@ -638,33 +718,43 @@ def run_fusion(dev, frames=30):
     g.add_channel(1, gvx.T_FLOAT, 1)
     g.set_stream(stream.cuda_stream)
     ms, pts = [], 0
+    names = ("topology", "update_atlas", "insert_points", "splat_density", "splat_confidence", "aprons")
+    stages = []
     with torch.cuda.stream(stream):
         for pd, cd in fr:
             n = pd.shape[0]
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+            e[0].record(stream)
             g.set_points(n, pd)
             g.set_point_attribs()
             g.rebuild_topology(n, 1.0, mode=gvx.TOPO_ACCUMULATE)
+            e[1].record(stream)
             g.update_atlas()
+            e[2].record(stream)
             g.insert_points(n)
+            e[3].record(stream)
             g.splat(gvx.SPLAT_TRILINEAR, n, 1.0, chan_density=0, accum=True)
+            e[4].record(stream)
             g.set_point_attribs(weight=cd)
             g.splat(gvx.SPLAT_TRILINEAR, n, 1.0, chan_density=1, accum=True)
+            e[5].record(stream)
             g.update_apron(0, 0.0)
             g.update_apron(1, 0.0)
-            e1.record(stream)
+            e[6].record(stream)
             torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
+            ms.append(e[0].elapsed_time(e[-1]))
+            stages.append([e[k].elapsed_time(e[k + 1]) for k in range(len(names))])
             pts += n
         inf = g.info()
     g.close()
     steady = ms[2:]  # the first two AccumulateTopology calls are full rebuilds of a growing tree
+    st_mean = [sum(x[k] for x in stages[2:]) / len(stages[2:]) for k in range(len(names))]
     return {"workload": "fusion: %d depth frames 640x480 (f=525) of 8 spheres + 2 planes in 2048^3, N(0,0.5) "
                         "noise; AccumulateTopology r=1, TRILINEAR density + confidence-weighted density (accum), "
                         "UpdateApron x2" % frames,
             "frames": frames, "points": int(pts), "active_bricks": int(inf["used_leaves"]),
             "ms_per_frame": round(sum(ms) / len(ms), 4), "ms_per_frame_incremental": round(sum(steady) / len(steady), 4),
+            "stage_ms_incremental": {k: round(v, 4) for k, v in zip(names, st_mean)},
             "mpoints_s": round(pts / (sum(ms) * 1e-3) / 1e6, 1)}
 
 
@@ -692,27 +782,42 @@ def reference_cuda(frames=3):
     pos0, vel = workloads.sph_slab(n=N_POINTS, seed=0, box=BOX)
     r = rh.RefGrid(LOGDIM)
     r.add_channel(0, 3)
-    times = []
+    names = ("topology", "update_atlas", "clear_channel", "insert_points_scatter_density", "update_apron")
+    times, stages = [], []
     for f in range(frames + 1):
         r.set_points(workloads.advect(pos0, vel, DT * f))
-        t0 = time.perf_counter()
+        torch.cuda.synchronize()
+        t = [time.perf_counter()]
         st = r.rebuild(RADIUS, mode=1)
         if st != 0:
             return {"unavailable": "reference rebuild failed: status %d" % st}
+        torch.cuda.synchronize()
+        t.append(time.perf_counter())
         r.update_atlas()
+        torch.cuda.synchronize()
+        t.append(time.perf_counter())
         r.clear_channel(0)
+        torch.cuda.synchronize()
+        t.append(time.perf_counter())
         r.scatter(RADIUS)
+        torch.cuda.synchronize()
+        t.append(time.perf_counter())
         r.update_apron(0, 0.0)
         torch.cuda.synchronize()
+        t.append(time.perf_counter())
         if f > 0:
-            times.append(time.perf_counter() - t0)
+            times.append(t[-1] - t[0])
+            stages.append([t[k + 1] - t[k] for k in range(len(names))])
     used = r.used_leaves()
     r.close()
     ms = 1e3 * sum(times) / len(times)
+    st_ms = {k: round(1e3 * sum(x[i] for x in stages) / len(stages), 3) for i, k in enumerate(names)}
     return {"value": N_POINTS / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_frame": ms, "frames": frames,
-            "active_bricks": used,
+            "active_bricks": used, "stage_ms": st_ms,
             "path": "reference kernels (cuda_gvdb_module.cu as PTX, --use_fast_math) + restated host "
-                    "orchestration, thrust sort/unique; ScatterDensity + UpdateApron of density"}
+                    "orchestration: GetBoundingBox with thrust min/max on the device, thrust sort/unique; "
+                    "ScatterDensity + UpdateApron of density; wall clock per stage with a device synchronisation "
+                    "after each (the reference synchronises inside every stage)"}
 
 
 def host_topology(frames=2):
@@ -784,7 +889,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiable, batched, fusion and point-cloud workloads")
-    ap.add_argument("--extra", choices=["differentiable", "batched", "fusion", "point_cloud"],
+    ap.add_argument("--extra", choices=["differentiable", "batched", "fusion", "point_cloud", "scatter_frame"],
                     help="run only this workload and print its JSON (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -792,7 +897,7 @@ def main():
         import torch
 
         fn = {"differentiable": run_differentiable, "batched": run_batched, "fusion": run_fusion,
-              "point_cloud": run_point_cloud}[args.extra]
+              "point_cloud": run_point_cloud, "scatter_frame": run_scatter_frame}[args.extra]
         print(json.dumps(fn(torch.device("cuda", 0))))
         return
     rank = int(os.environ.get("RANK", 0))
@@ -813,6 +918,7 @@ def main():
         out["batched"] = run_batched(torch.device("cuda", 0))
         out["fusion"] = run_fusion(torch.device("cuda", 0))
         out["point_cloud"] = run_point_cloud(torch.device("cuda", 0))
+        out["scatter_frame"] = run_scatter_frame(torch.device("cuda", 0))
     if rank == 0:
         if pool is not None:
             out["cpu_baseline"] = cpu_baseline(pool)

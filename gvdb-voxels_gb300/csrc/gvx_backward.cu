@@ -188,8 +188,9 @@ __global__ void __launch_bounds__(kBackThreads) k_splat_backward(BackArgs a)
     }
 }
 
-extern "C" gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const float trans[3],
-                                         const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r)
+extern "C" gvx_status gvx_splat_backward_ex(gvx_grid* g, int mode, int n, float radius, const float trans[3],
+                                            const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r,
+                                            int flags)
 {
     if (!g) {
         gvx_set_error("null grid handle");
@@ -214,7 +215,16 @@ extern "C" gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float rad
         return GVX_ERR_INVALID_ARG;
     }
     GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));
-    // the grouping of the forward: reused when valid, else re-keyed and re-sorted
+    // the grouping of the forward: reused when valid, else re-keyed and re-sorted.
+    // GVX_BWD_RECOMPUTE drops it first, so the permutation is recomputed from the
+    // positions (keys, radix sort, octant partition with the sorted attributes)
+    // rather than taken from the forward; the sort is deterministic, so the new
+    // grouping equals the forward's and the gradients are the same bit for bit.
+    if (flags & GVX_BWD_RECOMPUTE) {
+        g->group_valid = false;
+        g->oct_valid = false;
+        g->perm_valid = false;
+    }
     gvx_status rc = gvx_prepare_points(g, n, trans, ppr);
     if (rc) return rc;
     BackArgs a;
@@ -251,4 +261,10 @@ extern "C" gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float rad
     }
     GVX_CK(cudaGetLastError());
     return GVX_OK;
+}
+
+extern "C" gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const float trans[3],
+                                         const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r)
+{
+    return gvx_splat_backward_ex(g, mode, n, radius, trans, dL_drho, grad_pos, grad_w, grad_r, 0);
 }

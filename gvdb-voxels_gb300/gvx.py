@@ -82,6 +82,7 @@ def load(path=None):
         "gvx_gather_levelset": ([vp, i, i, f, fp, i, i, i, i], i),
         "gvx_splat": ([vp, i, i, f, fp, i, i, i], i),
         "gvx_splat_backward": ([vp, i, i, f, fp, vp, vp, vp, vp], i),
+        "gvx_splat_backward_ex": ([vp, i, i, f, fp, vp, vp, vp, vp, i], i),
         "gvx_update_apron": ([vp, i, f], i), "gvx_update_apron_all": ([vp], i),
         "gvx_compute": ([vp, i, i, i, fp, i, i, f], i),
         "gvx_insert_points_subcell_fp16": ([vp, i, i, f, fp, ctypes.POINTER(i)], i),
@@ -244,11 +245,13 @@ class Grid:
         self._check(self.lib.gvx_splat(self.h, mode, n, float(radius), _f3(trans), chan_density, chan_vel,
                                        int(accum)))
 
-    def splat_backward(self, mode, n, radius, dl_drho, grad_pos, grad_w, grad_r=None, trans=None):
+    def splat_backward(self, mode, n, radius, dl_drho, grad_pos, grad_w, grad_r=None, trans=None, recompute=False):
         """device buffers (torch tensors or raw pointers): dL/drho in the density
-        channel layout in, dL/dp (n x 3), dL/dw (n) and dL/dR (n) out"""
-        self._check(self.lib.gvx_splat_backward(self.h, mode, n, float(radius), _f3(trans), _ptr(dl_drho),
-                                                _ptr(grad_pos), _ptr(grad_w), _ptr(grad_r)))
+        channel layout in, dL/dp (n x 3), dL/dw (n) and dL/dR (n) out; recompute:
+        the sorted-key permutation is recomputed from the positions, not reused"""
+        self._check(self.lib.gvx_splat_backward_ex(self.h, mode, n, float(radius), _f3(trans), _ptr(dl_drho),
+                                                   _ptr(grad_pos), _ptr(grad_w), _ptr(grad_r),
+                                                   BWD_RECOMPUTE if recompute else 0))
 
     def insert_points_subcell(self, subcell, n, radius, trans=None):
         ln = ctypes.c_int(0)
@@ -425,6 +428,7 @@ def radix_sort(grid, keys_in, vals_in, keys_out, vals_out, n, bits):
 
 
 BATCH_GRAPH, BATCH_TUNE = 1, 2
+BWD_RECOMPUTE = 1
 
 
 class Batch:

@@ -257,6 +257,12 @@ gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float tra
  * Uses the grouping of the forward splat, re-sorting if the points changed. */
 gvx_status gvx_splat_backward(gvx_grid* g, int mode, int n, float radius, const float trans[3],
                               const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r);
+/* gvx_splat_backward with flags: GVX_BWD_RECOMPUTE recomputes the points' sorted-key
+ * permutation from the positions (re-key, re-sort, octant partition) instead of
+ * reusing the forward's stored grouping; the gradients are identical. */
+#define GVX_BWD_RECOMPUTE 1
+gvx_status gvx_splat_backward_ex(gvx_grid* g, int mode, int n, float radius, const float trans[3],
+                                 const float* dL_drho, float* grad_pos, float* grad_w, float* grad_r, int flags);
 /* UpdateApron(chan, boundval) / UpdateApron() (VG.h:407-408, VG.cpp:4411-4457) */
 gvx_status gvx_update_apron(gvx_grid* g, int chan, float boundval);
 gvx_status gvx_update_apron_all(gvx_grid* g);

@@ -22,7 +22,9 @@
 //     and thrust::unique on the device give the same total order and unique
 //     list, which are copied to the host for the allocation loop as the
 //     reference copies AUX_UNIQUE_LEVXYZ;
-//   - the min/max of the bounding box is taken on the host (thrust there);
+//   - the min/max of the bounding box: thrust::min_element / max_element on
+//     the device per axis, as gvdbDeviceMin/MaxElementF (gvdb_cutils.cu:22-39),
+//     then one copy of the 6 floats (RetrieveData of AUX_BOUNDING_BOX);
 //   - key buffers are sized generously (the reference's N*depth buffer can overflow);
 //   - ScatterDensity is launched with the kernel's own argument list (the
 //     reference host call omits the VDBInfo pointer, VG.cpp:5645);
@@ -33,6 +35,7 @@
 #include <string.h>
 
 #include <thrust/device_ptr.h>
+#include <thrust/extrema.h>
 #include <thrust/sort.h>
 #include <thrust/unique.h>
 
@@ -603,14 +606,12 @@ int rh_rebuild(rh_grid* g, float radius, const float* orig, int mode, int min_de
     void* args[] = {&n, &o, &pos, &off, &stride, &xo, &yo, &zo};
     if (launch(g_mod.splitpos, n / 256 + 1, 1, 1, 256, 1, 1, args)) return -1;
     RH_CK(cuCtxSynchronize());
-    std::vector<float> v[3];
     CUdeviceptr src[3] = {xo, yo, zo};
     float mn[3], mx[3];
     for (int a = 0; a < 3; a++) {
-        v[a].resize(n);
-        RH_CK(cuMemcpyDtoH(v[a].data(), src[a], (size_t)n * 4));
-        mn[a] = *std::min_element(v[a].begin(), v[a].end());
-        mx[a] = *std::max_element(v[a].begin(), v[a].end());
+        thrust::device_ptr<float> d = thrust::device_pointer_cast((float*)src[a]);
+        mn[a] = *thrust::min_element(d, d + n);
+        mx[a] = *thrust::max_element(d, d + n);
     }
     int pmin[3], pmax[3];
     float plo[3], phi[3];

@@ -202,6 +202,29 @@ def test_backward_is_deterministic(gvx_mod):
     assert np.array_equal(gr.cpu().numpy(), c["gpu"][2])
 
 
+def test_backward_with_recomputed_permutation(gvx_mod):
+    """GVX_BWD_RECOMPUTE: the permutation re-keyed and re-sorted from the positions gives the
+    gradients of the stored grouping bit for bit, and the forward after it is unchanged"""
+    import torch
+
+    c = make_case(gvx_mod, 30_000, 9, 8.0, 150.0, "cubic")
+    g, n = c["g"], len(c["pos"])
+    Gd = torch.from_numpy(c["G"]).cuda()
+    gp = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    gw = torch.zeros(n, dtype=torch.float32, device="cuda")
+    gr = torch.zeros(n, dtype=torch.float32, device="cuda")
+    launches = g.kernel_launches()
+    g.splat_backward(gvx_mod.SPLAT_CUBIC, n, 1.0, Gd, gp, gw, gr, recompute=True)
+    g.sync()
+    assert g.kernel_launches() - launches > 2  # keys, sort passes, octant partition, then the adjoint
+    assert np.array_equal(gp.cpu().numpy(), c["gpu"][0])
+    assert np.array_equal(gw.cpu().numpy(), c["gpu"][1])
+    assert np.array_equal(gr.cpu().numpy(), c["gpu"][2])
+    rho = g.read_channel(0).copy()
+    g.splat(gvx_mod.SPLAT_CUBIC, n, 1.0, chan_density=0)
+    assert np.array_equal(g.read_channel(0), rho)
+
+
 def test_autograd_function_wrapper(gvx_mod):
     """the adjoint behind a torch.autograd.Function (test harness only): the
     splat of (pos, w, R) as a differentiable op, L = 1/2 |rho - rho*|^2 over
