@@ -92,8 +92,10 @@ gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need)
             // grows inside the allocation: only the new bricks are cleared
             GVX_CK(cudaMemsetAsync((char*)ch.data.p + old_bytes, 0, new_bytes - old_bytes, g->stream));
         } else {
+            // a growing atlas (accumulating topologies) at least doubles its capacity, so that
+            // it is reallocated and copied a logarithmic number of times
             DevBuf nb;
-            GVX_CK(gvx_ensure(nb, new_bytes));
+            GVX_CK(gvx_ensure(nb, ch.data.p ? std::max(new_bytes, 2 * ch.data.cap) : new_bytes));
             GVX_CK(cudaMemsetAsync((char*)nb.p + old_bytes, 0, new_bytes - old_bytes, g->stream));
             if (ch.data.p && ch.slots)
                 GVX_CK(cudaMemcpyAsync(nb.p, ch.data.p, old_bytes, cudaMemcpyDeviceToDevice, g->stream));
@@ -101,8 +103,7 @@ gvx_status gvx_grow_atlas(gvx_grid* g, int64_t need)
             gvx_free(ch.data);
             ch.data = nb;
         }
-        ch.slots = slots;
-        ch.apron_valid = false;
+        ch.slots = slots;  // the bricks keep their slots and values; UpdateAtlas settles the aprons' state
     }
     g->sub[2] = nz;
     return GVX_OK;
@@ -184,6 +185,15 @@ gvx_status gvx_create(int device, gvx_grid** out)
         return gvx_cuda_fail(e, "cudaStreamCreate");
     }
     g->own_stream = true;
+    // the device error word starts clear; from then on it is cleared when it is read
+    e = gvx_ensure(g->d_err, 64);
+    if (e == cudaSuccess) e = cudaMemset(g->d_err.p, 0, 64);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(g->stream);
+        gvx_free(g->d_err);
+        delete g;
+        return gvx_cuda_fail(e, "gvx_create: error word");
+    }
     *out = g;
     return GVX_OK;
 }
@@ -205,7 +215,7 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
                       &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp,
-                      &g->sc_q, &g->sc_qclr, &g->own_stage, &g->apron_tab};
+                      &g->sc_q, &g->sc_qclr, &g->own_stage, &g->apron_tab, &g->apron_mark};
     for (DevBuf* b : bufs) gvx_free(*b);
     for (int l = 0; l < GVX_MAXLEV; l++) {
         gvx_free(g->nodes[l]);
@@ -213,6 +223,7 @@ gvx_status gvx_destroy(gvx_grid* g)
     }
     for (int c = 0; c < GVX_MAXCH; c++) gvx_free(g->ch[c].data);
     gvx_host_tree_free(g);
+    gvx_topo_staged_free(g);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
     if (g->h_pin) cudaFreeHost(g->h_pin);
@@ -334,7 +345,7 @@ gvx_status gvx_add_channel(gvx_grid* g, int chan, int type, int apron)
     ch.type = type;
     ch.ncomp = ncomp;
     ch.elem_bytes = eb;
-    ch.apron_valid = false;
+    apron_invalidate(ch);
     ch.slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
     const size_t bytes = (size_t)ch.slots * g->P * g->P * g->P * eb;
     GVX_CK(gvx_ensure(ch.data, bytes));
@@ -351,7 +362,7 @@ gvx_status gvx_clear_channel(gvx_grid* g, int chan)
     }
     GvxChannel& ch = g->ch[chan];
     GVX_CK(cudaMemsetAsync(ch.data.p, 0, (size_t)ch.slots * g->P * g->P * g->P * ch.elem_bytes, g->stream));
-    ch.apron_valid = false;
+    apron_invalidate(ch);
     return GVX_OK;
 }
 
@@ -363,7 +374,7 @@ gvx_status gvx_fill_channel(gvx_grid* g, int chan, const float value[4])
         return GVX_ERR_INVALID_ARG;
     }
     GvxChannel& ch = g->ch[chan];
-    ch.apron_valid = false;
+    apron_invalidate(ch);
     uint4 pat = make_uint4(0, 0, 0, 0);
     unsigned char* pb = (unsigned char*)&pat;
     if (ch.type == GVX_T_FLOAT) {
@@ -544,6 +555,8 @@ gvx_status gvx_clear(gvx_grid* g)
     g->rebuild_topo = true;
     g->lookup_valid = g->group_valid = g->atlas_valid = g->nbr_valid = g->sc_valid = false;
     g->perm_valid = false;
+    g->pools_appended = false;
+    g->atlas_prefix = -1;
     g->topo_gen++;
     return GVX_OK;
 }
@@ -607,12 +620,17 @@ gvx_status gvx_splat(gvx_grid* g, int mode, int n, float radius, const float tra
 
 static gvx_status update_apron_one(gvx_grid* g, int chan, float boundval)
 {
-    if (chan >= 0 && chan < GVX_MAXCH && g->ch[chan].used && g->ch[chan].apron_valid &&
-        g->ch[chan].apron_bv == boundval && g->atlas_valid)
-        return GVX_OK;  // the apron already holds these copies (written by the splat)
-    gvx_status rc = gvx_apron_run(g, chan, boundval);
+    const bool known = chan >= 0 && chan < GVX_MAXCH && g->ch[chan].used && g->atlas_valid &&
+                       g->ch[chan].apron_bv == boundval;
+    if (known && g->ch[chan].apron_valid) return GVX_OK;  // the apron already holds these copies (the splat's)
+    gvx_status rc;
+    if (known && g->ch[chan].apron_partial_from >= 0 && g->nbr_valid)
+        rc = gvx_apron_run_partial(g, chan, boundval, g->ch[chan].apron_partial_from);  // new bricks + neighbours
+    else
+        rc = gvx_apron_run(g, chan, boundval);
     if (rc) return rc;
     g->ch[chan].apron_valid = true;
+    g->ch[chan].apron_partial_from = -1;
     g->ch[chan].apron_bv = boundval;
     return GVX_OK;
 }
@@ -865,7 +883,7 @@ gvx_status gvx_channel_device_ptr(gvx_grid* g, int chan, void** dev_ptr, int64_t
         return GVX_ERR_INVALID_ARG;
     }
     *dev_ptr = g->ch[chan].data.p;
-    g->ch[chan].apron_valid = false;  // the caller may write the voxels: UpdateApron runs again
+    apron_invalidate(g->ch[chan]);  // the caller may write the voxels: UpdateApron runs again
     return GVX_OK;
 }
 

@@ -31,6 +31,7 @@ struct ApronArgs {
     const uint2* tab;  // per apron voxel: padded index | neighbour << 24, source index in the neighbour
     int napron;
     void* data;
+    const unsigned char* only;  // optional per-slot mark: bricks whose aprons are copied (others kept)
 };
 
 template <class T>
@@ -43,6 +44,7 @@ __global__ void __launch_bounds__(kApronWarps * 32) k_apron(ApronArgs a, T bound
     const int P3 = a.P * a.P * a.P;
     T* data = (T*)a.data;
     for (uint32_t s = wglobal; s < a.nslots; s += nwarps) {
+        if (a.only && !a.only[s]) continue;  // warp-uniform: one brick per warp
         const int leaf = a.slot_leaf[s];
         if (lane < 27) {
             const int nl = a.nbr[(size_t)leaf * 27 + lane];
@@ -174,11 +176,55 @@ gvx_status gvx_apron_faces_run(gvx_grid* g, int chan)
     k_apron_faces<<<blocks, kApronWarps * 32, 0, g->stream>>>(a);
     g->launches++;
     GVX_CK(cudaGetLastError());
-    g->ch[chan].apron_valid = false;  // edges and corners are not updated
+    apron_invalidate(g->ch[chan]);  // edges and corners are not updated
     return GVX_OK;
 }
 
-gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval)
+// marks the bricks of slots >= from (added by an appending topology build) and their 26
+// neighbours: the bricks whose aprons may differ from the neighbours' interiors
+__global__ void k_apron_mark(uint32_t from, uint32_t nslots, const int* __restrict__ slot_leaf,
+                             const int* __restrict__ leaf_slot, const int* __restrict__ nbr, unsigned char* mark)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t s = from + i / 27;
+    if (s >= nslots) return;
+    const int k = (int)(i % 27);
+    const int leaf = slot_leaf[s];
+    if (k == 13) {
+        mark[s] = 1;
+        return;
+    }
+    const int nl = nbr[(size_t)leaf * 27 + k];
+    if (nl < 0) return;
+    const int ns = leaf_slot[nl];
+    if (ns >= 0) mark[ns] = 1;
+}
+
+static gvx_status apron_launch(gvx_grid* g, int chan, float boundval, const unsigned char* only);
+
+gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval) { return apron_launch(g, chan, boundval, nullptr); }
+
+gvx_status gvx_apron_run_partial(gvx_grid* g, int chan, float boundval, int64_t from)
+{
+    if (g->apron == 0) return GVX_OK;
+    const int64_t used = g->atlas_used;
+    if (from >= used) return GVX_OK;  // no new brick: every apron holds its copies
+    if (g->apron_mark_from != from || g->apron_mark_gen != g->atlas_gen) {
+        // the marks are shared by the channels of one UpdateAtlas
+        GVX_CK(gvx_ensure(g->apron_mark, (size_t)used));
+        GVX_CK(cudaMemsetAsync(g->apron_mark.p, 0, (size_t)used, g->stream));
+        const uint64_t work = (uint64_t)(used - from) * 27u;
+        k_apron_mark<<<(unsigned)((work + 255) / 256), 256, 0, g->stream>>>(
+            (uint32_t)from, (uint32_t)used, g->slot_leaf.as<int>(), g->leaf_slot.as<int>(), g->nbr.as<int>(),
+            g->apron_mark.as<unsigned char>());
+        g->launches++;
+        g->apron_mark_from = from;
+        g->apron_mark_gen = g->atlas_gen;
+    }
+    return apron_launch(g, chan, boundval, g->apron_mark.as<unsigned char>());
+}
+
+static gvx_status apron_launch(gvx_grid* g, int chan, float boundval, const unsigned char* only)
 {
     if (chan < 0 || chan >= GVX_MAXCH || !g->ch[chan].used) {
         gvx_set_error("UpdateApron: channel %d does not exist", chan);
@@ -206,6 +252,7 @@ gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval)
     a.leaf_slot = g->leaf_slot.as<int>();
     a.nbr = g->nbr.as<int>();
     a.data = g->ch[chan].data.p;
+    a.only = only;
     if (a.nslots == 0) return GVX_OK;
     const unsigned threads = kApronWarps * 32;
     const uint64_t warps_needed = a.nslots;

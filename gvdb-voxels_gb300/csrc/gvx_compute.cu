@@ -191,7 +191,7 @@ extern "C" gvx_status gvx_compute(gvx_grid* g, int effect, int chan, int iterati
         }
         g->launches++;
         GVX_CK(cudaGetLastError());
-        ch.apron_valid = false;
+        apron_invalidate(ch);
         if (update_apron) {
             gvx_status rc = gvx_update_apron(g, chan, boundval);
             if (rc) return rc;

@@ -584,8 +584,8 @@ gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radiu
         k_gather_fp16<8><<<blocks, 256, 0, g->stream>>>(a);
     g->launches++;
     GVX_CK(cudaGetLastError());
-    g->ch[cl].apron_valid = false;
-    if (a.clr_out) g->ch[chan_clr].apron_valid = false;
+    apron_invalidate(g->ch[cl]);
+    if (a.clr_out) apron_invalidate(g->ch[chan_clr]);
     return GVX_OK;
 }
 
@@ -639,7 +639,7 @@ gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, 
         k_gather<8><<<blocks, 256, 0, g->stream>>>(a);
     g->launches++;
     GVX_CK(cudaGetLastError());
-    g->ch[chan].apron_valid = false;  // the gathers write interior voxels only
-    if (a.clr_out) g->ch[chan_clr].apron_valid = false;
+    apron_invalidate(g->ch[chan]);  // the gathers write interior voxels only
+    if (a.clr_out) apron_invalidate(g->ch[chan_clr]);
     return GVX_OK;
 }

@@ -13,7 +13,17 @@ struct GvxChannel {
     int64_t slots = 0;
     bool apron_valid = false;  // apron voxels hold the neighbours' interior values / boundval
     float apron_bv = 0.f;      // the boundary value they were filled with
+    // >= 0: the apron holds those copies except in the bricks of slots >= apron_partial_from
+    // (added by an appending topology build) and their neighbours
+    int64_t apron_partial_from = -1;
 };
+
+// the channel's apron no longer holds the neighbours' values anywhere it is known to
+inline void apron_invalidate(GvxChannel& ch)
+{
+    ch.apron_valid = false;
+    ch.apron_partial_from = -1;
+}
 
 struct GvxPoints {
     int n = 0;
@@ -115,6 +125,12 @@ struct gvx_grid {
     DevBuf amap;       // 4 ints per slot
     DevBuf apron_tab;  // apron voxel table of the apron kernel, for bricks of side apron_tab_P
     int apron_tab_P = 0;
+    int64_t atlas_prefix = -1;  // UpdateAtlas gave leaf i slot i for every leaf < atlas_prefix (all active)
+    bool pools_appended = false;  // the last topology build kept the pools' nodes and only appended
+    DevBuf apron_mark;            // per slot: 1 = its apron needs the copies (partial UpdateApron)
+    int64_t apron_mark_from = -1; // the marks are those of slots >= apron_mark_from ...
+    uint64_t apron_mark_gen = 0;  // ... for the atlas of this generation
+    uint64_t atlas_gen = 0;       // bumped by every UpdateAtlas
     DevBuf atlas_tmp;  // second atlas of the unpacked (Jacobi) smoothing
 
     // points
@@ -150,6 +166,7 @@ struct gvx_grid {
     DevBuf d_rmax;  // float bits of the largest per-point radius of the last point permute
     DevBuf d_next;  // work-unit counter of the splat launch
     void* h_pin = nullptr;  // pinned staging of the topology's small readbacks
+    struct gvx_topo_staged* staged = nullptr;  // a staged RebuildTopology between its stages (batches)
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index
@@ -201,6 +218,13 @@ gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr);
 gvx_status gvx_wait_attributes(gvx_grid* g);
 gvx_status gvx_wait_positions(gvx_grid* g);
 gvx_status gvx_topo_compute_bounds(gvx_grid* g);
+// RebuildTopology in three stages (for batches of grids; see gvx_topology.cu): between two
+// stages of one grid the host may queue other grids' work, so that one synchronisation per
+// stage serves the whole batch
+gvx_status gvx_topo_stage1(gvx_grid* g, int n, float radius, int mode, int min_depth);
+gvx_status gvx_topo_stage2(gvx_grid* g);
+gvx_status gvx_topo_stage3(gvx_grid* g);
+void gvx_topo_staged_free(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
 // InsertPoints: grouping + sorted attribute arrays
 gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel);
@@ -215,6 +239,9 @@ gvx_status gvx_gather_run(gvx_grid* g, int levelset, int subcell, float radius, 
 
 // apron (gvx_apron.cu)
 gvx_status gvx_apron_run(gvx_grid* g, int chan, float boundval);
+// UpdateApron of the bricks of slots >= from and of their neighbours only (the other aprons
+// already hold the copies)
+gvx_status gvx_apron_run_partial(gvx_grid* g, int chan, float boundval, int64_t from);
 gvx_status gvx_apron_faces_run(gvx_grid* g, int chan);
 
 // channel storage (gvx_api.cu)

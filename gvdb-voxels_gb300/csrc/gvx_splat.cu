@@ -1064,15 +1064,18 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
 // accumulating splat started from an apron that was not a valid copy
 static void splat_finish(gvx_grid* g, int chan_d, int chan_v, int accum)
 {
-    bool valid_after = true;
-    if (accum) {
-        if (chan_d >= 0) valid_after &= g->ch[chan_d].apron_valid && g->ch[chan_d].apron_bv == 0.0f;
-        if (chan_v >= 0) valid_after &= g->ch[chan_v].apron_valid && g->ch[chan_v].apron_bv == 0.0f;
-    }
     for (int c : {chan_d, chan_v}) {
         if (c < 0) continue;
-        g->ch[c].apron_valid = valid_after;
-        g->ch[c].apron_bv = 0.0f;
+        GvxChannel& ch = g->ch[c];
+        if (!accum) {
+            ch.apron_valid = true;  // every apron voxel is the neighbour's sum, or 0 where no brick is
+            ch.apron_partial_from = -1;
+        } else if (ch.apron_bv != 0.0f) {
+            apron_invalidate(ch);
+        }
+        // accumulating onto copies (all of them, or all but those near new bricks) adds the same
+        // sums to both sides of every copy: the state is kept
+        ch.apron_bv = 0.0f;
     }
 }
 
@@ -1358,9 +1361,43 @@ gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads)
         gvx_set_error("null batch handle");
         return GVX_ERR_INVALID_ARG;
     }
+    if (mode < GVX_TOPO_AUTO || mode > GVX_TOPO_ACCUMULATE) {
+        gvx_set_error("BatchTopology: mode %d", mode);
+        return GVX_ERR_INVALID_ARG;
+    }
     const size_t n = b->grids.size();
     if (n == 0) return GVX_OK;
-    const size_t nt = std::min<size_t>(n, (size_t)std::max(1, threads > 0 ? threads : 8));
+    if (threads <= 0) {
+        // staged, from this thread: every grid's GetBoundingBox, then (one wait per grid, by
+        // then mostly passed) every grid's build up to its node counts, then every grid's
+        // pools, UpdateAtlas and InsertPoints; the grids' streams overlap on the GPU
+        GVX_CK(cudaSetDevice(b->device));
+        const char* what[3] = {"GetBoundingBox", "RebuildTopology", "pools/UpdateAtlas/InsertPoints"};
+        for (int stage = 0; stage < 3; stage++) {
+            for (size_t i = 0; i < n; i++) {
+                gvx_grid* g = b->grids[i];
+                gvx_status r = GVX_OK;
+                if (stage == 0) {
+                    r = gvx_wait_positions(g);
+                    if (r == GVX_OK) r = gvx_topo_stage1(g, g->pts.n, radius, mode, 1);
+                } else if (stage == 1) {
+                    r = gvx_topo_stage2(g);
+                } else {
+                    r = gvx_topo_stage3(g);
+                    if (r == GVX_OK) r = gvx_wait_attributes(g);
+                    if (r == GVX_OK) r = gvx_topo_update_atlas(g);
+                    if (r == GVX_OK) r = gvx_prepare_points(g, g->pts.n, nullptr, false);
+                }
+                if (r != GVX_OK) {
+                    const std::string m = gvx_last_error();
+                    gvx_set_error("BatchTopology: grid %zu (%s): %s", i, what[stage], m.c_str());
+                    return r;
+                }
+            }
+        }
+        return GVX_OK;
+    }
+    const size_t nt = std::min<size_t>(n, (size_t)threads);
     std::atomic<size_t> next{0};
     std::vector<gvx_status> st(n, GVX_OK);
     std::vector<std::string> msg(n);
@@ -1560,8 +1597,8 @@ gvx_status gvx_scatter_ref(gvx_grid* g, int n, float radius, const float trans[3
     a.clr_off = g->pts.clr_off;
     a.clr_stride = g->pts.clr_stride;
     a.clr_out = clr_mode ? g->ch[clr_chan].data.as<uint32_t>() : nullptr;
-    g->ch[0].apron_valid = false;
-    if (clr_mode) g->ch[clr_chan].apron_valid = false;
+    apron_invalidate(g->ch[0]);
+    if (clr_mode) apron_invalidate(g->ch[clr_chan]);
     if (a.nslots == 0) return GVX_OK;
     GVX_CK(cudaFuncSetAttribute(k_scatter_ref, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

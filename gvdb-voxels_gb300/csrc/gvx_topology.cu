@@ -1054,7 +1054,9 @@ gvx_status gvx_check_device_error(gvx_grid* g, const char* stage)
 
 // `bytes` (at most 256) of device memory and the device error word in one round
 // trip through pinned staging, then the error word reported as above
-static gvx_status readback_checked(gvx_grid* g, void* dst, const void* src, size_t bytes, const char* stage)
+// (queued: the copies into the staging; then, once the stream has passed them,
+// readback_finish takes the bytes and reports the error word)
+static gvx_status readback_start(gvx_grid* g, const void* src, size_t bytes, const char* stage)
 {
     if (bytes > 256) {
         gvx_set_error("%s: readback of %zu bytes", stage, bytes);
@@ -1063,11 +1065,22 @@ static gvx_status readback_checked(gvx_grid* g, void* dst, const void* src, size
     if (!g->h_pin) GVX_CK(cudaMallocHost(&g->h_pin, 512));
     GVX_CK(cudaMemcpyAsync(g->h_pin, src, bytes, cudaMemcpyDeviceToHost, g->stream));
     GVX_CK(cudaMemcpyAsync((char*)g->h_pin + 256, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    return GVX_OK;
+}
+
+static gvx_status readback_finish(gvx_grid* g, void* dst, size_t bytes, const char* stage)
+{
     GVX_CK(cudaStreamSynchronize(g->stream));
     memcpy(dst, g->h_pin, bytes);
     uint32_t e = 0;
     memcpy(&e, (const char*)g->h_pin + 256, sizeof(e));
     return report_device_error(g, e, stage);
+}
+
+static gvx_status readback_checked(gvx_grid* g, void* dst, const void* src, size_t bytes, const char* stage)
+{
+    gvx_status rc = readback_start(g, src, bytes, stage);
+    return rc ? rc : readback_finish(g, dst, bytes, stage);
 }
 
 static gvx_status ensure_grid_scratch(gvx_grid* g)
@@ -1167,8 +1180,23 @@ static gvx_status grow_nodes(gvx_grid* g, int lev, int64_t cnt)
 }
 
 // FULL rebuild: ActivateBricksGPU + ActivateExtraBricksGPU semantics
-static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], int depth, const int rootpos[3],
-                            const float mn[3], const float mx[3])
+// A full build between its counts readback being queued and being read: what
+// topo_full_complete needs of topo_full_launch.
+struct FullBuild {
+    int n;
+    float radius;
+    float o[3];
+    int depth;
+    int rootpos[3];
+    KeySpace ks;
+    uint32_t words0;
+    UpperDesc ud;
+};
+
+// Everything of a full build (VG.cpp:1229-1413) up to the node counts, which are
+// queued for the host; topo_full_complete reads them and writes the pools.
+static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float o[3], int depth,
+                                   const int rootpos[3], const float mn[3], const float mx[3], FullBuild& fb)
 {
     cudaStream_t st = g->stream;
     const int b = g->brick;
@@ -1274,8 +1302,34 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
     GVX_CK(cudaGetLastError());
 
     // ---- counts to the host (the one mid-build synchronisation)
+    fb.n = n;
+    fb.radius = radius;
+    fb.depth = depth;
+    for (int a = 0; a < 3; a++) {
+        fb.o[a] = o[a];
+        fb.rootpos[a] = rootpos[a];
+    }
+    fb.ks = ks;
+    fb.words0 = words0;
+    fb.ud = ud;
+    return readback_start(g, counts, 64 * sizeof(uint32_t), "RebuildTopology");
+}
+
+static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
+{
+    cudaStream_t st = g->stream;
+    const int n = fb.n, depth = fb.depth;
+    const float* o = fb.o;
+    const int* rootpos = fb.rootpos;
+    const KeySpace ks = fb.ks;
+    const uint32_t words0 = fb.words0;
+    const UpperDesc& ud = fb.ud;
+    const uint32_t* counts = g->d_counts.as<uint32_t>();
+    (void)counts;
+    const BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
+    const BitRank x0{g->x0_bits.as<uint32_t>(), g->x0_prefix.as<uint32_t>(), words0};
     uint32_t hc[64];
-    rc = readback_checked(g, hc, counts, sizeof(hc), "RebuildTopology");
+    gvx_status rc = readback_finish(g, hc, sizeof(hc), "RebuildTopology");
     if (rc) return rc;
     const uint32_t U0 = hc[0], X0 = hc[1];
     uint32_t Ul[GVX_MAXLEV] = {}, Xl[GVX_MAXLEV] = {};
@@ -1400,6 +1454,14 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
     return GVX_OK;
 }
 
+static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], int depth, const int rootpos[3],
+                            const float mn[3], const float mx[3])
+{
+    FullBuild fb{};
+    gvx_status rc = topo_full_launch(g, n, radius, o, depth, rootpos, mn, mx, fb);
+    return rc ? rc : topo_full_complete(g, fb);
+}
+
 // slots of d_counts read back by the incremental build
 enum { kCntNew = 0, kCntD0 = 20, kCntActive = 48 };
 
@@ -1424,8 +1486,12 @@ static gvx_status grow_keep(gvx_grid* g, DevBuf& b, size_t bytes, size_t keep)
 
 // leaf lookup over the ACTIVE leaves in key space `ks` (bitmap + rank -> pool
 // index), the per-leaf keys, the neighbour table and the point ranges of the
-// grouping made in `ks`; with read_used, the active count becomes used_leaves
-static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t words0, bool read_used)
+// grouping made in `ks`.  readback: kReadUsed = the active count becomes
+// used_leaves (one synchronisation, with the device error word); kReadError =
+// the device error word only; kReadNone = no synchronisation (the caller knows
+// the active count; a device error stays in the word for the next readback)
+enum { kReadNone = 0, kReadError = 1, kReadUsed = 2 };
+static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t words0, int readback)
 {
     cudaStream_t st = g->stream;
     const uint32_t L0 = (uint32_t)g->count[0];
@@ -1466,11 +1532,15 @@ static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t 
     g->nbr_valid = true;
     rc = fill_leaf_ranges(g, L0);
     if (rc) return rc;
-    if (read_used) {
+    if (readback == kReadUsed) {
         uint32_t used = 0;
         gvx_status rc = readback_checked(g, &used, counts + kCntActive, 4, "RebuildTopology");
         if (rc) return rc;
         g->used_leaves = used;
+        return GVX_OK;
+    }
+    if (readback == kReadNone) {
+        GVX_CK(cudaGetLastError());
         return GVX_OK;
     }
     return gvx_check_device_error(g, "RebuildTopology");
@@ -1640,7 +1710,7 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
     g->group_valid = false;  // the grouping now follows `ks`
     if (total_new == 0) {
         // no new node: the reference returns before it applies the markers (VG.cpp:1066)
-        rc = build_active_lookup(g, ks, words0, false);
+        rc = build_active_lookup(g, ks, words0, accum ? kReadNone : kReadError);
         if (rc) return rc;
         g->last_rebuild = 0;
     } else {
@@ -1719,8 +1789,11 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
             g->launches++;
         }
         GVX_CK(cudaGetLastError());
-        rc = build_active_lookup(g, ks, words0, true);
+        // accumulating, no leaf is delinked and a dead one stays dead (its parent reference is
+        // gone, k_apply_markers): the active count grows by the new leaves, known on the host
+        rc = build_active_lookup(g, ks, words0, accum ? kReadNone : kReadUsed);
         if (rc) return rc;
+        if (accum) g->used_leaves += nnew[0];
         g->atlas_valid = false;
         g->last_rebuild = 2;
     }
@@ -1735,6 +1808,7 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
 // touches anything; any later failure leaves no usable tree
 static gvx_status incremental_status(gvx_grid* g, gvx_status rc)
 {
+    if (rc == GVX_OK) g->pools_appended = true;  // the pools kept their nodes, new ones appended
     if (rc == GVX_OK || rc == GVX_ERR_UNSUPPORTED || rc == GVX_ERR_DEPTH) return rc;
     g->rebuild_topo = true;
     g->root_level = -1;
@@ -1743,7 +1817,22 @@ static gvx_status incremental_status(gvx_grid* g, gvx_status rc)
     return rc;
 }
 
-gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
+// the grid's state after a full build: a failed one leaves no usable tree
+static gvx_status full_status(gvx_grid* g, gvx_status rc)
+{
+    if (rc) {
+        g->root_level = -1;
+        g->lookup_valid = false;
+        g->group_valid = false;
+        return rc;
+    }
+    g->rebuild_topo = false;
+    g->last_rebuild = 1;
+    return GVX_OK;
+}
+
+// RebuildTopology up to GetBoundingBox's readback, which is queued
+static gvx_status rebuild_begin(gvx_grid* g, int n, float radius, const float orig[3], int mode)
 {
     if (!g->configured) {
         gvx_set_error("RebuildTopology: Configure was not called");
@@ -1760,9 +1849,11 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     gvx_status rc = ensure_grid_scratch(g);
     if (rc) return rc;
     g->sc_valid = false;
+    g->pools_appended = false;
     const float o[3] = {orig ? orig[0] : 0.f, orig ? orig[1] : 0.f, orig ? orig[2] : 0.f};
     cudaStream_t st = g->stream;
-    GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, st));
+    // (the device error word is not cleared here: an error left by the unchecked tail of an
+    // accumulating build is reported by this build's first readback)
 
     // ---- GetBoundingBox: one reduction, 24 bytes to the host
     uint32_t init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
@@ -1782,9 +1873,18 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
                                                                      (uint32_t)g->count[0], g->range[0], act_dev);
         g->launches++;
     }
-    uint32_t hb[14];
-    rc = readback_checked(g, hb, g->d_bbox.p, sizeof(hb), "GetBoundingBox");
-    if (rc) return rc;
+    return readback_start(g, g->d_bbox.p, 14 * sizeof(uint32_t), "GetBoundingBox");
+}
+
+// the rest of RebuildTopology, from the bounding box (and active-leaf box) read
+// back; a full build with `fb` stops after queueing its counts readback (*pending),
+// for topo_full_complete
+static gvx_status rebuild_after_bbox(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth,
+                                     const uint32_t hb[14], FullBuild* fb, bool* pending)
+{
+    gvx_status rc = GVX_OK;
+    const float o[3] = {orig ? orig[0] : 0.f, orig ? orig[1] : 0.f, orig ? orig[2] : 0.f};
+    if (pending) *pending = false;
     float mn[3], mx[3];
     int pmin[3], pmax[3];
     for (int a = 0; a < 3; a++) {
@@ -1838,17 +1938,79 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
     }
     g->topo_gen++;  // the device tree changes (or is rebuilt) from here on
     if (!g->rebuild_topo) return incremental_status(g, topo_incremental(g, n, radius, o, depth, false, mn, mx, act));
-    rc = topo_full(g, n, radius, o, depth, rootpos, mn, mx);
-    if (rc) {
-        g->root_level = -1;
-        g->lookup_valid = false;
-        g->group_valid = false;
-        return rc;
+    g->atlas_prefix = -1;  // the pools are rebuilt from scratch
+    if (fb) {
+        rc = topo_full_launch(g, n, radius, o, depth, rootpos, mn, mx, *fb);
+        if (rc == GVX_OK) {
+            *pending = true;
+            return GVX_OK;
+        }
+    } else {
+        rc = topo_full(g, n, radius, o, depth, rootpos, mn, mx);
     }
-    g->rebuild_topo = false;
-    g->last_rebuild = 1;
-    return GVX_OK;
+    return full_status(g, rc);
 }
+
+gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
+{
+    gvx_status rc = rebuild_begin(g, n, radius, orig, mode);
+    if (rc) return rc;
+    uint32_t hb[14];
+    rc = readback_finish(g, hb, sizeof(hb), "GetBoundingBox");
+    if (rc) return rc;
+    return rebuild_after_bbox(g, n, radius, orig, mode, min_depth, hb, nullptr, nullptr);
+}
+
+// Staged RebuildTopology for batches of grids (gvx_batch_topology): stage 1
+// queues GetBoundingBox and its readback; stage 2, once the grid's stream has
+// passed it, reads the box and queues a full build up to its node counts (any
+// other kind of build runs to its end here); stage 3 reads the counts and
+// finishes the full build.  The host waits on a grid only where its stream
+// has had the time of the other grids' stages to get there.
+struct gvx_topo_staged {
+    int n;
+    float radius;
+    int mode, min_depth;
+    bool pending;
+    FullBuild fb;
+};
+
+gvx_status gvx_topo_stage1(gvx_grid* g, int n, float radius, int mode, int min_depth)
+{
+    if (!g->staged) g->staged = new gvx_topo_staged();
+    gvx_topo_staged& S = *g->staged;
+    S.n = n;
+    S.radius = radius;
+    S.mode = mode;
+    S.min_depth = min_depth;
+    S.pending = false;
+    return rebuild_begin(g, n, radius, nullptr, mode);
+}
+
+gvx_status gvx_topo_stage2(gvx_grid* g)
+{
+    gvx_topo_staged& S = *g->staged;
+    uint32_t hb[14];
+    gvx_status rc = readback_finish(g, hb, sizeof(hb), "GetBoundingBox");
+    if (rc) return rc;
+    return rebuild_after_bbox(g, S.n, S.radius, nullptr, S.mode, S.min_depth, hb, &S.fb, &S.pending);
+}
+
+gvx_status gvx_topo_stage3(gvx_grid* g)
+{
+    gvx_topo_staged& S = *g->staged;
+    if (!S.pending) return GVX_OK;
+    S.pending = false;
+    return full_status(g, topo_full_complete(g, S.fb));
+}
+
+void gvx_topo_staged_free(gvx_grid* g)
+{
+    delete g->staged;
+    g->staged = nullptr;
+}
+
+
 
 // A tree given as node pools and child lists (LoadVBX, VG.cpp:507-686: Configure, PoolRead per level,
 // FinishTopology).  The pools are taken as they are; the leaf lookup, leaf keys and neighbour table
@@ -1913,6 +2075,8 @@ gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, c
     }
     g->root_level = R;
     g->topo_gen++;
+    g->pools_appended = false;
+    g->atlas_prefix = -1;
     for (int a = 0; a < 3; a++) g->root_pos[a] = root.pos[a];
     g->rebuild_topo = true;
     g->last_rebuild = 1;
@@ -1923,7 +2087,7 @@ gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, c
     g->atlas_valid = false;
     GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, st));
     const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << total_bits) / 32ull));
-    return build_active_lookup(g, ks, words0, true);
+    return build_active_lookup(g, ks, words0, kReadUsed);
 }
 
 gvx_status gvx_topo_update_atlas(gvx_grid* g)
@@ -1938,6 +2102,14 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     }
     cudaStream_t st = g->stream;
     const int64_t used = g->used_leaves;
+    // Slots go to the active leaves in pool order.  When the last UpdateAtlas gave every leaf
+    // below atlas_prefix its own index as slot and the build since only appended leaves, all of
+    // them active (AccumulateTopology), those leaves keep their slots and values: the aprons stay
+    // copies except in the new bricks and around them.
+    const int64_t from = g->pools_appended && g->atlas_prefix >= 0 && g->atlas_prefix <= used &&
+                                 used == g->count[0]
+                             ? g->atlas_prefix
+                             : -1;
     gvx_status rc = gvx_grow_atlas(g, used);
     if (rc) return rc;
     const int64_t slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
@@ -1965,7 +2137,17 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     g->atlas_used = used;
     g->atlas_valid = true;
     g->sc_valid = false;  // subcell indices follow the atlas slots
-    for (int c = 0; c < GVX_MAXCH; c++) g->ch[c].apron_valid = false;  // bricks moved to new slots
+    for (int c = 0; c < GVX_MAXCH; c++) {
+        GvxChannel& ch = g->ch[c];
+        if (from < 0 || !(ch.apron_valid || ch.apron_partial_from >= 0)) {
+            apron_invalidate(ch);  // bricks moved to new slots
+        } else if (from < used) {
+            ch.apron_partial_from = ch.apron_valid ? from : std::min(ch.apron_partial_from, from);
+            ch.apron_valid = false;
+        }
+    }
+    g->atlas_prefix = used == g->count[0] ? used : -1;
+    g->atlas_gen++;
     return GVX_OK;
 }
 

@@ -406,7 +406,7 @@ extern "C" gvx_status gvx_load_vbx(gvx_grid* g, const char* path, int force_majo
             }
             GVX_CK(cudaMemcpyAsync(g->ch[c].data.p, bm.data(), bm.size(), cudaMemcpyHostToDevice, g->stream));
             GVX_CK(cudaStreamSynchronize(g->stream));
-            g->ch[c].apron_valid = false;
+            apron_invalidate(g->ch[c]);
         }
     }
     return GVX_OK;

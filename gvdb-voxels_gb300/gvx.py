@@ -471,8 +471,8 @@ class Batch:
         self._check(self.lib.gvx_batch_splat(self.h, mode, float(radius), chan_density, chan_vel, int(accum), flags))
 
     def topology(self, radius, mode=None, threads=0):
-        """gvx_batch_topology: RebuildTopology + UpdateAtlas + InsertPoints of every grid, from a
-        pool of host threads"""
+        """gvx_batch_topology: RebuildTopology + UpdateAtlas + InsertPoints of every grid, staged
+        from this thread (threads 0) or as per-grid calls from a pool of host threads"""
         self._check(self.lib.gvx_batch_topology(self.h, float(radius), TOPO_FULL if mode is None else mode,
                                                 int(threads)))
 

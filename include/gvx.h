@@ -393,12 +393,16 @@ gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count);
 gvx_status gvx_batch_splat(gvx_batch* b, int mode, float radius, int chan_density, int chan_vel, int accum,
                            int flags);
 gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_sm, float* ms);
-/* Topology of every grid of the batch (no reference counterpart): per grid, the
- * calls gvx_rebuild_topology(radius, no origin, mode), gvx_update_atlas and
- * gvx_insert_points over its bound points, as a caller would make them, made
- * from `threads` host threads at once (0: 8) so that the grids' builds overlap
- * on the GPU.  Grids that share a stream still build one after another.  The
- * first failing grid's status is returned, its index in gvx_last_error(). */
+/* Topology of every grid of the batch (no reference counterpart): per grid, what
+ * gvx_rebuild_topology(radius, no origin, mode), gvx_update_atlas and
+ * gvx_insert_points over its bound points do, with the same results.
+ * threads == 0: staged from the calling thread -- every grid's GetBoundingBox is
+ * queued, then every grid's build up to its node counts, then every grid's pools,
+ * UpdateAtlas and InsertPoints -- so the host waits on each grid twice, where the
+ * stream has had the other grids' launches to get there, and the grids' streams
+ * overlap on the GPU.  threads > 0: the per-grid calls themselves from that many
+ * host threads.  Grids that share a stream build one after another.  The first
+ * failing grid's status is returned, its index in gvx_last_error(). */
 gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads);
 
 /* Test hook (no reference counterpart): one pass of the radix sort over n > 4096

@@ -28,7 +28,10 @@
 //   - key buffers are sized generously (the reference's N*depth buffer can overflow);
 //   - ScatterDensity is launched with the kernel's own argument list (the
 //     reference host call omits the VDBInfo pointer, VG.cpp:5645);
-//   - channels are cleared by uploading zeros (kernelFillTex writes 4 bytes per element).
+//   - float channels are cleared by the reference's own kernelFillTex (AtlasFill);
+//     channels of wider voxels by a device copy of zeros (kernelFillTex writes 4
+//     bytes per voxel); the atlas grows by a device array-to-array copy as
+//     AllocateTextureGPU preserves its data.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -113,6 +116,8 @@ struct Mod {
     CUmodule m = nullptr;
     CUfunction splitpos, calcbrick, link, extra, increextra, delinkleaf, delink, insertpts, scatter, setflag,
         countsc, insertsc, scpos, gatherd, gatherl, apronf, apronf4, insertsc16, gatherl16, convxform;
+    CUmodule mcopy = nullptr;  // cuda_gvdb_copydata.ptx: kernelFillTex (Allocator::AtlasFill)
+    CUfunction filltex = nullptr;
 } g_mod;
 
 struct DBuf {
@@ -165,6 +170,7 @@ struct rh_grid {
     // aux
     DBuf range_res, keys, cnt, markers, splitx, splity, splitz;
     DBuf pnode, poff, gcnt;
+    DBuf zero;  // zero-filled source of device-side clears of array regions
     DBuf scflag, scmap, sccnt, scoff, scpts, scpos, scnid;
     int sc_len = 0, num_sc = 0;
     float3 pos_min{0, 0, 0}, pos_range{0, 0, 0};  // mPosMin, mPosRange of GetBoundingBox (VG.cpp:5452-5462)
@@ -470,23 +476,61 @@ int copy_host_array(rh_grid* g, int c, const void* src, void* dst, bool to_array
     return 0;
 }
 
-// AtlasResize (AL.cpp:622-650): new array, zeros, old content kept
+// voxel slices [z0, z1) of channel c's array set to zero on the device (a copy from a
+// zero-filled linear buffer; the array has sub[0] x sub[1] bricks per slice)
+int zero_array_slices(rh_grid* g, int c, CUarray arr, size_t z0, size_t z1)
+{
+    if (z1 <= z0) return 0;
+    const size_t W = (size_t)g->sub[0] * g->P, H = (size_t)g->sub[1] * g->P;
+    const size_t bytes = W * H * (z1 - z0) * g->ch[c].elem;
+    if (dens(g->zero, bytes)) return -1;
+    RH_CK(cuMemsetD8(g->zero.p, 0, bytes));
+    CUDA_MEMCPY3D cp;
+    memset(&cp, 0, sizeof(cp));
+    cp.srcMemoryType = CU_MEMORYTYPE_DEVICE;
+    cp.srcDevice = g->zero.p;
+    cp.srcPitch = W * g->ch[c].elem;
+    cp.srcHeight = H;
+    cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+    cp.dstArray = arr;
+    cp.dstZ = z0;
+    cp.WidthInBytes = W * g->ch[c].elem;
+    cp.Height = H;
+    cp.Depth = z1 - z0;
+    RH_CK(cuMemcpy3D(&cp));
+    return 0;
+}
+
+// AtlasResize (AL.cpp:622-650): a new array; the old content is kept by a
+// device array-to-array copy, as AllocateTextureGPU's "preserve" does
+// (AL.cpp:428-448); the new slices are zero
 int resize_atlas(rh_grid* g, int nz)
 {
     int old[3] = {g->sub[0], g->sub[1], g->sub[2]};
     for (int c = 0; c < 32; c++) {
         if (!g->ch[c].used) continue;
-        size_t oldbytes = (size_t)old[0] * g->P * old[1] * g->P * old[2] * g->P * g->ch[c].elem;
-        std::vector<unsigned char> keep(oldbytes);
-        g->sub[2] = old[2];
-        if (copy_host_array(g, c, nullptr, keep.data(), false)) return -1;
+        CUarray na = nullptr;
+        CUsurfObject ns = 0;
+        if (make_array(g, c, old[0], old[1], nz, &na, &ns)) return -1;
+        const size_t W = (size_t)old[0] * g->P, H = (size_t)old[1] * g->P;
+        const size_t keep_z = (size_t)std::min(old[2], nz) * g->P;
+        if (keep_z) {
+            CUDA_MEMCPY3D cp;
+            memset(&cp, 0, sizeof(cp));
+            cp.srcMemoryType = CU_MEMORYTYPE_ARRAY;
+            cp.srcArray = g->ch[c].arr;
+            cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+            cp.dstArray = na;
+            cp.WidthInBytes = W * g->ch[c].elem;
+            cp.Height = H;
+            cp.Depth = keep_z;
+            RH_CK(cuMemcpy3D(&cp));
+        }
+        if (zero_array_slices(g, c, na, keep_z, (size_t)nz * g->P)) return -1;
         cuSurfObjectDestroy(g->ch[c].surf);
         cuArrayDestroy(g->ch[c].arr);
-        if (make_array(g, c, old[0], old[1], nz, &g->ch[c].arr, &g->ch[c].surf)) return -1;
-        g->sub[2] = nz;
-        std::vector<unsigned char> full((size_t)old[0] * g->P * old[1] * g->P * nz * g->P * g->ch[c].elem, 0);
-        memcpy(full.data(), keep.data(), oldbytes);
-        if (copy_host_array(g, c, full.data(), nullptr, true)) return -1;
+        g->ch[c].arr = na;
+        g->ch[c].surf = ns;
     }
     g->sub[2] = nz;
     return 0;
@@ -521,6 +565,14 @@ int rh_load(const char* module_ptx)
               {&g_mod.apronf4, "gvdbUpdateApronF4"},      {&g_mod.insertsc16, "gvdbInsertSubcell_fp16"},
               {&g_mod.gatherl16, "gvdbGatherLevelSet_fp16"}, {&g_mod.convxform, "gvdbConvAndTransform"}};
     for (auto& e : fs) RH_CK(cuModuleGetFunction(e.f, g_mod.m, e.name));
+    // the copy-data module beside it (ClearChannel's fill kernel), when it was built
+    std::string cp = module_ptx;
+    const size_t at = cp.rfind("cuda_gvdb_module.ptx");
+    if (at != std::string::npos) {
+        cp.replace(at, strlen("cuda_gvdb_module.ptx"), "cuda_gvdb_copydata.ptx");
+        if (cuModuleLoad(&g_mod.mcopy, cp.c_str()) == CUDA_SUCCESS)
+            RH_CK(cuModuleGetFunction(&g_mod.filltex, g_mod.mcopy, "kernelFillTex"));
+    }
     g_mod.loaded = true;
     return 0;
 }
@@ -558,7 +610,7 @@ void rh_destroy(rh_grid* g)
         }
     DBuf* bufs[] = {&g->damap, &g->dinfo, &g->dpos, &g->range_res, &g->keys, &g->cnt, &g->markers, &g->splitx,
                     &g->splity, &g->splitz, &g->pnode, &g->poff, &g->gcnt, &g->scflag, &g->scmap, &g->sccnt,
-                    &g->scoff, &g->scpts, &g->scpos, &g->scnid};
+                    &g->scoff, &g->scpts, &g->scpos, &g->scnid, &g->zero};
     for (DBuf* b : bufs)
         if (b->p) cuMemFree(b->p);
     for (int l = 0; l < 10; l++) {
@@ -702,10 +754,23 @@ int rh_update_atlas(rh_grid* g)
     return commit_pools(g);
 }
 
+// ClearChannel (VG.cpp:1596-1603) -> Allocator::AtlasFill (AL.cpp:813-822):
+// kernelFillTex (cuda_gvdb_copydata.cu:21-27) over the atlas in 8^3 blocks.  That
+// kernel writes one 4-byte zero per voxel, which clears float channels; wider
+// voxels are cleared by a device copy of zeros instead (the reference's fill
+// leaves their other components as they were).
 int rh_clear_channel(rh_grid* g, int c)
 {
-    std::vector<unsigned char> z((size_t)g->sub[0] * g->P * g->sub[1] * g->P * g->sub[2] * g->P * g->ch[c].elem, 0);
-    return copy_host_array(g, c, z.data(), nullptr, true);
+    if (g_mod.filltex && g->ch[c].elem == 4) {
+        int3 res = make_int3(g->sub[0] * g->P, g->sub[1] * g->P, g->sub[2] * g->P);
+        int dsize = g->ch[c].elem;
+        CUsurfObject so = g->ch[c].surf;
+        void* args[] = {&res, &dsize, &so};
+        if (launch(g_mod.filltex, res.x / 8 + 1, res.y / 8 + 1, res.z / 8 + 1, 8, 8, 8, args)) return -1;
+        RH_CK(cuCtxSynchronize());
+        return 0;
+    }
+    return zero_array_slices(g, c, g->ch[c].arr, 0, (size_t)g->sub[2] * g->P);
 }
 
 int rh_write_channel_dense(rh_grid* g, int c, const void* src) { return copy_host_array(g, c, src, nullptr, true); }

@@ -106,9 +106,11 @@ def test_batch_autotune_keeps_results(gvx_mod):
     b.close()
 
 
-def test_batch_topology_matches_per_grid_builds(gvx_mod):
-    """gvx_batch_topology from 4 host threads, grids on their own streams: the same pools, child lists,
-    atlas maps and point groupings (checked through a splat) as one-by-one builds"""
+@pytest.mark.parametrize("threads", [0, 4])
+def test_batch_topology_matches_per_grid_builds(gvx_mod, threads):
+    """gvx_batch_topology staged from one host thread (threads 0) or from 4 host threads, grids on
+    their own streams: the same pools, child lists, atlas maps and point groupings (checked through
+    a splat) as one-by-one builds"""
     cl = clouds(9, 11)
     ref = make_grids(gvx_mod, cl, radius=1.0)
     grids = []
@@ -120,12 +122,13 @@ def test_batch_topology_matches_per_grid_builds(gvx_mod):
         grids.append(g)
     b = gvx_mod.Batch(0)
     b.set_grids(grids)
-    b.topology(1.0, threads=4)
+    b.topology(1.0, threads=threads)
     for g in grids:
         g.sync()
     for g, r, (p, _) in zip(grids, ref, cl):
         gi, ri = g.info(), r.info()
         assert gi["root_level"] == ri["root_level"] and gi["used_leaves"] == ri["used_leaves"]
+        assert np.array_equal(g.read_atlas_map(), r.read_atlas_map())
         for lev in range(ri["root_level"] + 1):
             assert np.array_equal(g.read_nodes(lev), r.read_nodes(lev))
             if lev > 0:

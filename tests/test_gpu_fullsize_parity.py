@@ -230,7 +230,7 @@ def test_batched_smallest_clouds_match_oracle(gvx_mod, orc):
         grids.append(g)
     b = gvx_mod.Batch(0)
     b.set_grids(grids)
-    b.topology(1.0, threads=3)
+    b.topology(1.0, threads=0)
     b.splat(gvx_mod.SPLAT_TRILINEAR, 1.0, chan_density=0, graph=True)
     for g in grids:
         g.update_apron(0, 0.0)

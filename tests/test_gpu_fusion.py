@@ -12,7 +12,11 @@ pytestmark = pytest.mark.gpu
 LOGDIM = (3, 3, 3, 3, 5)
 
 
-def test_fusion_frames_match_oracle(gvx_mod, orc):
+@pytest.mark.parametrize("apron", [False, True])
+def test_fusion_frames_match_oracle(gvx_mod, orc, apron):
+    """apron=True: UpdateApron(c, 0) after every frame on both sides, whole bricks compared.
+    Under AccumulateTopology the bricks keep their slots, so libgvx updates only the aprons of
+    the new bricks and of their neighbours; the oracle updates every apron."""
     import workloads
 
     # a quarter-resolution camera, the scene at half scale in 1024^3 (it spans several level-2
@@ -39,6 +43,10 @@ def test_fusion_frames_match_oracle(gvx_mod, orc):
         o.update_atlas()
         o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, chan_density=0, accum=True)
         o.splat(orc.SPLAT_TRILINEAR, pos, 1.0, weight=conf, chan_density=1, accum=True)
+        if apron:
+            for c in (0, 1):
+                g.update_apron(c, 0.0)
+                o.update_apron(c, 0.0)
         compare_topology(g, o)
         assert g.info()["last_rebuild"] == o.last_mode(), "frame %d" % k
         used = o.used_leaves()
