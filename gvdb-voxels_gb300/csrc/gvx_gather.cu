@@ -215,12 +215,10 @@ __global__ void k_gather_fp16(GatherQArgs a)
 {
     const int lane = threadIdx.x & 31;
     const int sc = a.sc, nv = sc * sc * sc;
-    // subcells one at a time from a counter: their lists differ widely in length
-    for (;;) {
-        uint32_t s = 0;
-        if (lane == 0) s = atomicAdd(a.next, 1u);
-        s = __shfl_sync(0xFFFFFFFFu, s, 0);
-        if (s >= a.nsub) break;
+    // subcells from a counter (WarpUnits): their lists differ widely in length
+    WarpUnits wu(a.next, lane);
+    uint32_t s;
+    while (wu.next(a.next, a.nsub, lane, s)) {
         const uint32_t slot = s / (uint32_t)a.spb;
         const int loc = (int)(s - slot * (uint32_t)a.spb);
         const GvxNode& nd = a.nodes0[a.slot_leaf[slot]];
@@ -293,12 +291,10 @@ __global__ void k_gather(GatherArgs a)
 {
     const int lane = threadIdx.x & 31;
     const int sc = a.sc, nv = sc * sc * sc;
-    // subcells one at a time from a counter: their lists differ widely in length
-    for (;;) {
-        uint32_t s = 0;
-        if (lane == 0) s = atomicAdd(a.next, 1u);
-        s = __shfl_sync(0xFFFFFFFFu, s, 0);
-        if (s >= a.nsub) break;
+    // subcells from a counter (WarpUnits): their lists differ widely in length
+    WarpUnits wu(a.next, lane);
+    uint32_t s;
+    while (wu.next(a.next, a.nsub, lane, s)) {
         const uint32_t slot = s / (uint32_t)a.spb;
         const int loc = (int)(s - slot * (uint32_t)a.spb);
         const GvxNode& nd = a.nodes0[a.slot_leaf[slot]];

@@ -671,7 +671,10 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t units = a.nslots * (uint32_t)a.slabs;
-    // units one at a time from a counter (zeroed before the launch): bricks differ widely in cost
+    // units one at a time from a counter (zeroed before the launch): bricks differ widely in cost,
+    // and the costly ones cluster (dense regions, the surface of an accumulating frame), so claims
+    // of several units, or a next unit claimed ahead, leave warps idle at the end (measured: the
+    // batched clouds' splats 16.7 -> 23.2 ms with claims of 4)
     for (;;) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(a.next, 1u);
@@ -722,8 +725,8 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
             else
                 hi = mid - 1;
         }
-        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid], s_ro[wid],
-                                                phase, lane);
+        splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(args[lo], u - s_us[lo], tile, &s_bar[wid], s_rs[wid],
+                                                       s_ro[wid], phase, lane);
     }
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
 }
@@ -1199,8 +1202,8 @@ static gvx_status batch_tables(gvx_batch* b, int mode, float radius, int chan_d,
         }
         ustart[i] = (uint32_t)tot;
         tot += (uint64_t)args[i].nslots * args[i].slabs;
-        if (tot >= (1ull << 32)) {
-            gvx_set_error("BatchSplat: more than 2^32 work units");
+        if (tot >= (1ull << 31)) {
+            gvx_set_error("BatchSplat: more than 2^31 work units");
             return GVX_ERR_CAPACITY;
         }
     }
