@@ -600,6 +600,31 @@ def run_batched(dev, iters=5):
             b.splat(gvx.SPLAT_TRILINEAR, 1.0, graph=True)
             torch.cuda.synchronize()
             e2e_bat.append((time.perf_counter() - t0) * 1e3)
+        # whole frames through gvx_batch_frame: the first unplanned (staged topology, plans made),
+        # the second planned without a graph, then every grid's planned build and the splat as one
+        # captured CUDA graph, replayed (the grids on their own streams, forked in the graph)
+        for g, s_ in zip(grids, own):
+            g.set_stream(s_.cuda_stream)
+        fb = gvx.Batch(dev.index)
+        fb.set_stream(stream.cuda_stream)
+        fb.set_grids(grids)
+        frame_first = []
+        for k in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fb.frame(1.0, gvx.SPLAT_TRILINEAR, 1.0)
+            torch.cuda.synchronize()
+            frame_first.append(((time.perf_counter() - t0) * 1e3, fb.frame_path()))
+        frame_ms, frame_paths = [], set()
+        for k in range(max(iters, 5)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fb.frame(1.0, gvx.SPLAT_TRILINEAR, 1.0)
+            torch.cuda.synchronize()
+            frame_ms.append((time.perf_counter() - t0) * 1e3)
+            frame_paths.add(fb.frame_path())
+        frame_launches = fb.kernel_launches()
+        fb.close()
         tb.close()
     b.close()
     for g in grids:
@@ -615,11 +640,20 @@ def run_batched(dev, iters=5):
             "topology_ms": topo_ms,
             "end_to_end_sequential_ms": round(min(e2e_seq), 3), "end_to_end_batched_ms": round(min(e2e_bat), 3),
             "end_to_end_speedup": round(min(e2e_seq) / min(e2e_bat), 3),
+            "frame_ms": round(min(frame_ms), 3), "frame_ms_mean": round(sum(frame_ms) / len(frame_ms), 3),
+            "frame_speedup": round(min(e2e_seq) / min(frame_ms), 3),
+            "frame_paths": sorted(frame_paths),
+            "frame_first_ms": [[round(t, 3), list(pth)] for t, pth in frame_first],
+            "frame_batch_stream_launches": int(frame_launches),
             "scope": "speedup: the splat alone, per-cloud gvx_splat loop vs one batched launch replayed from its "
                      "captured graph (aprons fused). end_to_end: topology (full rebuild, UpdateAtlas, InsertPoints) "
                      "+ splat, wall clock: the per-cloud loop on one stream vs gvx_batch_topology staged from one "
                      "host thread (two host waits per grid, the grids' streams overlapping) + the batched graph. "
-                     "topology_ms: gvx_batch_topology alone, per-grid calls from 1 or 16 host threads, or staged"}
+                     "topology_ms: gvx_batch_topology alone, per-grid calls from 1 or 16 host threads, or staged. "
+                     "frame_ms: gvx_batch_frame, wall clock per frame once its graph is captured: every grid's "
+                     "planned full rebuild, UpdateAtlas and InsertPoints (forked onto the grids' streams) and the "
+                     "batched splat replayed as one CUDA graph, one host wait; frame_paths (path, grids rebuilt): "
+                     "2 = graph replay; frame_first_ms: the unplanned, the first planned and the capturing frame"}
 
 
 def run_scatter_frame(dev, frames=3):

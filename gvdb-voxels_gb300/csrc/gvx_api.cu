@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "gvx_grid.cuh"
@@ -27,9 +28,19 @@ gvx_status gvx_cuda_fail(cudaError_t e, const char* what)
     return GVX_ERR_DEVICE;
 }
 
+static std::atomic<uint64_t> g_alloc_epoch{0};
+static thread_local bool t_no_alloc = false;
+
+uint64_t gvx_alloc_epoch() { return g_alloc_epoch.load(); }
+
+GvxNoAllocScope::GvxNoAllocScope() : prev(t_no_alloc) { t_no_alloc = true; }
+GvxNoAllocScope::~GvxNoAllocScope() { t_no_alloc = prev; }
+
 cudaError_t gvx_ensure(DevBuf& b, size_t bytes)
 {
     if (bytes <= b.cap && b.p) return cudaSuccess;
+    if (t_no_alloc) return cudaErrorNotPermitted;
+    g_alloc_epoch++;
     if (b.p) {
         cudaError_t e = cudaFree(b.p);
         if (e != cudaSuccess) return e;
@@ -48,7 +59,10 @@ cudaError_t gvx_ensure(DevBuf& b, size_t bytes)
 
 void gvx_free(DevBuf& b)
 {
-    if (b.p) cudaFree(b.p);
+    if (b.p) {
+        g_alloc_epoch++;
+        cudaFree(b.p);
+    }
     b.p = nullptr;
     b.cap = 0;
 }
@@ -118,11 +132,11 @@ __global__ void k_fill(unsigned char* data, int64_t n, int eb, uint4 pattern)
 }
 
 __global__ void k_pnode(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t n,
-                        uint32_t invalid_key, LeafLookup L, int* pnode)
+                        int kshift, uint32_t invalid_key, LeafLookup L, int* pnode)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = skeys[i];
+    const uint32_t k = skeys[i] >> kshift;
     int leaf = -1;
     if (k < invalid_key) {
         int c[3];
@@ -224,6 +238,7 @@ gvx_status gvx_destroy(gvx_grid* g)
     for (int c = 0; c < GVX_MAXCH; c++) gvx_free(g->ch[c].data);
     gvx_host_tree_free(g);
     gvx_topo_staged_free(g);
+    gvx_topo_plan_free(g);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
     if (g->h_pin) cudaFreeHost(g->h_pin);
@@ -576,7 +591,8 @@ gvx_status gvx_insert_points(gvx_grid* g, int n, const float trans[3], int32_t* 
     GVX_CK(gvx_ensure(tmp, (size_t)n * 4));
     k_pnode<<<(n + 255) / 256, 256, 0, g->stream>>>(g->keys[g->sorted_buf].as<uint32_t>(),
                                                     g->vals[g->sorted_buf].as<uint32_t>(), (uint32_t)n,
-                                                    1u << g->lookup.ks.total_bits, g->lookup, tmp.as<int>());
+                                                    g->key_shift, 1u << g->lookup.ks.total_bits, g->lookup,
+                                                    tmp.as<int>());
     g->launches++;
     cudaError_t e = cudaMemcpyAsync(pnode_out, tmp.p, (size_t)n * 4, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);

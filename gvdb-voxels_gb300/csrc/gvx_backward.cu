@@ -31,6 +31,7 @@ struct BackArgs {
     uint32_t n;               // sorted points
     const uint32_t* skeys;    // compact level-0 keys, sorted
     const uint32_t* svals;    // sorted -> original point index
+    int kshift;               // the sort keys are leaf key << kshift | octant
     uint32_t invalid_key;
     const float4* spos;       // (x, y, z, w), sorted
     const float4* svel;       // (., ., ., R), sorted (per-point radius) or null
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(kBackThreads) k_splat_backward(BackArgs a)
         if (lane == 0) i = atomicAdd(a.next, 1u);
         i = __shfl_sync(0xFFFFFFFFu, i, 0);
         if (i >= a.n) break;
-        const uint32_t key = a.skeys[i];
+        const uint32_t key = a.skeys[i] >> a.kshift;
         const uint32_t orig = a.svals[i];
         // the point takes part iff its own brick is in the lookup (as in the forward)
         int own = -1;
@@ -238,6 +239,7 @@ extern "C" gvx_status gvx_splat_backward_ex(gvx_grid* g, int mode, int n, float 
     a.n = g->n_sorted;
     a.skeys = g->keys[g->sorted_buf].as<uint32_t>();
     a.svals = g->vals[g->sorted_buf].as<uint32_t>();
+    a.kshift = g->key_shift;
     a.invalid_key = 1u << g->lookup.ks.total_bits;
     a.spos = g->spos.as<float4>();
     a.svel = ppr ? g->svel.as<float4>() : nullptr;

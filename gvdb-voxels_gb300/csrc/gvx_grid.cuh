@@ -45,6 +45,8 @@ struct LeafLookup {
     BitRank b;
     uint32_t b_offset;
     const int* remap;  // optional rank -> pool index
+    const uint32_t* b_offset_p;  // optional: b_offset read from device memory (planned builds)
+    uint32_t cap;                // optional (0: none): pool indices >= cap are not returned
 };
 
 __device__ inline int ll_find(const LeafLookup& L, int cx, int cy, int cz)
@@ -53,12 +55,16 @@ __device__ inline int ll_find(const LeafLookup& L, int cx, int cy, int cz)
         cz >= (1 << L.ks.bits[2]))
         return -1;
     const uint32_t key = ks_pack(L.ks, cx, cy, cz, 0);
+    uint32_t r;
     if (br_test(L.a, key)) {
-        const uint32_t r = br_rank(L.a, key);
-        return L.remap ? L.remap[r] : (int)r;
+        r = br_rank(L.a, key);
+        if (L.remap) return L.remap[r];
+    } else if (L.b.bits && br_test(L.b, key)) {
+        r = (L.b_offset_p ? *L.b_offset_p : L.b_offset) + br_rank(L.b, key);
+    } else {
+        return -1;
     }
-    if (L.b.bits && br_test(L.b, key)) return (int)(L.b_offset + br_rank(L.b, key));
-    return -1;
+    return (L.cap && r >= L.cap) ? -1 : (int)r;
 }
 
 struct gvx_grid {
@@ -109,8 +115,10 @@ struct gvx_grid {
     DevBuf leaf_key;     // compact level-0 key per leaf (pool order)
     DevBuf leaf_range;   // int2 [start, end) in the sorted point order
     DevBuf leaf_oct;     // 8 ints per leaf: first sorted index of each octant of the leaf's points
+    int key_shift = 0;       // the sort keys are leaf key << key_shift | octant (key_shift 3) or the leaf key (0)
     bool oct_valid = false;  // the sorted points are in octant order inside every leaf, leaf_oct filled
     uint32_t oct_leaves = 0;
+    DevCount oct_count{};  // leaves to partition, read on the device (a planned build); else oct_leaves
     DevBuf leaf_slot;    // atlas slot per leaf, -1 if inactive
     DevBuf slot_leaf;    // leaf per atlas slot (active slots only)
     DevBuf nbr;          // 27 leaf indices per leaf
@@ -167,6 +175,7 @@ struct gvx_grid {
     DevBuf d_next;  // work-unit counter of the splat launch
     void* h_pin = nullptr;  // pinned staging of the topology's small readbacks
     struct gvx_topo_staged* staged = nullptr;  // a staged RebuildTopology between its stages (batches)
+    struct gvx_topo_plan* plan = nullptr;      // fixed key space and capacities of planned builds (batches)
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index
@@ -226,6 +235,21 @@ gvx_status gvx_topo_stage2(gvx_grid* g);
 gvx_status gvx_topo_stage3(gvx_grid* g);
 void gvx_topo_staged_free(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
+// Planned full builds (batches; see gvx_topology.cu): a plan made from the grid's last staged
+// full build; a planned build queues RebuildTopology (full) + UpdateAtlas with no host wait and
+// no allocation (capturable), with InsertPoints' octant pass writing `attr`; plan_finish, after
+// the stream has passed it, checks that the plan held and sets the host state (*held false: the
+// build is void, the grid is to be built again without the plan)
+gvx_status gvx_topo_plan_make(gvx_grid* g);
+bool gvx_topo_plan_ready(const gvx_grid* g);
+gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr);
+gvx_status gvx_topo_plan_record_error(gvx_grid* g, cudaStream_t st);
+void gvx_topo_plan_replayed(gvx_grid* g);  // its captured build was launched again
+gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held);
+void gvx_topo_plan_free(gvx_grid* g);
+uint64_t gvx_topo_plan_id(const gvx_grid* g);  // changes whenever the plan is made again
+// device count of the atlas slots a planned build assigns (clamped to *cap by the reader)
+const uint32_t* gvx_topo_plan_slots(const gvx_grid* g, uint32_t* cap);
 // InsertPoints: grouping + sorted attribute arrays
 gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool need_svel);
 gvx_status gvx_check_device_error(gvx_grid* g, const char* stage);

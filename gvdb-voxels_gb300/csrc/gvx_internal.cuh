@@ -100,6 +100,25 @@ struct WarpUnits {
     }
 };
 
+// A count a kernel takes either from the host (p null) or from device memory
+// (p[i0] + p[i1], i1 < 0 for none), clamped to `cap` (the capacity of the
+// buffers it sizes): launches enqueued before the count is known on the host
+// (the planned builds of batched grids) stay inside their buffers whatever
+// the count turns out to be.
+struct DevCount {
+    const uint32_t* p;
+    int i0, i1;
+    uint32_t host, cap;
+    __device__ uint32_t get() const
+    {
+        if (!p) return host;
+        const uint32_t v = p[i0] + (i1 >= 0 ? p[i1] : 0u);
+        return v < cap ? v : cap;
+    }
+};
+inline DevCount dc_host(uint32_t n) { return DevCount{nullptr, 0, -1, n, n}; }
+inline DevCount dc_dev(const uint32_t* p, int i0, int i1, uint32_t cap) { return DevCount{p, i0, i1, 0u, cap}; }
+
 struct BitRank {
     uint32_t* bits;
     uint32_t* prefix;
@@ -131,8 +150,25 @@ gvx_status gvx_cuda_fail(cudaError_t e, const char* what);
         if (_e != cudaSuccess) return gvx_cuda_fail(_e, #call);        \
     } while (0)
 
+#define GVX_CK_STATUS(call)             \
+    do {                                \
+        gvx_status _s = (call);         \
+        if (_s != GVX_OK) return _s;    \
+    } while (0)
+
 cudaError_t gvx_ensure(DevBuf& b, size_t bytes);
 void gvx_free(DevBuf& b);
+// Device allocations and frees made by gvx_ensure / gvx_free in this process (a
+// captured CUDA graph holds buffer addresses: it is replayed only while no
+// buffer has moved since its capture).
+uint64_t gvx_alloc_epoch();
+// While alive, gvx_ensure on this thread fails (cudaErrorNotPermitted) instead of
+// allocating: work queued inside a stream capture must find its buffers sized.
+struct GvxNoAllocScope {
+    GvxNoAllocScope();
+    ~GvxNoAllocScope();
+    bool prev;
+};
 
 // ---- onesweep radix sort (gvx_sort.cu) -----------------------------------
 struct SortScratch {

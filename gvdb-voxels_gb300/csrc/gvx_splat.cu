@@ -980,13 +980,11 @@ static int clamp_layers(int P, size_t eb, int want)
     return std::min(std::min(want, P), fit);
 }
 
-// validation, InsertPoints grouping and the kernel arguments of one grid's splat;
-// layers <= 0 picks the default slab height (half the padded brick)
-static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
-                                int chan_v, int accum, int layers, SplatArgs* out, SplatKind* kind)
+// validation of one grid's splat and its kernel kind; *layers in: the wanted slab height (<= 0:
+// half the padded brick), out: clamped to the tile budget
+static gvx_status splat_check(gvx_grid* g, int mode, float radius, int chan_d, int chan_v, int* layers,
+                              SplatKind* kind)
 {
-    gvx_status rc = check_splat_state(g, "Splat");
-    if (rc) return rc;
     if (mode != GVX_SPLAT_TRILINEAR && mode != GVX_SPLAT_CUBIC) {
         gvx_set_error("Splat: unknown mode %d", mode);
         return GVX_ERR_INVALID_ARG;
@@ -1017,16 +1015,26 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
         gvx_set_error("Splat: bricks of 1 voxel are not supported (tiles are moved in 16-byte units)");
         return GVX_ERR_UNSUPPORTED;
     }
-    const bool need_svel = has_v || ppr;
-    rc = gvx_prepare_points(g, n, trans, need_svel);
-    if (rc) return rc;
     const int P = g->P;
-    const size_t eb = has_v ? 16 : 4;
-    layers = clamp_layers(P, eb, layers > 0 ? layers : (P + 1) / 2);
-    if (layers < 1) {
+    *layers = clamp_layers(P, has_v ? 16 : 4, *layers > 0 ? *layers : (P + 1) / 2);
+    if (*layers < 1) {
         gvx_set_error("Splat: a %d^2 layer of the padded brick exceeds the shared tile budget", P);
         return GVX_ERR_UNSUPPORTED;
     }
+    kind->has_d = has_d;
+    kind->has_v = has_v;
+    kind->ppr = ppr;
+    kind->mode = mode;
+    kind->small = mode == GVX_SPLAT_TRILINEAR || (!ppr && radius <= 2.0f);
+    return GVX_OK;
+}
+
+// the kernel arguments of one grid's splat over its current grouping and atlas
+static void splat_fill(gvx_grid* g, const SplatKind& k, float radius, int chan_d, int chan_v, int accum, int layers,
+                       SplatArgs* out)
+{
+    const bool need_svel = k.has_v || k.ppr;
+    const int P = g->P;
     SplatArgs& a = *out;
     memset(&a, 0, sizeof(a));
     a.brick = g->brick;
@@ -1041,25 +1049,34 @@ static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, cons
     a.leaf_oct = g->leaf_oct.as<int>();
     a.spos = g->spos.as<float4>();
     a.svel = need_svel ? g->svel.as<float4>() : nullptr;
-    a.per_point_radius = ppr;
+    a.per_point_radius = k.ppr;
     a.radius = radius;
-    a.den = has_d ? g->ch[chan_d].data.as<float>() : nullptr;
-    a.vel = has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
+    a.den = k.has_d ? g->ch[chan_d].data.as<float>() : nullptr;
+    a.vel = k.has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
     a.slab_layers = layers;
     a.slabs = (P + layers - 1) / layers;
     a.lb = 0;
     while ((1 << a.lb) < g->brick) a.lb++;
     a.max_radius = (float)(g->brick - 1);
-    a.reach = mode == GVX_SPLAT_TRILINEAR ? 1 : (ppr ? g->brick - 1 : (int)ceilf(radius));
-    a.rmax = ppr && g->n_sorted ? g->d_rmax.as<unsigned int>() : nullptr;
+    a.reach = k.mode == GVX_SPLAT_TRILINEAR ? 1 : (k.ppr ? g->brick - 1 : (int)ceilf(radius));
+    a.rmax = k.ppr && g->n_sorted ? g->d_rmax.as<unsigned int>() : nullptr;
     a.accum = accum != 0;
     a.boundval = 0.0f;
     a.err = g->d_err.as<uint32_t>();
-    kind->has_d = has_d;
-    kind->has_v = has_v;
-    kind->ppr = ppr;
-    kind->mode = mode;
-    kind->small = mode == GVX_SPLAT_TRILINEAR || (!ppr && radius <= 2.0f);
+}
+
+// validation, InsertPoints grouping and the kernel arguments of one grid's splat;
+// layers <= 0 picks the default slab height (half the padded brick)
+static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
+                                int chan_v, int accum, int layers, SplatArgs* out, SplatKind* kind)
+{
+    gvx_status rc = check_splat_state(g, "Splat");
+    if (rc) return rc;
+    rc = splat_check(g, mode, radius, chan_d, chan_v, &layers, kind);
+    if (rc) return rc;
+    rc = gvx_prepare_points(g, n, trans, kind->has_v || kind->ppr);
+    if (rc) return rc;
+    splat_fill(g, *kind, radius, chan_d, chan_v, accum, layers, out);
     return GVX_OK;
 }
 
@@ -1144,7 +1161,28 @@ struct gvx_batch {
     cudaEvent_t ev = nullptr;
     BatchTuning tuning;
     int64_t launches = 0;
+    // gvx_batch_frame: the grids' planned builds and the splat, captured in one graph
+    DevBuf f_args, f_ustart, f_cnt, f_caps;
+    cudaEvent_t f_fork = nullptr;
+    std::vector<cudaEvent_t> f_join;     // one per grid
+    cudaGraph_t f_graph = nullptr;
+    cudaGraphExec_t f_exec = nullptr;
+    std::vector<uint64_t> f_key, f_failed_key;
+    bool f_warm = false;                 // a planned frame ran without a graph since the plans were made
+    float f_topo_radius = -1.f;          // the radius the plans were made for
+    int64_t f_launches = 0;              // batch-stream launches of one replay
+    std::vector<int64_t> f_grid_launches;
+    int f_path = 0, f_void = 0;          // how the last frame ran, its grids built again without a plan
 };
+
+static void frame_drop_graph(gvx_batch* b)
+{
+    if (b->f_exec) cudaGraphExecDestroy(b->f_exec);
+    if (b->f_graph) cudaGraphDestroy(b->f_graph);
+    b->f_exec = nullptr;
+    b->f_graph = nullptr;
+    b->f_key.clear();
+}
 
 static void batch_drop_graph(gvx_batch* b)
 {
@@ -1284,6 +1322,214 @@ static gvx_status batch_tune(gvx_batch* b, int mode, float radius, int chan_d, i
     return rc;
 }
 
+// ---------------------------------------------------------------------------
+// A whole frame of a batch (gvx_batch_frame): every grid's full RebuildTopology,
+// UpdateAtlas and InsertPoints, then the batched splat.  Once every grid has a
+// plan (gvx_topo_plan_make, from a staged full build), the builds are planned --
+// no host wait, no allocation -- and, with GVX_BATCH_GRAPH, the grids' builds
+// (forked onto their own streams) and the splat are captured in one CUDA graph,
+// replayed every frame while no buffer has moved.  The splat's unit ranges come
+// from the builds' slot counts on the device (k_batch_ustart).
+
+// unit ranges of a batch whose slot counts are in device memory: ustart[k] = slabs * the sum
+// of the slot counts of grids < k (each clamped to its capacity); the unit counter
+// ustart[ngrids + 1] zeroed
+__global__ void k_batch_ustart(const uint32_t* const* __restrict__ counts, const uint32_t* __restrict__ caps,
+                               int ngrids, int slabs, uint32_t* __restrict__ ustart)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t t = 0;
+    for (int k = 0; k < ngrids; k++) {
+        ustart[k] = t;
+        t += min(*counts[k], caps[k]) * (uint32_t)slabs;
+    }
+    ustart[ngrids] = t;
+    ustart[ngrids + 1] = 0u;
+}
+
+// the sorted attributes InsertPoints writes, then the planned build (whose octant pass writes them)
+static gvx_status frame_build(gvx_grid* g, bool want_svel)
+{
+    const size_t m = (size_t)std::max(g->pts.n, 1);
+    GVX_CK(gvx_ensure(g->spos, m * sizeof(float4)));
+    if (want_svel) GVX_CK(gvx_ensure(g->svel, m * sizeof(float4)));
+    unsigned int* rmax = nullptr;
+    if (g->pts.radius && want_svel) {
+        GVX_CK(gvx_ensure(g->d_rmax, sizeof(unsigned int)));
+        GVX_CK(cudaMemsetAsync(g->d_rmax.p, 0, sizeof(unsigned int), g->stream));
+        rmax = g->d_rmax.as<unsigned int>();
+    }
+    GvxSortedAttr A;
+    A.vel = g->pts.vel;
+    A.vel_off = g->pts.vel_off;
+    A.vel_stride = g->pts.vel_stride;
+    A.weight = g->pts.weight;
+    A.radius = g->pts.radius;
+    A.spos = g->spos.as<float4>();
+    A.svel = want_svel ? g->svel.as<float4>() : nullptr;
+    A.rmax = rmax;
+    return gvx_topo_plan_enqueue(g, &A);
+}
+
+// every grid's planned build on its own stream, forked from and joined back into the batch
+// stream (a grid whose build fails is joined all the same, so that a capture stays whole)
+static gvx_status frame_builds(gvx_batch* b, const std::vector<char>& want_svel)
+{
+    gvx_status first = GVX_OK;
+    GVX_CK(cudaEventRecord(b->f_fork, b->stream));
+    for (size_t i = 0; i < b->grids.size(); i++) {
+        gvx_grid* g = b->grids[i];
+        const bool own = g->stream != b->stream;
+        if (own) GVX_CK(cudaStreamWaitEvent(g->stream, b->f_fork, 0));
+        gvx_status rc = frame_build(g, want_svel[i] != 0);
+        if (rc != GVX_OK && first == GVX_OK) {
+            const std::string m = gvx_last_error();
+            gvx_set_error("BatchFrame: grid %zu: %s", i, m.c_str());
+            first = rc;
+        }
+        if (own) {
+            GVX_CK(cudaEventRecord(b->f_join[i], g->stream));
+            GVX_CK(cudaStreamWaitEvent(b->stream, b->f_join[i], 0));
+        }
+    }
+    return first;
+}
+
+// the splat arguments and the slot-count table of every grid to the device (before a capture,
+// or after the builds of a frame without a graph)
+static gvx_status frame_upload(gvx_batch* b, const SplatKind& kind, float radius, int chan_d, int chan_v,
+                               int layers)
+{
+    const size_t ng = b->grids.size();
+    std::vector<SplatArgs> args(ng);
+    std::vector<const uint32_t*> cnt(ng);
+    std::vector<uint32_t> caps(ng);
+    for (size_t i = 0; i < ng; i++) {
+        splat_fill(b->grids[i], kind, radius, chan_d, chan_v, 0, layers, &args[i]);
+        cnt[i] = gvx_topo_plan_slots(b->grids[i], &caps[i]);
+    }
+    GVX_CK(cudaMemcpyAsync(b->f_args.p, args.data(), ng * sizeof(SplatArgs), cudaMemcpyHostToDevice, b->stream));
+    GVX_CK(cudaMemcpyAsync(b->f_cnt.p, cnt.data(), ng * sizeof(void*), cudaMemcpyHostToDevice, b->stream));
+    GVX_CK(cudaMemcpyAsync(b->f_caps.p, caps.data(), ng * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+    return GVX_OK;
+}
+
+// the unit ranges from the slot counts, then the batched splat
+static gvx_status frame_splat(gvx_batch* b, const SplatKind& kind, const SplatArgs& a0, int blocks)
+{
+    const int ng = (int)b->grids.size();
+    k_batch_ustart<<<1, 32, 0, b->stream>>>(b->f_cnt.as<const uint32_t*>(), b->f_caps.as<uint32_t>(), ng, a0.slabs,
+                                            b->f_ustart.as<uint32_t>());
+    const size_t smem = splat_smem(a0, kind);  // (the shared-memory limit set by batch_max_blocks)
+    void* kern = splat_kernel(kind, true);
+    const SplatArgs* dargs = b->f_args.as<SplatArgs>();
+    uint32_t* dus = b->f_ustart.as<uint32_t>();
+    int n = ng;
+    void* kargs[] = {(void*)&dargs, (void*)&dus, (void*)&n};
+    GVX_CK(cudaLaunchKernel(kern, dim3(blocks), dim3(kSlabWarps * 32), kargs, smem, b->stream));
+    b->launches += 2;
+    // every grid's device error word (topology and splat) into its plan's record
+    for (gvx_grid* g : b->grids) GVX_CK_STATUS(gvx_topo_plan_record_error(g, b->stream));
+    return GVX_OK;
+}
+
+// what a captured frame depends on: buffer addresses (the allocation epoch), the plans, the
+// points and attributes bound, the streams and the splat's parameters
+static std::vector<uint64_t> frame_key(gvx_batch* b, float topo_radius, int mode, float radius, int chan_d,
+                                       int chan_v, int layers, int blocks)
+{
+    auto fb = [](float f) {
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        return (uint64_t)u;
+    };
+    std::vector<uint64_t> k = {gvx_alloc_epoch(), fb(topo_radius), (uint64_t)mode, fb(radius), (uint64_t)chan_d,
+                               (uint64_t)chan_v, (uint64_t)layers, (uint64_t)blocks, (uint64_t)(uintptr_t)b->stream};
+    for (gvx_grid* g : b->grids) {
+        const GvxPoints& p = g->pts;
+        for (uint64_t v : {gvx_topo_plan_id(g), (uint64_t)(uintptr_t)g->stream, (uint64_t)(uintptr_t)p.pos,
+                           (uint64_t)p.pos_off, (uint64_t)p.pos_stride, (uint64_t)p.n, (uint64_t)(uintptr_t)p.vel,
+                           (uint64_t)p.vel_off, (uint64_t)p.vel_stride, (uint64_t)(uintptr_t)p.weight,
+                           (uint64_t)(uintptr_t)p.radius})
+            k.push_back(v);
+    }
+    return k;
+}
+
+// the planned builds and the splat captured in b->f_exec (nothing allocated meanwhile)
+static gvx_status frame_capture(gvx_batch* b, const std::vector<char>& want_svel, const SplatKind& kind,
+                                const SplatArgs& a0, int blocks)
+{
+    const size_t ng = b->grids.size();
+    std::vector<int64_t> l0(ng);
+    for (size_t i = 0; i < ng; i++) l0[i] = b->grids[i]->launches;
+    const int64_t b0 = b->launches;
+    gvx_status rc;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e;
+    {
+        GvxNoAllocScope no_alloc;
+        GVX_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        rc = frame_builds(b, want_svel);
+        if (rc == GVX_OK) rc = frame_splat(b, kind, a0, blocks);
+        e = cudaStreamEndCapture(b->stream, &graph);
+    }
+    (void)cudaGetLastError();
+    b->f_grid_launches.assign(ng, 0);
+    for (size_t i = 0; i < ng; i++) {
+        b->f_grid_launches[i] = b->grids[i]->launches - l0[i];
+        b->grids[i]->launches = l0[i];  // counted when the graph runs
+    }
+    b->f_launches = b->launches - b0;
+    b->launches = b0;
+    if (rc != GVX_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc != GVX_OK ? rc : gvx_cuda_fail(e, "BatchFrame capture");
+    }
+    e = cudaGraphInstantiate(&b->f_exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        b->f_exec = nullptr;
+        return gvx_cuda_fail(e, "BatchFrame graph instantiation");
+    }
+    b->f_graph = graph;
+    return GVX_OK;
+}
+
+// a frame without plans: the staged batch topology and the batched splat, then every grid's
+// plan from its build
+static gvx_status frame_unplanned(gvx_batch* b, float topo_radius, int mode, float radius, int chan_d, int chan_v,
+                                  int flags)
+{
+    frame_drop_graph(b);
+    b->f_warm = false;
+    b->f_topo_radius = -1.f;
+    b->f_path = 0;
+    gvx_status rc = gvx_batch_topology(b, topo_radius, GVX_TOPO_FULL, 0);
+    if (rc) return rc;
+    rc = gvx_batch_splat(b, mode, radius, chan_d, chan_v, 0, flags & GVX_BATCH_TUNE);
+    if (rc) return rc;
+    GVX_CK(cudaStreamSynchronize(b->stream));
+    bool all = true;
+    for (gvx_grid* g : b->grids) all = gvx_topo_plan_make(g) == GVX_OK && all;
+    if (all) b->f_topo_radius = topo_radius;
+    return GVX_OK;
+}
+
+// one grid of a planned frame whose plan did not hold: built and splatted again without one,
+// and planned anew
+static gvx_status frame_rebuild(gvx_grid* g, float topo_radius, int mode, float radius, int chan_d, int chan_v)
+{
+    gvx_status rc = gvx_topo_stage1(g, g->pts.n, topo_radius, GVX_TOPO_FULL, 1);
+    if (rc == GVX_OK) rc = gvx_topo_stage2(g);
+    if (rc == GVX_OK) rc = gvx_topo_stage3(g);
+    if (rc == GVX_OK) rc = gvx_topo_update_atlas(g);
+    if (rc == GVX_OK) rc = gvx_splat_run(g, mode, g->pts.n, radius, nullptr, chan_d, chan_v, 0);
+    if (rc == GVX_OK) GVX_CK(cudaStreamSynchronize(g->stream));
+    if (rc == GVX_OK) (void)gvx_topo_plan_make(g);  // (without a plan the next frame runs unplanned)
+    return rc;
+}
+
 extern "C" {
 
 gvx_status gvx_batch_create(int device, gvx_batch** out)
@@ -1314,8 +1560,12 @@ gvx_status gvx_batch_destroy(gvx_batch* b)
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     batch_drop_graph(b);
+    frame_drop_graph(b);
     gvx_free(b->d_args);
     gvx_free(b->d_ustart);
+    for (DevBuf* d : {&b->f_args, &b->f_ustart, &b->f_cnt, &b->f_caps}) gvx_free(*d);
+    if (b->f_fork) cudaEventDestroy(b->f_fork);
+    for (cudaEvent_t e : b->f_join) cudaEventDestroy(e);
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1334,6 +1584,7 @@ gvx_status gvx_batch_set_stream(gvx_batch* b, void* stream)
     b->stream = (cudaStream_t)stream;
     b->own_stream = false;
     batch_drop_graph(b);
+    frame_drop_graph(b);
     return GVX_OK;
 }
 
@@ -1351,6 +1602,9 @@ gvx_status gvx_batch_set_grids(gvx_batch* b, gvx_grid* const* grids, int count)
     }
     b->grids.assign(grids, grids + count);
     batch_drop_graph(b);
+    frame_drop_graph(b);
+    b->f_warm = false;
+    b->f_topo_radius = -1.f;
     return GVX_OK;
 }
 
@@ -1546,6 +1800,188 @@ gvx_status gvx_batch_kernel_launches(gvx_batch* b, int64_t* out)
         return GVX_ERR_INVALID_ARG;
     }
     *out = b->launches;
+    return GVX_OK;
+}
+
+
+gvx_status gvx_batch_frame(gvx_batch* b, float topo_radius, int mode, float radius, int chan_density, int chan_vel,
+                           int flags)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (!(topo_radius >= 0.f)) {
+        gvx_set_error("BatchFrame: topology radius must be >= 0");
+        return GVX_ERR_INVALID_ARG;
+    }
+    GVX_CK(cudaSetDevice(b->device));
+    const size_t ng = b->grids.size();
+    b->f_void = 0;
+    if (ng == 0) return GVX_OK;
+    bool planned = b->f_topo_radius == topo_radius;
+    for (gvx_grid* g : b->grids) planned = planned && gvx_topo_plan_ready(g);
+    if (!planned) return frame_unplanned(b, topo_radius, mode, radius, chan_density, chan_vel, flags);
+
+    // the splat's kind and slab height, the same for every grid
+    SplatKind kind{};
+    int layers = 0;
+    std::vector<char> want_svel(ng);
+    for (size_t i = 0; i < ng; i++) {
+        gvx_grid* g = b->grids[i];
+        int l = b->tuning.layers;
+        SplatKind k;
+        gvx_status rc = splat_check(g, mode, radius, chan_density, chan_vel, &l, &k);
+        if (rc) return rc;
+        if (i == 0) {
+            kind = k;
+            layers = l;
+        } else if (!(k == kind) || g->P != b->grids[0]->P || l != layers) {
+            gvx_set_error("BatchFrame: grid %zu differs from grid 0 in brick shape, channels or radius kind", i);
+            return GVX_ERR_INVALID_ARG;
+        }
+        want_svel[i] = k.has_v || k.ppr || g->pts.vel || g->pts.radius;
+    }
+    SplatArgs a0;
+    memset(&a0, 0, sizeof(a0));
+    a0.P = b->grids[0]->P;
+    a0.slab_layers = layers;
+    a0.slabs = (a0.P + layers - 1) / layers;
+    uint64_t units = 0;
+    for (gvx_grid* g : b->grids) {
+        uint32_t cap = 0;
+        (void)gvx_topo_plan_slots(g, &cap);
+        units += (uint64_t)cap * a0.slabs;
+    }
+    if (units >= (1ull << 31)) {
+        gvx_set_error("BatchFrame: more than 2^31 work units");
+        return GVX_ERR_CAPACITY;
+    }
+    int per_sm = 1;
+    gvx_status rc = batch_max_blocks(b, kind, a0, &per_sm);
+    if (rc) return rc;
+    int bps = b->tuning.blocks_per_sm;
+    if (bps <= 0 || bps > per_sm) bps = per_sm;
+    const int blocks = sm_count(b->device) * bps;
+
+    // the grids' queued work (point uploads included) before the frame
+    if (!b->f_fork) GVX_CK(cudaEventCreateWithFlags(&b->f_fork, cudaEventDisableTiming));
+    while (b->f_join.size() < ng) {
+        cudaEvent_t e;
+        GVX_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->f_join.push_back(e);
+    }
+    for (size_t i = 0; i < ng; i++) {
+        gvx_grid* g = b->grids[i];
+        rc = gvx_wait_positions(g);
+        if (rc == GVX_OK) rc = gvx_wait_attributes(g);
+        if (rc) return rc;
+        if (g->stream != b->stream) {
+            GVX_CK(cudaEventRecord(b->f_join[i], g->stream));
+            GVX_CK(cudaStreamWaitEvent(b->stream, b->f_join[i], 0));
+        }
+    }
+    GVX_CK(gvx_ensure(b->f_args, ng * sizeof(SplatArgs)));
+    GVX_CK(gvx_ensure(b->f_ustart, (ng + 2) * sizeof(uint32_t)));
+    GVX_CK(gvx_ensure(b->f_cnt, ng * sizeof(void*)));
+    GVX_CK(gvx_ensure(b->f_caps, ng * sizeof(uint32_t)));
+
+    bool use_graph = (flags & GVX_BATCH_GRAPH) && b->f_warm;
+    if (use_graph) {
+        const std::vector<uint64_t> key = frame_key(b, topo_radius, mode, radius, chan_density, chan_vel, layers, blocks);
+        if (!(b->f_exec && key == b->f_key)) {
+            frame_drop_graph(b);
+            use_graph = key != b->f_failed_key;
+            if (use_graph) {
+                rc = frame_upload(b, kind, radius, chan_density, chan_vel, layers);
+                if (rc) return rc;
+                if (frame_capture(b, want_svel, kind, a0, blocks) == GVX_OK) {
+                    b->f_key = key;
+                } else {
+                    b->f_failed_key = key;  // the frame runs without a graph; no new attempt with this key
+                    use_graph = false;
+                }
+            }
+        }
+    }
+    if (use_graph) {
+        GVX_CK(cudaGraphLaunch(b->f_exec, b->stream));
+        b->launches += b->f_launches;
+        for (size_t i = 0; i < ng; i++) {
+            b->grids[i]->launches += b->f_grid_launches[i];
+            gvx_topo_plan_replayed(b->grids[i]);
+        }
+        b->f_path = 2;
+    } else {
+        rc = frame_builds(b, want_svel);
+        if (rc == GVX_OK) rc = frame_upload(b, kind, radius, chan_density, chan_vel, layers);
+        if (rc == GVX_OK) rc = frame_splat(b, kind, a0, blocks);
+        if (rc) {
+            cudaStreamSynchronize(b->stream);
+            return rc;
+        }
+        b->f_path = 1;
+    }
+    GVX_CK(cudaStreamSynchronize(b->stream));
+
+    // which plans held: the grids whose did not are built again without one
+    gvx_status first = GVX_OK;
+    std::vector<size_t> redo;
+    for (size_t i = 0; i < ng; i++) {
+        gvx_grid* g = b->grids[i];
+        bool held = false;
+        rc = gvx_topo_plan_finish(g, &held);
+        if (rc != GVX_OK) {
+            if (first == GVX_OK) {
+                const std::string m = gvx_last_error();
+                gvx_set_error("BatchFrame: grid %zu: %s", i, m.c_str());
+                first = rc;
+            }
+            continue;
+        }
+        if (!held) {
+            redo.push_back(i);
+            continue;
+        }
+        g->perm_valid = true;  // as gvx_prepare_points leaves it
+        g->perm_has_svel = want_svel[i] != 0;
+        g->perm_vel = g->pts.vel;
+        g->perm_w = g->pts.weight;
+        g->perm_r = g->pts.radius;
+        splat_finish(g, chan_density, chan_vel, 0);
+    }
+    if (first != GVX_OK) {
+        frame_drop_graph(b);
+        b->f_warm = false;
+        b->f_topo_radius = -1.f;
+        return first;
+    }
+    if (b->f_path == 1) b->f_warm = true;
+    if (!redo.empty()) {
+        frame_drop_graph(b);
+        b->f_warm = false;
+        b->f_void = (int)redo.size();
+        for (size_t i : redo) {
+            rc = frame_rebuild(b->grids[i], topo_radius, mode, radius, chan_density, chan_vel);
+            if (rc) {
+                const std::string m = gvx_last_error();
+                gvx_set_error("BatchFrame: grid %zu: %s", i, m.c_str());
+                b->f_topo_radius = -1.f;
+                return rc;
+            }
+        }
+    }
+    return GVX_OK;
+}
+
+gvx_status gvx_batch_frame_path(gvx_batch* b, int* path, int* rebuilt)
+{
+    if (!b) {
+        gvx_set_error("null batch handle");
+        return GVX_ERR_INVALID_ARG;
+    }
+    if (path) *path = b->f_path;
+    if (rebuilt) *rebuilt = b->f_void;
     return GVX_OK;
 }
 

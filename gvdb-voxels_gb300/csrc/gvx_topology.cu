@@ -24,6 +24,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "gvx_grid.cuh"
 
 namespace {
@@ -149,10 +151,14 @@ __global__ void k_bbox(const char* pos, int off, int stride, uint32_t n, float o
 }
 
 // compact level-0 key of every point (invalid points -> invalid_key, sorted
-// last), identity values, and the digit histograms of the sort
+// last), identity values, and the digit histograms of the sort.  kshift 3: the
+// key is (leaf key << 3) | octant, octant = 4 hx + 2 hy + hz the half of the
+// brick (2^lb voxels) that the point's voxel lies in on every axis, so the
+// stable sort leaves every leaf's points in (octant, index) order; invalid_key
+// is the shifted one then
 __global__ void k_keys(const char* pos, int off, int stride, uint32_t n, float ox, float oy, float oz,
-                       KeySpace ks, float inv_b, int passes, uint32_t invalid_key, uint32_t* keys,
-                       uint32_t* vals, uint32_t* hist, uint32_t* err)
+                       KeySpace ks, float inv_b, int kshift, int lb, int passes, uint32_t invalid_key,
+                       uint32_t* keys, uint32_t* vals, uint32_t* hist, uint32_t* err)
 {
     __shared__ uint32_t sh[4 * 256];
     for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) sh[i] = 0u;
@@ -173,10 +179,19 @@ __global__ void k_keys(const char* pos, int off, int stride, uint32_t n, float o
                 c[a] = (int)(w[a] * inv_b) - ks.lo[a];  // floor(w / b), exact for a power-of-two b
                 if (c[a] < 0 || c[a] >= (1 << ks.bits[a])) in = false;
             }
-            if (in)
-                key = ks_pack(ks, c[0], c[1], c[2], 0);
-            else
+            if (in) {
+                key = ks_pack(ks, c[0], c[1], c[2], 0) << kshift;
+                if (kshift) {
+                    // voxel x >= the brick's corner + half  <=>  bit lb-1 of x (x >= 0, bricks aligned)
+                    int oct = 7;
+                    if (lb > 0)
+                        oct = ((((int)w[0]) >> (lb - 1)) & 1) << 2 | ((((int)w[1]) >> (lb - 1)) & 1) << 1 |
+                              ((((int)w[2]) >> (lb - 1)) & 1);
+                    key |= (uint32_t)oct;
+                }
+            } else {
                 degen = true;
+            }
         }
         keys[i] = key;
         vals[i] = i;
@@ -188,14 +203,15 @@ __global__ void k_keys(const char* pos, int off, int stride, uint32_t n, float o
     if (degen) atomicOr(err, GVX_DERR_DEGENERATE);
 }
 
-// first point of every run of equal valid keys sets the key's bit
-__global__ void k_mark_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t invalid_key, uint32_t* bits)
+// first point of every run of equal valid leaf keys (sorted keys >> kshift) sets the key's bit
+__global__ void k_mark_runs(const uint32_t* __restrict__ skeys, uint32_t n, int kshift, uint32_t invalid_key,
+                            uint32_t* bits)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = skeys[i];
+    const uint32_t k = skeys[i] >> kshift;
     if (k >= invalid_key) return;
-    if (i == 0 || skeys[i - 1] != k) atomicOr(&bits[k >> 5], 1u << (k & 31));
+    if (i == 0 || (skeys[i - 1] >> kshift) != k) atomicOr(&bits[k >> 5], 1u << (k & 31));
 }
 
 // dilation mask of every direct leaf: OR over its points of the leaves touched
@@ -203,12 +219,12 @@ __global__ void k_mark_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint
 // as 27 bits (dz+1)*9 + (dy+1)*3 + (dx+1)
 // (hi_mul = 2 for the full rebuild's box, 1 for the incremental box [int(p)-r, int(p)+r], PT.cuh:433-434)
 __global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ svals, uint32_t n,
-                              uint32_t invalid_key, BitRank d0, const char* pos, int off, int stride, float ox,
-                              float oy, float oz, float radius, float hi_mul, int brick, uint32_t* masks)
+                              int kshift, uint32_t invalid_key, BitRank d0, const char* pos, int off, int stride,
+                              float ox, float oy, float oz, float radius, float hi_mul, int brick, uint32_t* masks)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n;
-    uint32_t key = live ? skeys[i] : invalid_key;
+    uint32_t key = live ? skeys[i] >> kshift : invalid_key;
     const bool valid = key < invalid_key;
     uint32_t m = 0u;
     int leaf = -1;
@@ -241,9 +257,10 @@ __global__ void k_point_masks(const uint32_t* __restrict__ skeys, const uint32_t
     if (valid && lane == __ffs(peers) - 1) atomicOr(&masks[leaf], agg);
 }
 
-// leaves of the dilation boxes that hold no point -> X0 bitmap
+// leaves of the dilation boxes that hold no point -> X0 bitmap; lim: per axis, the first key-space
+// coordinate past the root (a key space rounded up to powers of two may reach past it)
 __global__ void k_dilate(const uint32_t* __restrict__ dlist, const uint32_t* __restrict__ count, KeySpace ks,
-                         const uint32_t* __restrict__ masks, BitRank d0, uint32_t* x0bits, uint32_t* err)
+                         int3 lim, const uint32_t* __restrict__ masks, BitRank d0, uint32_t* x0bits, uint32_t* err)
 {
     // grid-stride over the leaves (their count is on the device; the grid is sized for the points)
     const uint32_t cnt = *count, stride = gridDim.x * blockDim.x;
@@ -256,8 +273,7 @@ __global__ void k_dilate(const uint32_t* __restrict__ dlist, const uint32_t* __r
         for (int b = 0; b < 27; b++) {
             if (!((m >> b) & 1u)) continue;
             const int nx = c[0] + (b % 3) - 1, ny = c[1] + (b / 3) % 3 - 1, nz = c[2] + b / 9 - 1;
-            if (nx < 0 || ny < 0 || nz < 0 || nx >= (1 << ks.bits[0]) || ny >= (1 << ks.bits[1]) ||
-                nz >= (1 << ks.bits[2])) {
+            if (nx < 0 || ny < 0 || nz < 0 || nx >= lim.x || ny >= lim.y || nz >= lim.z) {
                 degen = true;  // the reference descends outside the root here
                 continue;
             }
@@ -476,13 +492,13 @@ gvx_status gvx_scan_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t*
 
 // set bits -> sorted key list (select)
 __global__ void k_select(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ prefix, uint32_t words,
-                         uint32_t* out)
+                         uint32_t* out, uint32_t cap)
 {
     const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= words) return;
     uint32_t b = bits[w];
     uint32_t o = prefix[w];
-    while (b) {
+    while (b && o < cap) {  // cap: the list's capacity
         const int k = __ffs(b) - 1;
         b &= b - 1u;
         out[o++] = w * 32u + (uint32_t)k;
@@ -504,6 +520,11 @@ struct NodeLevelArgs {
     GvxNode* nodes;
     uint64_t* pclist;
     uint32_t* leaf_key;  // level 0 only
+    // planned builds: the counts from device memory (dc[ci_u], dc[ci_x], dc[ci_pu]; ci_pu < 0: none),
+    // this level's node capacity and the parent level's (0: no parent check)
+    const uint32_t* dc;
+    int ci_u, ci_x, ci_pu;
+    uint32_t cap, pcap;
 };
 
 // one node per thread: Node record, parent reference, and the parent's child-list slot
@@ -511,8 +532,14 @@ struct NodeLevelArgs {
 __global__ void k_write_nodes(NodeLevelArgs a)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.ucount + a.xcount) return;
-    const uint32_t key = i < a.ucount ? a.dlist[i] : a.xlist[i - a.ucount];
+    uint32_t ucount = a.ucount, xcount = a.xcount, pucount = a.pucount;
+    if (a.dc) {
+        ucount = min(a.dc[a.ci_u], a.cap);
+        xcount = min(a.dc[a.ci_x], a.cap - ucount);
+        pucount = a.ci_pu >= 0 ? a.dc[a.ci_pu] : 0u;
+    }
+    if (i >= ucount + xcount) return;
+    const uint32_t key = i < ucount ? a.dlist[i] : a.xlist[i - ucount];
     int c[3];
     ks_unpack(a.ks, key, a.tshift, c);
     GvxNode nd;
@@ -530,18 +557,26 @@ __global__ void k_write_nodes(NodeLevelArgs a)
     uint32_t pidx;
     int rel[3];
     const int res = a.res_parent;
+    bool linked = true;
     if (a.lev + 1 == a.depth) {
         pidx = 0u;
-        for (int k = 0; k < 3; k++) rel[k] = a.lo[k] + c[k] - a.root_rel[k];
+        for (int k = 0; k < 3; k++) {
+            rel[k] = a.lo[k] + c[k] - a.root_rel[k];
+            // (a key space rounded up to powers of two may reach past the root: a planned build's
+            // points there make it void -- the frame's root differs -- and are not linked)
+            linked = linked && rel[k] >= 0 && rel[k] < res;
+        }
     } else {
         const int sh = a.logdim_parent;
         const uint32_t pk = ks_pack(a.ks, c[0] >> sh, c[1] >> sh, c[2] >> sh, a.tshift_parent);
-        pidx = br_test(a.pd, pk) ? br_rank(a.pd, pk) : a.pucount + br_rank(a.px, pk);
+        pidx = br_test(a.pd, pk) ? br_rank(a.pd, pk) : pucount + br_rank(a.px, pk);
         for (int k = 0; k < 3; k++) rel[k] = c[k] & (res - 1);
     }
     nd.parent = ((uint64_t)pidx << 16) | ((uint64_t)(a.lev + 1) << 8);
     const int bit = (rel[2] * res + rel[1]) * res + rel[0];
-    a.pclist[(size_t)pidx * res * res * res + bit] = ((uint64_t)i << 16) | ((uint64_t)a.lev << 8);
+    // (a parent beyond its pool's capacity: no link -- the planned build is void)
+    if (linked && (!a.pcap || pidx < a.pcap))
+        a.pclist[(size_t)pidx * res * res * res + bit] = ((uint64_t)i << 16) | ((uint64_t)a.lev << 8);
     a.nodes[i] = nd;
     if (a.leaf_key) a.leaf_key[i] = key;
 }
@@ -566,23 +601,35 @@ __global__ void k_write_root(GvxNode* root, int lev, int px, int py, int pz)
     *root = nd;
 }
 
-// run of equal keys in sorted order -> [start, end) of its leaf
-__global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t invalid_key, LeafLookup L,
-                             int2* leaf_range)
+// run of equal leaf keys in sorted order -> [start, end) of its leaf.  With octants in the keys
+// (kshift 3) also the first sorted index of every octant of the leaf's points (leaf_oct[8 l + o] =
+// start + the points of octants < o), written at the starts of the octant runs and at the leaf's end
+__global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, int kshift, uint32_t invalid_key,
+                             LeafLookup L, int2* leaf_range, int* leaf_oct)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = skeys[i];
+    const uint32_t sk = skeys[i], k = sk >> kshift;
     if (k >= invalid_key) return;
-    const bool first = i == 0 || skeys[i - 1] != k;
-    const bool last = i + 1 == n || skeys[i + 1] != k;
-    if (!first && !last) return;
+    const uint32_t prev = i == 0 ? 0xFFFFFFFFu : skeys[i - 1];
+    const bool first = i == 0 || (prev >> kshift) != k;
+    const bool last = i + 1 == n || (skeys[i + 1] >> kshift) != k;
+    const bool ostart = kshift && (first || prev != sk);
+    if (!first && !last && !ostart) return;
     int c[3];
     ks_unpack(L.ks, k, 0, c);
     const int leaf = ll_find(L, c[0], c[1], c[2]);
     if (leaf < 0) return;
     if (first) leaf_range[leaf].x = (int)i;
     if (last) leaf_range[leaf].y = (int)(i + 1);
+    if (kshift) {
+        int* lo = leaf_oct + (size_t)leaf * 8;
+        const int o = (int)(sk & 7u);
+        if (ostart)
+            for (int q = first ? 0 : (int)(prev & 7u) + 1; q <= o; q++) lo[q] = (int)i;
+        if (last)
+            for (int q = o + 1; q < 8; q++) lo[q] = (int)(i + 1);
+    }
 }
 
 // Points of every leaf in octant order: a stable partition of the leaf's range
@@ -590,75 +637,91 @@ __global__ void k_group_runs(const uint32_t* __restrict__ skeys, uint32_t n, uin
 // (floor of the translated position, as the keys take it) lies in on every
 // axis, octant = 4 hx + 2 hy + hz, and the first index of every octant.  The
 // sorted order becomes (leaf key, octant, point index); the splat reads only
-// the octants of a neighbouring brick whose points can reach its slab.  One
-// warp per leaf; lanes 0-7 keep the octants' counters.  With A.spos the sorted
+// the octants of a neighbouring brick whose points can reach its slab.  For
+// key spaces too wide for the octant in the sort key (more than 2^28 leaf
+// cells; otherwise the sort itself orders the octants).  A segment of G lanes
+// per leaf, launched with G = 32 (segments of 8 lanes were slower on leaves
+// of very different sizes: the longest leaf of a warp sets its trip count);
+// the segment's lanes 0-7 keep the octants' counters.  With A.spos the sorted
 // point attributes of the leaves' points are written in the same pass (as
 // k_permute writes them); entries outside the leaf ranges are not, and no
 // reader takes them (a point is splatted only when its own leaf exists).
-__global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t nleaves,
+template <int G>
+__global__ void k_octant_partition(const int2* __restrict__ leaf_range, DevCount nlc,
                                    const GvxNode* __restrict__ nodes0, const char* pos, int off, int stride, float ox,
                                    float oy, float oz, int half, const uint32_t* __restrict__ vin,
                                    uint32_t* __restrict__ vout, int* __restrict__ leaf_oct, GvxSortedAttr A)
 {
-    const uint32_t leaf = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    static_assert(G == 8 || G == 16 || G == 32, "segments of 8, 16 or 32 lanes");
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    if (leaf >= nleaves) return;  // whole warps
-    const int2 r = leaf_range[leaf];
-    const int bx = nodes0[leaf].pos[0] + half, by = nodes0[leaf].pos[1] + half, bz = nodes0[leaf].pos[2] + half;
-    auto octant = [&](uint32_t v) {
-        float w[3];
+    const int sl = lane & (G - 1), sb = lane - sl;  // lane in the segment, the segment's first lane
+    const uint32_t smask = G == 32 ? 0xFFFFFFFFu : (((1u << G) - 1u) << sb);
+    const uint32_t nl = nlc.get();
+    if ((gt & ~31u) / G >= nl) return;  // whole warps: the warp's first leaf is past the last
+    const uint32_t leaf = gt / G;
+    const bool live = leaf < nl;
+    int2 r = make_int2(0, 0);
+    int bx = 0, by = 0, bz = 0;
+    if (live) {
+        r = leaf_range[leaf];
+        bx = nodes0[leaf].pos[0] + half;
+        by = nodes0[leaf].pos[1] + half;
+        bz = nodes0[leaf].pos[2] + half;
+    }
+    // translated position and octant of sorted entry i (octant -1 past the leaf's range)
+    auto fetch = [&](int i, uint32_t& v, float* w) {
+        if (i >= r.y) return -1;
+        v = vin[i];
         load_pos(pos, off, stride, v, w);
-        const int x = (int)floorf(w[0] + ox), y = (int)floorf(w[1] + oy), z = (int)floorf(w[2] + oz);
+        w[0] += ox;
+        w[1] += oy;
+        w[2] += oz;
+        const int x = (int)floorf(w[0]), y = (int)floorf(w[1]), z = (int)floorf(w[2]);
         return (x >= bx ? 4 : 0) | (y >= by ? 2 : 0) | (z >= bz ? 1 : 0);
     };
-    int cnt = 0;  // lane o < 8: points of octant o
-    uint32_t v0 = 0u;  // the first 32 points and their octants, kept for the placement pass
+    const int nch = __reduce_max_sync(0xFFFFFFFFu, (r.y - r.x + G - 1) / G);  // chunks of the warp's longest leaf
+    int cnt = 0;  // segment lane o < 8: points of octant o
+    uint32_t v0 = 0u;  // the segment's first G points, kept for the placement pass
+    float w0[3] = {0.f, 0.f, 0.f};
     int o0 = -1;
-    for (int b = r.x; b < r.y; b += 32) {
-        const int i = b + lane;
+    for (int c = 0; c < nch; c++) {
         uint32_t v = 0u;
-        int o = -1;
-        if (i < r.y) {
-            v = vin[i];
-            o = octant(v);
-        }
-        if (b == r.x) {
+        float w[3];
+        const int o = fetch(r.x + c * G + sl, v, w);
+        if (c == 0) {
             v0 = v;
             o0 = o;
+            w0[0] = w[0];
+            w0[1] = w[1];
+            w0[2] = w[2];
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k);
-            if (lane == k) cnt += __popc(m);
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k) & smask;
+            if (sl == k) cnt += __popc(m);
         }
     }
     int incl = cnt;
 #pragma unroll
     for (int s = 1; s < 8; s <<= 1) {
-        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, s);
-        if (lane >= s) incl += t;
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, s, G);
+        if (sl >= s) incl += t;
     }
-    int run = r.x + incl - cnt;  // lane o < 8: next index of octant o
-    if (lane < 8) leaf_oct[(size_t)leaf * 8 + lane] = run;
-    for (int b = r.x; b < r.y; b += 32) {
-        const int i = b + lane;
+    int run = r.x + incl - cnt;  // segment lane o < 8: next index of octant o
+    if (live && sl < 8) leaf_oct[(size_t)leaf * 8 + sl] = run;
+    for (int c = 0; c < nch; c++) {
         uint32_t v = v0;
+        float w[3] = {w0[0], w0[1], w0[2]};
         int o = o0;
-        if (b != r.x && i < r.y) {
-            v = vin[i];
-            o = octant(v);
-        } else if (b != r.x) {
-            o = -1;
-        }
-        const uint32_t same = __match_any_sync(0xFFFFFFFFu, o);
-        const int dst = __shfl_sync(0xFFFFFFFFu, run, o < 0 ? 0 : o) + __popc(same & ((1u << lane) - 1u));
+        if (c > 0) o = fetch(r.x + c * G + sl, v, w);
+        const uint32_t same = __match_any_sync(0xFFFFFFFFu, o < 0 ? 0xFFFFFFFFu : (uint32_t)(o | (sb << 3)));
+        const int dst = __shfl_sync(0xFFFFFFFFu, run, sb + (o < 0 ? 0 : o)) + __popc(same & ((1u << lane) - 1u));
         if (o >= 0) vout[dst] = v;
         if (A.spos) {
             float rr = 0.0f;
             if (o >= 0) {
-                float w[3];
-                load_pos(pos, off, stride, v, w);
-                A.spos[dst] = make_float4(w[0] + ox, w[1] + oy, w[2] + oz, A.weight ? A.weight[v] : 1.0f);
+                A.spos[dst] = make_float4(w[0], w[1], w[2], A.weight ? A.weight[v] : 1.0f);
                 if (A.radius) rr = A.radius[v];
                 if (A.svel) {
                     float4 q = make_float4(0.f, 0.f, 0.f, rr);
@@ -680,8 +743,8 @@ __global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k);
-            if (lane == k) run += __popc(m);
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, o == k) & smask;
+            if (sl == k) run += __popc(m);
         }
     }
 }
@@ -689,9 +752,10 @@ __global__ void k_octant_partition(const int2* __restrict__ leaf_range, uint32_t
 // 27-neighbourhood of every leaf (leaf pool indices, -1 where no leaf; all -1
 // for an inactive leaf, whose key is kNoKey)
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;
-__global__ void k_neighbors(const uint32_t* __restrict__ leaf_key, uint32_t nleaves, LeafLookup L, int* nbr)
+__global__ void k_neighbors(const uint32_t* __restrict__ leaf_key, DevCount nl, LeafLookup L, int* nbr)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nleaves = nl.get();
     if (t >= nleaves * 27u) return;
     const uint32_t leaf = t / 27u, d = t % 27u;
     const uint32_t key = leaf_key[leaf];
@@ -705,9 +769,10 @@ __global__ void k_neighbors(const uint32_t* __restrict__ leaf_key, uint32_t nlea
 }
 
 // active leaves (mFlags) -> bitmap over pool indices
-__global__ void k_flag_bits(const GvxNode* __restrict__ nodes, uint32_t n, uint32_t* bits)
+__global__ void k_flag_bits(const GvxNode* __restrict__ nodes, DevCount nc, uint32_t* bits)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = nc.get();
     const bool f = i < n && nodes[i].flags;
     const uint32_t b = __ballot_sync(0xFFFFFFFFu, f);
     if ((threadIdx.x & 31) == 0 && i < ((n + 31u) & ~31u)) bits[i >> 5] = b;
@@ -715,12 +780,12 @@ __global__ void k_flag_bits(const GvxNode* __restrict__ nodes, uint32_t n, uint3
 
 // UpdateAtlas: active leaf k (pool order) -> atlas slot k, mValue, atlas map
 // (VG.cpp:2650-2690, AL.cpp:692-715)
-__global__ void k_atlas_assign(GvxNode* nodes, uint32_t n, const uint32_t* __restrict__ fbits,
+__global__ void k_atlas_assign(GvxNode* nodes, DevCount nc, const uint32_t* __restrict__ fbits,
                                const uint32_t* __restrict__ fprefix, int sx, int sy, int P, int apron,
                                int* leaf_slot, int* slot_leaf, int4* amap)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= nc.get()) return;
     if (!((fbits[i >> 5] >> (i & 31)) & 1u)) {
         leaf_slot[i] = -1;
         return;
@@ -736,6 +801,12 @@ __global__ void k_atlas_assign(GvxNode* nodes, uint32_t n, const uint32_t* __res
     leaf_slot[i] = (int)s;
     slot_leaf[s] = (int)i;
     amap[s] = make_int4(nd->pos[0], nd->pos[1], nd->pos[2], (int)i);
+}
+
+// GetBoundingBox's accumulators before k_bbox: min = all ones, max = 0 (order-preserving bits)
+__global__ void k_bbox_reset(uint32_t* out)
+{
+    if (threadIdx.x < 6) out[threadIdx.x] = threadIdx.x < 3 ? 0xFFFFFFFFu : 0u;
 }
 
 __global__ void k_bounds_init(int* out)
@@ -1099,16 +1170,20 @@ static gvx_status sort_points(gvx_grid* g, int n, const float t[3], const KeySpa
     GVX_CK(gvx_ensure(g->keys[1], (size_t)n * 4));
     GVX_CK(gvx_ensure(g->vals[0], (size_t)n * 4));
     GVX_CK(gvx_ensure(g->vals[1], (size_t)n * 4));
-    const uint32_t invalid_key = 1u << ks.total_bits;
-    const int bits = ks.total_bits + 1;
+    // the octant below the leaf key when the key space leaves room for it (28 bits of leaves)
+    const int kshift = ks.total_bits <= 28 ? 3 : 0;
+    int lb = 0;
+    while ((1 << lb) < g->brick) lb++;
+    const uint32_t invalid_key = 1u << (ks.total_bits + kshift);
+    const int bits = ks.total_bits + kshift + 1;
     const int passes = gvx_sort_passes(bits);
     gvx_status rc = gvx_sort_prepare_hist(g->sort, bits, g->stream);
     if (rc) return rc;
     const unsigned kb = std::min(blocks_for(n, 256), 152u * 8u);
     k_keys<<<kb, 256, 0, g->stream>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, t[0], t[1], t[2],
-                                      ks, 1.0f / (float)g->brick, passes, invalid_key, g->keys[0].as<uint32_t>(),
-                                      g->vals[0].as<uint32_t>(), gvx_sort_hist_ptr(g->sort),
-                                      g->d_err.as<uint32_t>());
+                                      ks, 1.0f / (float)g->brick, kshift, lb, passes, invalid_key,
+                                      g->keys[0].as<uint32_t>(), g->vals[0].as<uint32_t>(),
+                                      gvx_sort_hist_ptr(g->sort), g->d_err.as<uint32_t>());
     g->launches++;
     uint32_t* kk[2] = {g->keys[0].as<uint32_t>(), g->keys[1].as<uint32_t>()};
     uint32_t* vv[2] = {g->vals[0].as<uint32_t>(), g->vals[1].as<uint32_t>()};
@@ -1117,6 +1192,7 @@ static gvx_status sort_points(gvx_grid* g, int n, const float t[3], const KeySpa
                         &g->launches);
     if (rc) return rc;
     g->sorted_buf = res;
+    g->key_shift = kshift;
     g->n_sorted = (uint32_t)n;
     for (int a = 0; a < 3; a++) g->sort_trans[a] = t[a];
     g->perm_valid = false;
@@ -1132,8 +1208,8 @@ static gvx_status fill_leaf_ranges(gvx_grid* g, uint32_t nleaves)
     GVX_CK(cudaMemsetAsync(g->leaf_oct.p, 0, (size_t)(nleaves + 1) * 8 * sizeof(int), g->stream));
     if (g->n_sorted) {
         k_group_runs<<<blocks_for(g->n_sorted, 256), 256, 0, g->stream>>>(
-            g->keys[g->sorted_buf].as<uint32_t>(), g->n_sorted, 1u << g->lookup.ks.total_bits, g->lookup,
-            g->leaf_range.as<int2>());
+            g->keys[g->sorted_buf].as<uint32_t>(), g->n_sorted, g->key_shift, 1u << g->lookup.ks.total_bits,
+            g->lookup, g->leaf_range.as<int2>(), g->leaf_oct.as<int>());
         g->launches++;
     }
     g->oct_leaves = nleaves;
@@ -1142,24 +1218,67 @@ static gvx_status fill_leaf_ranges(gvx_grid* g, uint32_t nleaves)
     return GVX_OK;
 }
 
-// Octant order inside every leaf (k_octant_partition), once per grouping, for
-// the splats: partition into the other value buffer (a copy of the sorted
-// values, so entries outside the leaf ranges keep theirs), then copy back.
+// the sorted point attributes (as k_permute writes them), one thread per sorted entry
+__global__ void k_attr_permute(const uint32_t* __restrict__ svals, uint32_t n, const char* pos, int off, int stride,
+                               float ox, float oy, float oz, GvxSortedAttr A)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    const uint32_t v = live ? svals[i] : 0u;
+    float rr = 0.0f;
+    if (live) {
+        float w[3];
+        load_pos(pos, off, stride, v, w);
+        A.spos[i] = make_float4(w[0] + ox, w[1] + oy, w[2] + oz, A.weight ? A.weight[v] : 1.0f);
+        if (A.radius) rr = A.radius[v];
+        if (A.svel) {
+            float4 q = make_float4(0.f, 0.f, 0.f, rr);
+            if (A.vel) {
+                const float* u = (const float*)(A.vel + (size_t)v * A.vel_stride + A.vel_off);
+                q.x = u[0];
+                q.y = u[1];
+                q.z = u[2];
+            }
+            A.svel[i] = q;
+        }
+        rr = rr != rr ? 3.0e38f : fmaxf(rr, 0.0f);
+    }
+    if (A.rmax) {
+        const unsigned int mm = __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(rr));
+        if ((threadIdx.x & 31) == 0 && mm && mm > *(volatile unsigned int*)A.rmax) atomicMax(A.rmax, mm);
+    }
+}
+
+// Octant order inside every leaf, once per grouping, for the splats.  With the
+// octants in the sort keys the sorted order is already (leaf key, octant,
+// index) and fill_leaf_ranges has the octant starts: only the sorted attributes
+// are written, one thread per entry.  Otherwise k_octant_partition partitions
+// into the other value buffer (a copy of the sorted values, so entries outside
+// the leaf ranges keep theirs), then copies back.
 gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr)
 {
     if (g->oct_valid) return GVX_OK;
     GvxSortedAttr none;
     memset(&none, 0, sizeof(none));
     const uint32_t nleaves = g->oct_leaves;
-    if (g->n_sorted && nleaves) {
+    if (g->key_shift) {
+        if (g->n_sorted && attr && attr->spos) {
+            k_attr_permute<<<blocks_for(g->n_sorted, 256), 256, 0, g->stream>>>(
+                g->vals[g->sorted_buf].as<uint32_t>(), g->n_sorted, g->pts.pos, g->pts.pos_off, g->pts.pos_stride,
+                g->sort_trans[0], g->sort_trans[1], g->sort_trans[2], *attr);
+            g->launches++;
+            GVX_CK(cudaGetLastError());
+        }
+    } else if (g->n_sorted && nleaves) {
         uint32_t* vin = g->vals[g->sorted_buf].as<uint32_t>();
         uint32_t* vtmp = g->vals[1 - g->sorted_buf].as<uint32_t>();
         const size_t vb = (size_t)g->n_sorted * sizeof(uint32_t);
         GVX_CK(cudaMemcpyAsync(vtmp, vin, vb, cudaMemcpyDeviceToDevice, g->stream));
-        k_octant_partition<<<blocks_for((uint64_t)nleaves * 32u, 256), 256, 0, g->stream>>>(
-            g->leaf_range.as<int2>(), nleaves, g->nodes[0].as<GvxNode>(), g->pts.pos, g->pts.pos_off,
-            g->pts.pos_stride, g->sort_trans[0], g->sort_trans[1], g->sort_trans[2], g->brick / 2, vin, vtmp,
-            g->leaf_oct.as<int>(), attr ? *attr : none);
+        const DevCount nlc = g->oct_count.p ? g->oct_count : dc_host(nleaves);
+        k_octant_partition<32><<<blocks_for((uint64_t)nleaves * 32u, 256), 256, 0, g->stream>>>(
+            g->leaf_range.as<int2>(), nlc, g->nodes[0].as<GvxNode>(), g->pts.pos, g->pts.pos_off, g->pts.pos_stride,
+            g->sort_trans[0], g->sort_trans[1], g->sort_trans[2], g->brick / 2, vin, vtmp, g->leaf_oct.as<int>(),
+            attr ? *attr : none);
         g->launches++;
         GVX_CK(cudaMemcpyAsync(vin, vtmp, vb, cudaMemcpyDeviceToDevice, g->stream));
         GVX_CK(cudaGetLastError());
@@ -1167,6 +1286,16 @@ gvx_status gvx_topo_octants(gvx_grid* g, const GvxSortedAttr* attr)
     g->oct_valid = true;
     g->perm_valid = false;  // the sorted attributes follow the new order (the caller sets it when attr wrote them)
     return GVX_OK;
+}
+
+// k_dilate's per-axis limit: the key space's end or the root's (rootpos in voxels, the root's
+// side in leaves), whichever comes first
+static int3 dilate_limit(const KeySpace& ks, const int rootpos[3], int brick, int root_leaves)
+{
+    int l[3];
+    for (int a = 0; a < 3; a++)
+        l[a] = (int)std::min<int64_t>(int64_t(1) << ks.bits[a], (int64_t)rootpos[a] / brick + root_leaves - ks.lo[a]);
+    return make_int3(l[0], l[1], l[2]);
 }
 
 static gvx_status grow_nodes(gvx_grid* g, int lev, int64_t cnt)
@@ -1191,24 +1320,20 @@ struct FullBuild {
     KeySpace ks;
     uint32_t words0;
     UpperDesc ud;
+    float mn[3], mx[3];  // the points' bounding box (GetBoundingBox before its margins)
 };
 
-// Everything of a full build (VG.cpp:1229-1413) up to the node counts, which are
-// queued for the host; topo_full_complete reads them and writes the pools.
-static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float o[3], int depth,
-                                   const int rootpos[3], const float mn[3], const float mx[3], FullBuild& fb)
+static gvx_status topo_full_launch_ks(gvx_grid* g, int n, float radius, const float o[3], int depth,
+                                      const int rootpos[3], const KeySpace& ks, FullBuild& fb, bool queue_readback);
+
+// the compact level-0 key space of a full build over the points' bounding box
+// (+ dilation margin), inside the root
+// (widen > 0: every axis's range grows by 1/widen of its length + 1 leaf on each side, inside
+// the root -- the key space of a plan; hi_out: the last leaf coordinate of the range per axis)
+static gvx_status full_key_space(gvx_grid* g, float radius, int depth, const int rootpos[3], const float mn[3],
+                                 const float mx[3], KeySpace& ks, int widen = 0, int* hi_out = nullptr)
 {
-    cudaStream_t st = g->stream;
     const int b = g->brick;
-    const bool extra = radius >= 1.0f;
-    if (extra && radius > 0.5f * (float)(b - 1)) {
-        gvx_set_error("RebuildTopology: radius %g exceeds (brick-1)/2 = %g (dilation beyond the 26 neighbours)",
-                      radius, 0.5 * (b - 1));
-        return GVX_ERR_UNSUPPORTED;
-    }
-    // ---- compact level-0 key space over the points' bounding box (+ dilation margin), inside the root
-    KeySpace ks;
-    const int root_lo = rootpos[0] / b;
     const int root_span = g->range[depth] / b;  // leaves per root side
     const int align = 1 << g->tshift[depth - 1];
     int64_t total_bits = 0;
@@ -1217,22 +1342,59 @@ static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float
         const float lo_v = mn[a] > 0.f ? mn[a] : 0.f;
         int lo = (int)floorf((lo_v - radius - 2.0f) / (float)b);
         int hi = mx[a] < 0.f ? rl : (int)floorf((mx[a] + 2.0f * radius + 2.0f) / (float)b);
+        if (widen > 0 && hi >= lo) {
+            const int m = (hi - lo + 1) / widen + 1;
+            lo -= m;
+            hi += m;
+        }
         lo = std::max(lo, rl);
         hi = std::min(hi, rl + root_span - 1);
         if (hi < lo) hi = lo;
         lo = rl + ((lo - rl) / align) * align;
         ks.lo[a] = lo;
         ks.bits[a] = ceil_log2((int64_t)hi - lo + 1);
+        if (hi_out) hi_out[a] = hi;
         total_bits += ks.bits[a];
     }
-    (void)root_lo;
     if (total_bits > 30) {
         gvx_set_error("RebuildTopology: point extents span 2^%lld leaf cells; the compact key space holds 2^30",
                       (long long)total_bits);
         return GVX_ERR_UNSUPPORTED;
     }
     ks.total_bits = (int)total_bits;
-    const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << total_bits) / 32ull));
+    return GVX_OK;
+}
+
+// Everything of a full build (VG.cpp:1229-1413) up to the node counts, which are
+// queued for the host; topo_full_complete reads them and writes the pools.
+static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float o[3], int depth,
+                                   const int rootpos[3], const float mn[3], const float mx[3], FullBuild& fb)
+{
+    const int b = g->brick;
+    if (radius >= 1.0f && radius > 0.5f * (float)(b - 1)) {
+        gvx_set_error("RebuildTopology: radius %g exceeds (brick-1)/2 = %g (dilation beyond the 26 neighbours)",
+                      radius, 0.5 * (b - 1));
+        return GVX_ERR_UNSUPPORTED;
+    }
+    KeySpace ks;
+    gvx_status rc = full_key_space(g, radius, depth, rootpos, mn, mx, ks);
+    if (rc) return rc;
+    for (int a = 0; a < 3; a++) {
+        fb.mn[a] = mn[a];
+        fb.mx[a] = mx[a];
+    }
+    return topo_full_launch_ks(g, n, radius, o, depth, rootpos, ks, fb, true);
+}
+
+// a full build in key space `ks` up to its node counts (d_counts), which are queued for the
+// host when queue_readback
+static gvx_status topo_full_launch_ks(gvx_grid* g, int n, float radius, const float o[3], int depth,
+                                      const int rootpos[3], const KeySpace& ks, FullBuild& fb, bool queue_readback)
+{
+    cudaStream_t st = g->stream;
+    const int b = g->brick;
+    const bool extra = radius >= 1.0f;
+    const uint32_t words0 = std::max<uint32_t>(1u, (uint32_t)((1ull << ks.total_bits) / 32ull));
     const uint32_t invalid_key = 1u << ks.total_bits;
 
     // ---- scratch
@@ -1268,24 +1430,26 @@ static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float
     uint32_t* counts = g->d_counts.as<uint32_t>();
 
     // ---- D0: leaves holding points
-    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, invalid_key, g->d0_bits.as<uint32_t>());
+    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, g->key_shift, invalid_key,
+                                                    g->d0_bits.as<uint32_t>());
     g->launches++;
     rc = gvx_bitmap_prefix(g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0, counts + 0, g->tmp_scan,
                            st, &g->launches);
     if (rc) return rc;
     BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
-    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>());
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>(), 0xFFFFFFFFu);
     g->launches++;
 
     // ---- X0: dilation leaves (radius >= 1, VG.cpp:1207-1208)
     BitRank x0{g->x0_bits.as<uint32_t>(), g->x0_prefix.as<uint32_t>(), words0};
     if (extra) {
         GVX_CK(cudaMemsetAsync(g->masks.p, 0, (size_t)n * 4, st));
-        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
+        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, g->key_shift, invalid_key, d0, g->pts.pos,
                                                           g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
                                                           radius, 2.0f, b, g->masks.as<uint32_t>());
-        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), counts + 0, ks,
-                                                     g->masks.as<uint32_t>(), d0, x0.bits, g->d_err.as<uint32_t>());
+        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(
+            g->leaf_key.as<uint32_t>(), counts + 0, ks, dilate_limit(ks, rootpos, b, g->range[depth] / b),
+            g->masks.as<uint32_t>(), d0, x0.bits, g->d_err.as<uint32_t>());
         g->launches += 2;
     }
     rc = gvx_bitmap_prefix(x0.bits, x0.prefix, words0, counts + 1, g->tmp_scan, st, &g->launches);
@@ -1312,7 +1476,7 @@ static gvx_status topo_full_launch(gvx_grid* g, int n, float radius, const float
     fb.ks = ks;
     fb.words0 = words0;
     fb.ud = ud;
-    return readback_start(g, counts, 64 * sizeof(uint32_t), "RebuildTopology");
+    return queue_readback ? readback_start(g, counts, 64 * sizeof(uint32_t), "RebuildTopology") : GVX_OK;
 }
 
 static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
@@ -1358,7 +1522,7 @@ static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
     for (int l = 1; l < depth; l++) list_words += (size_t)Ul[l] + Xl[l];
     GVX_CK(gvx_ensure(g->lists, list_words * 4));
     uint32_t* x0list = g->lists.as<uint32_t>();
-    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, x0.prefix, words0, x0list);
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, x0.prefix, words0, x0list, 0xFFFFFFFFu);
     g->launches++;
     uint32_t* lp = x0list + X0 + 1;
     const uint32_t* dl[GVX_MAXLEV] = {};
@@ -1368,10 +1532,10 @@ static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
     for (int l = 1; l < depth; l++) {
         uint32_t* base = g->upper.as<uint32_t>() + ud.off[l];
         const uint32_t w = ud.words[l];
-        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base, base + 2 * w, w, lp);
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base, base + 2 * w, w, lp, 0xFFFFFFFFu);
         dl[l] = lp;
         lp += Ul[l];
-        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base + w, base + 3 * w, w, lp);
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base + w, base + 3 * w, w, lp, 0xFFFFFFFFu);
         xl[l] = lp;
         lp += Xl[l];
         g->launches += 2;
@@ -1379,7 +1543,7 @@ static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
     // leaf keys in pool order: D0 (already there) then X0
     GVX_CK(gvx_ensure(g->leaf_key, (size_t)std::max<uint64_t>((uint64_t)U0 + X0, (uint64_t)n) * 4 + 4));
     // (ensure may have reallocated: D0 list must be rebuilt in that case)
-    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>());
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, g->leaf_key.as<uint32_t>(), 0xFFFFFFFFu);
     dl[0] = g->leaf_key.as<uint32_t>();
     if (X0)
         GVX_CK(cudaMemcpyAsync(g->leaf_key.as<uint32_t>() + U0, x0list, (size_t)X0 * 4, cudaMemcpyDeviceToDevice, st));
@@ -1430,11 +1594,13 @@ static gvx_status topo_full_complete(gvx_grid* g, const FullBuild& fb)
     g->lookup.b = x0;
     g->lookup.b_offset = U0;
     g->lookup.remap = nullptr;
+    g->lookup.b_offset_p = nullptr;
+    g->lookup.cap = 0;
     g->lookup_valid = true;
     const uint32_t L0 = U0 + X0;
     GVX_CK(gvx_ensure(g->nbr, (size_t)std::max<uint32_t>(L0, 1u) * 27 * sizeof(int)));
     if (L0) {
-        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), L0, g->lookup,
+        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), dc_host(L0), g->lookup,
                                                                         g->nbr.as<int>());
         g->launches++;
     }
@@ -1522,10 +1688,12 @@ static gvx_status build_active_lookup(gvx_grid* g, const KeySpace& ks, uint32_t 
     g->lookup.b = BitRank{nullptr, nullptr, 0u};
     g->lookup.b_offset = 0u;
     g->lookup.remap = g->remap.as<int>();
+    g->lookup.b_offset_p = nullptr;
+    g->lookup.cap = 0;
     g->lookup_valid = true;
     GVX_CK(gvx_ensure(g->nbr, (size_t)std::max<uint32_t>(L0, 1u) * 27 * sizeof(int)));
     if (L0) {
-        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), L0, g->lookup,
+        k_neighbors<<<blocks_for((uint64_t)L0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(), dc_host(L0), g->lookup,
                                                                         g->nbr.as<int>());
         g->launches++;
     }
@@ -1633,22 +1801,24 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
     if (rc) return rc;
     const uint32_t* skeys = g->keys[g->sorted_buf].as<uint32_t>();
     const uint32_t* svals = g->vals[g->sorted_buf].as<uint32_t>();
-    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, invalid_key, g->d0_bits.as<uint32_t>());
+    k_mark_runs<<<blocks_for(n, 256), 256, 0, st>>>(skeys, (uint32_t)n, g->key_shift, invalid_key,
+                                                    g->d0_bits.as<uint32_t>());
     g->launches++;
     rc = gvx_bitmap_prefix(g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0, counts + kCntD0,
                            g->tmp_scan, st, &g->launches);
     if (rc) return rc;
     const BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
     uint32_t* dlist = g->lists.as<uint32_t>();
-    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, dlist);
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(d0.bits, d0.prefix, words0, dlist, 0xFFFFFFFFu);
     g->launches++;
     if (radius > 0.f) {
         GVX_CK(cudaMemsetAsync(g->masks.p, 0, (size_t)n * 4, st));
-        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, invalid_key, d0, g->pts.pos,
+        k_point_masks<<<blocks_for(n, 256), 256, 0, st>>>(skeys, svals, (uint32_t)n, g->key_shift, invalid_key, d0, g->pts.pos,
                                                           g->pts.pos_off, g->pts.pos_stride, o[0], o[1], o[2],
                                                           radius, 1.0f, b, g->masks.as<uint32_t>());
-        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(dlist, counts + kCntD0, ks, g->masks.as<uint32_t>(), d0,
-                                                     g->x0_bits.as<uint32_t>(), err);
+        k_dilate<<<std::min(blocks_for(n, 256), 152u * 8u), 256, 0, st>>>(
+            dlist, counts + kCntD0, ks, dilate_limit(ks, g->root_pos, b, g->range[R] / b), g->masks.as<uint32_t>(), d0,
+            g->x0_bits.as<uint32_t>(), err);
         g->launches += 2;
     }
     if (ud.nlev > 0) {
@@ -1736,7 +1906,7 @@ static gvx_status topo_incremental(gvx_grid* g, int n, float radius, const float
         uint32_t* lp = g->lists.as<uint32_t>();
         for (int l = 0; l < depth; l++) {
             if (!nnew[l]) continue;
-            k_select<<<blocks_for(Nb[l].words, 256), 256, 0, st>>>(Nb[l].bits, Nb[l].prefix, Nb[l].words, lp);
+            k_select<<<blocks_for(Nb[l].words, 256), 256, 0, st>>>(Nb[l].bits, Nb[l].prefix, Nb[l].words, lp, 0xFFFFFFFFu);
             g->launches++;
             nl[l] = lp;
             lp += nnew[l];
@@ -1831,6 +2001,34 @@ static gvx_status full_status(gvx_grid* g, gvx_status rc)
     return GVX_OK;
 }
 
+// GetBoundingBox's box read back (hb[0..5], order-preserving float bits) -> the points' box
+// (mn, mx), bbox_min/max with the reference's margins (VG.cpp:5452-5460), and DetermineDepth:
+// the lowest level whose node covers posMin and posMax, and that node's position (depth -1: none)
+static void bbox_depth(gvx_grid* g, const uint32_t* hb, float mn[3], float mx[3], int* depth, int rootpos[3])
+{
+    int pmin[3], pmax[3];
+    for (int a = 0; a < 3; a++) {
+        mn[a] = ord2f(hb[a]);
+        mx[a] = ord2f(hb[3 + a]);
+        float lo = mn[a] - 1.0f, hi = mx[a] + 2.0f;
+        lo = 0 > lo ? 0 : lo;
+        hi = 0 > hi ? 0 : hi;
+        g->bbox_min[a] = lo;
+        g->bbox_max[a] = hi;
+        pmin[a] = (int)lo;
+        pmax[a] = (int)hi;
+    }
+    *depth = -1;
+    for (int l = 0; l < g->levels; l++) {
+        const int r = g->range[l];
+        if (pmin[0] / r == pmax[0] / r && pmin[1] / r == pmax[1] / r && pmin[2] / r == pmax[2] / r) {
+            *depth = l;
+            for (int a = 0; a < 3; a++) rootpos[a] = pmin[a] / r * r;
+            break;
+        }
+    }
+}
+
 // RebuildTopology up to GetBoundingBox's readback, which is queued
 static gvx_status rebuild_begin(gvx_grid* g, int n, float radius, const float orig[3], int mode)
 {
@@ -1886,28 +2084,8 @@ static gvx_status rebuild_after_bbox(gvx_grid* g, int n, float radius, const flo
     const float o[3] = {orig ? orig[0] : 0.f, orig ? orig[1] : 0.f, orig ? orig[2] : 0.f};
     if (pending) *pending = false;
     float mn[3], mx[3];
-    int pmin[3], pmax[3];
-    for (int a = 0; a < 3; a++) {
-        mn[a] = ord2f(hb[a]);
-        mx[a] = ord2f(hb[3 + a]);
-        float lo = mn[a] - 1.0f, hi = mx[a] + 2.0f;  // VG.cpp:5452-5460
-        lo = 0 > lo ? 0 : lo;
-        hi = 0 > hi ? 0 : hi;
-        g->bbox_min[a] = lo;
-        g->bbox_max[a] = hi;
-        pmin[a] = (int)lo;
-        pmax[a] = (int)hi;
-    }
-    // ---- DetermineDepth: lowest level whose node covers posMin and posMax
     int depth = -1, rootpos[3] = {0, 0, 0};
-    for (int l = 0; l < g->levels; l++) {
-        const int r = g->range[l];
-        if (pmin[0] / r == pmax[0] / r && pmin[1] / r == pmax[1] / r && pmin[2] / r == pmax[2] / r) {
-            depth = l;
-            for (int a = 0; a < 3; a++) rootpos[a] = pmin[a] / r * r;
-            break;
-        }
-    }
+    bbox_depth(g, hb, mn, mx, &depth, rootpos);
     int act[6];
     memcpy(act, hb + 8, sizeof(act));
     if (mode == GVX_TOPO_ACCUMULATE && !g->rebuild_topo) {
@@ -1973,6 +2151,8 @@ struct gvx_topo_staged {
     int mode, min_depth;
     bool pending;
     FullBuild fb;
+    bool last_full;     // the last stage 3 finished a full build (fb), the tree is still that one
+    uint64_t last_gen;  // topo_gen after it
 };
 
 gvx_status gvx_topo_stage1(gvx_grid* g, int n, float radius, int mode, int min_depth)
@@ -1984,6 +2164,7 @@ gvx_status gvx_topo_stage1(gvx_grid* g, int n, float radius, int mode, int min_d
     S.mode = mode;
     S.min_depth = min_depth;
     S.pending = false;
+    S.last_full = false;
     return rebuild_begin(g, n, radius, nullptr, mode);
 }
 
@@ -2001,13 +2182,405 @@ gvx_status gvx_topo_stage3(gvx_grid* g)
     gvx_topo_staged& S = *g->staged;
     if (!S.pending) return GVX_OK;
     S.pending = false;
-    return full_status(g, topo_full_complete(g, S.fb));
+    gvx_status rc = full_status(g, topo_full_complete(g, S.fb));
+    S.last_full = rc == GVX_OK;
+    S.last_gen = g->topo_gen;
+    return rc;
 }
 
 void gvx_topo_staged_free(gvx_grid* g)
 {
     delete g->staged;
     g->staged = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Planned full builds, for batches of grids rebuilt every frame (gvx_batch_frame).
+// A full build waits on the host twice: for the bounding box, from which the
+// host takes the depth, the root and the compact key space, and for the node
+// counts, which size the pools.  A plan fixes both from the grid's last full
+// build: the key space (that build's, widened on every side by an eighth of its
+// extent and a leaf), the depth and root, and every pool's capacity (its count + 25% + 64).
+// A planned build then queues GetBoundingBox, the full RebuildTopology, UpdateAtlas
+// and the octant/attribute pass of InsertPoints with no host wait and no
+// allocation, so that a batch of them can be captured in one CUDA graph: its
+// kernels take the counts from device memory (DevCount) and clamp every write to
+// the capacities.  The counts, the bounding box and the device error word go to
+// pinned memory at the end.  Once the stream has passed them, gvx_topo_plan_finish
+// checks that the plan held: the frame's own DetermineDepth gives the plan's root,
+// the frame's own key space lies inside the plan's, and every count fits its
+// capacity.  Then the pools, lists and atlas are those of an unplanned build --
+// the pool order is the order of the leaf coordinates (x, y, z lexicographic),
+// the same in every key space that holds them -- and the host state is set as an
+// unplanned build sets it.  Otherwise the planned build is void and the caller
+// builds the grid again without a plan.
+
+enum { kRecCounts = 0, kRecBbox = 64, kRecErr = 80, kRecWords = 96 };
+enum { kCntSlots = 56 };  // d_counts slot of a planned UpdateAtlas's slot count
+
+struct gvx_topo_plan {
+    FullBuild fb;                      // key space, depth, root, points, radius (words0, ud after enqueue)
+    uint32_t cap[GVX_MAXLEV] = {};     // node capacity of levels 0 .. depth-1
+    uint32_t* rec = nullptr;           // pinned: counts, bounding box, error word of the last build
+    int sorted_buf = 0;                // where the planned sort leaves the keys
+    uint64_t id = 0;
+    bool enqueued = false;
+};
+
+static std::atomic<uint64_t> g_plan_ids{0};
+
+void gvx_topo_plan_free(gvx_grid* g)
+{
+    if (!g->plan) return;
+    if (g->plan->rec) cudaFreeHost(g->plan->rec);
+    delete g->plan;
+    g->plan = nullptr;
+}
+
+// (a plan fixes sizes, not addresses: any points of the same count may be built under it)
+bool gvx_topo_plan_ready(const gvx_grid* g)
+{
+    return g->plan && g->plan->id && g->pts.pos && g->pts.n == g->plan->fb.n;
+}
+
+uint64_t gvx_topo_plan_id(const gvx_grid* g) { return g->plan ? g->plan->id : 0; }
+
+const uint32_t* gvx_topo_plan_slots(const gvx_grid* g, uint32_t* cap)
+{
+    *cap = g->plan ? g->plan->cap[0] : 0u;
+    return g->d_counts.as<uint32_t>() + kCntSlots;
+}
+
+gvx_status gvx_topo_plan_make(gvx_grid* g)
+{
+    const gvx_topo_staged* S = g->staged;
+    if (!S || !S->last_full || S->last_gen != g->topo_gen || g->root_level < 0 || !g->lookup_valid) {
+        gvx_set_error("plan: the grid's tree is not the result of a staged full build");
+        return GVX_ERR_STATE;
+    }
+    if (!g->plan) g->plan = new gvx_topo_plan();
+    gvx_topo_plan& P = *g->plan;
+    P.id = 0;
+    P.enqueued = false;
+    if (!P.rec) GVX_CK(cudaMallocHost(&P.rec, kRecWords * sizeof(uint32_t)));
+    const FullBuild& last = S->fb;
+    KeySpace ks;
+    // the widened key space, unless it would hold more than 8x the build's cells
+    if (full_key_space(g, last.radius, last.depth, last.rootpos, last.mn, last.mx, ks, 8) != GVX_OK ||
+        ks.total_bits > last.ks.total_bits + 3)
+        ks = last.ks;
+    P.fb = last;
+    P.fb.ks = ks;
+    for (int l = 0; l < GVX_MAXLEV; l++) P.cap[l] = 0;
+    for (int l = 0; l < last.depth; l++) {
+        const uint64_t c = (uint64_t)g->count[l];
+        const uint64_t cap = c + c / 4 + 64;
+        if (cap >= (1ull << 31)) {
+            gvx_set_error("plan: level %d holds %llu nodes", l, (unsigned long long)c);
+            return GVX_ERR_CAPACITY;
+        }
+        P.cap[l] = (uint32_t)cap;
+    }
+    P.id = ++g_plan_ids;
+    return GVX_OK;
+}
+
+// pools, child lists, leaf keys, lookup, neighbours and point ranges of a planned build (the
+// part of topo_full_complete after the counts), every launch over the capacities
+static gvx_status plan_pools(gvx_grid* g, const gvx_topo_plan& P, const FullBuild& fb)
+{
+    cudaStream_t st = g->stream;
+    const int depth = fb.depth;
+    const KeySpace ks = fb.ks;
+    const uint32_t words0 = fb.words0;
+    const UpperDesc& ud = fb.ud;
+    const uint32_t* dcnt = g->d_counts.as<uint32_t>();
+    const uint32_t cap0 = P.cap[0];
+    const BitRank d0{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), words0};
+    const BitRank x0{g->x0_bits.as<uint32_t>(), g->x0_prefix.as<uint32_t>(), words0};
+
+    for (int l = 0; l < depth; l++) GVX_CK_STATUS(grow_nodes(g, l, P.cap[l]));
+    GVX_CK_STATUS(grow_nodes(g, depth, 1));
+    for (int l = 1; l <= depth; l++) {
+        const size_t vc = (size_t)g->res[l] * g->res[l] * g->res[l];
+        const size_t cnt = l < depth ? P.cap[l] : 1;
+        GVX_CK(cudaMemsetAsync(g->clist[l].p, 0xFF, cnt * vc * sizeof(uint64_t), st));
+    }
+    // lists: X0 (cap0), then D_l and X_l (cap_l each) per upper level
+    size_t list_words = cap0;
+    for (int l = 1; l < depth; l++) list_words += 2 * (size_t)P.cap[l];
+    GVX_CK(gvx_ensure(g->lists, list_words * 4 + 4));
+    uint32_t* x0list = g->lists.as<uint32_t>();
+    k_select<<<blocks_for(words0, 256), 256, 0, st>>>(x0.bits, x0.prefix, words0, x0list, cap0);
+    g->launches++;
+    uint32_t* lp = x0list + cap0;
+    const uint32_t* dl[GVX_MAXLEV] = {};
+    const uint32_t* xl[GVX_MAXLEV] = {};
+    dl[0] = g->leaf_key.as<uint32_t>();  // the D0 list of the first half; level 0's nodes append X0 to it
+    xl[0] = x0list;
+    for (int l = 1; l < depth; l++) {
+        uint32_t* base = g->upper.as<uint32_t>() + ud.off[l];
+        const uint32_t w = ud.words[l];
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base, base + 2 * w, w, lp, P.cap[l]);
+        dl[l] = lp;
+        lp += P.cap[l];
+        k_select<<<blocks_for(w, 256), 256, 0, st>>>(base + w, base + 3 * w, w, lp, P.cap[l]);
+        xl[l] = lp;
+        lp += P.cap[l];
+        g->launches += 2;
+    }
+
+    // ---- nodes, parents and child lists, top-down, counts from d_counts
+    k_write_root<<<1, 1, 0, st>>>(g->nodes[depth].as<GvxNode>(), depth, fb.rootpos[0], fb.rootpos[1],
+                                  fb.rootpos[2]);
+    g->launches++;
+    for (int l = depth - 1; l >= 0; l--) {
+        NodeLevelArgs a;
+        memset(&a, 0, sizeof(a));
+        a.lev = l;
+        a.depth = depth;
+        a.dlist = dl[l];
+        a.xlist = xl[l];
+        a.ks = ks;
+        a.tshift = g->tshift[l];
+        a.tshift_parent = g->tshift[l + 1];
+        a.logdim_parent = g->logdim[l + 1];
+        a.res_parent = g->res[l + 1];
+        for (int k = 0; k < 3; k++) {
+            a.lo[k] = ks.lo[k] >> g->tshift[l];
+            a.root_rel[k] = fb.rootpos[k] / g->range[l];
+        }
+        a.range = g->range[l];
+        a.ci_pu = -1;
+        if (l + 1 < depth) {
+            uint32_t* base = g->upper.as<uint32_t>() + ud.off[l + 1];
+            const uint32_t w = ud.words[l + 1];
+            a.pd = BitRank{base, base + 2 * w, w};
+            a.px = BitRank{base + w, base + 3 * w, w};
+            a.ci_pu = 2 + 2 * l;
+            a.pcap = P.cap[l + 1];
+        }
+        a.nodes = g->nodes[l].as<GvxNode>();
+        a.pclist = g->clist[l + 1].as<uint64_t>();
+        a.leaf_key = l == 0 ? g->leaf_key.as<uint32_t>() : nullptr;
+        a.dc = dcnt;
+        a.ci_u = l == 0 ? 0 : 2 + 2 * (l - 1);
+        a.ci_x = a.ci_u + 1;
+        a.cap = P.cap[l];
+        k_write_nodes<<<blocks_for(P.cap[l], 256), 256, 0, st>>>(a);
+        g->launches++;
+    }
+
+    // ---- leaf lookup (X0 offset U0 from d_counts), neighbours, point ranges
+    g->lookup.ks = ks;
+    g->lookup.a = d0;
+    g->lookup.b = x0;
+    g->lookup.b_offset = 0u;
+    g->lookup.remap = nullptr;
+    g->lookup.b_offset_p = dcnt;
+    g->lookup.cap = cap0;
+    GVX_CK(gvx_ensure(g->nbr, (size_t)cap0 * 27 * sizeof(int)));
+    k_neighbors<<<blocks_for((uint64_t)cap0 * 27, 256), 256, 0, st>>>(g->leaf_key.as<uint32_t>(),
+                                                                      dc_dev(dcnt, 0, 1, cap0), g->lookup,
+                                                                      g->nbr.as<int>());
+    g->launches++;
+    return fill_leaf_ranges(g, cap0);
+}
+
+// UpdateAtlas of a planned build: slots in pool order over the leaf capacity, the slot count
+// to d_counts[kCntSlots]
+static gvx_status plan_atlas(gvx_grid* g, const gvx_topo_plan& P)
+{
+    cudaStream_t st = g->stream;
+    const uint32_t cap0 = P.cap[0];
+    const DevCount nl = dc_dev(g->d_counts.as<uint32_t>(), 0, 1, cap0);
+    GVX_CK_STATUS(gvx_grow_atlas(g, cap0));
+    const int64_t slots = (int64_t)g->sub[0] * g->sub[1] * g->sub[2];
+    const uint32_t fw = cap0 / 32u + 1u;
+    GVX_CK(gvx_ensure(g->amap, (size_t)slots * sizeof(int4)));
+    GVX_CK(cudaMemsetAsync(g->amap.p, 0xFF, (size_t)slots * sizeof(int4), st));
+    GVX_CK(gvx_ensure(g->leaf_slot, (size_t)cap0 * 4));
+    GVX_CK(gvx_ensure(g->slot_leaf, (size_t)std::max<int64_t>(slots, 1) * 4));
+    GVX_CK(gvx_ensure(g->bm_a, (size_t)fw * 4));
+    GVX_CK(gvx_ensure(g->bm_a_prefix, (size_t)fw * 4));
+    GVX_CK(cudaMemsetAsync(g->bm_a.p, 0, (size_t)fw * 4, st));
+    k_flag_bits<<<blocks_for(cap0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), nl, g->bm_a.as<uint32_t>());
+    g->launches++;
+    GVX_CK_STATUS(gvx_bitmap_prefix(g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), fw,
+                                    g->d_counts.as<uint32_t>() + kCntSlots, g->tmp_scan, st, &g->launches));
+    k_atlas_assign<<<blocks_for(cap0, 256), 256, 0, st>>>(
+        g->nodes[0].as<GvxNode>(), nl, g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), g->sub[0], g->sub[1],
+        g->P, g->apron, g->leaf_slot.as<int>(), g->slot_leaf.as<int>(), g->amap.as<int4>());
+    g->launches++;
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr)
+{
+    if (!gvx_topo_plan_ready(g)) {
+        gvx_set_error("planned build: no plan for the grid's points");
+        return GVX_ERR_STATE;
+    }
+    gvx_topo_plan& P = *g->plan;
+    cudaStream_t st = g->stream;
+    const int n = P.fb.n, depth = P.fb.depth;
+    const uint32_t cap0 = P.cap[0];
+    const float o[3] = {0.f, 0.f, 0.f};
+    GVX_CK_STATUS(ensure_grid_scratch(g));
+    P.enqueued = false;
+
+    // ---- GetBoundingBox (read by gvx_topo_plan_finish)
+    k_bbox_reset<<<1, 32, 0, st>>>(g->d_bbox.as<uint32_t>());
+    const unsigned bb = (std::min(blocks_for(n, 256), 152u * 8u) + 2u) / 3u * 3u;
+    k_bbox<<<bb, 256, 0, st>>>(g->pts.pos, g->pts.pos_off, g->pts.pos_stride, (uint32_t)n, 0.f, 0.f, 0.f,
+                               g->d_bbox.as<uint32_t>(), g->d_err.as<uint32_t>());
+    g->launches += 2;
+
+    // ---- the full build in the plan's key space, sized by the capacities
+    GVX_CK(gvx_ensure(g->leaf_key, ((size_t)std::max<uint32_t>(cap0, (uint32_t)n) + 1) * 4));
+    FullBuild fb{};
+    GVX_CK_STATUS(topo_full_launch_ks(g, n, P.fb.radius, o, depth, P.fb.rootpos, P.fb.ks, fb, false));
+    P.fb.words0 = fb.words0;
+    P.fb.ud = fb.ud;
+    gvx_status rc = plan_pools(g, P, fb);
+    if (rc == GVX_OK) rc = plan_atlas(g, P);
+    // ---- InsertPoints: octant order and the sorted attributes over the leaf capacity
+    if (rc == GVX_OK) {
+        g->oct_count = dc_dev(g->d_counts.as<uint32_t>(), 0, 1, cap0);
+        g->oct_valid = false;
+        rc = gvx_topo_octants(g, attr);
+    }
+    // the kernels took the device counts by value: the host state goes back to host counts
+    g->oct_count = DevCount{};
+    g->lookup.b_offset_p = nullptr;
+    g->lookup.cap = 0;
+    g->lookup_valid = false;
+    if (rc) return rc;
+    GVX_CK(cudaMemcpyAsync(P.rec + kRecCounts, g->d_counts.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GVX_CK(cudaMemcpyAsync(P.rec + kRecBbox, g->d_bbox.p, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GVX_CK(cudaGetLastError());
+    P.sorted_buf = g->sorted_buf;
+    P.enqueued = true;
+    return GVX_OK;
+}
+
+// a captured planned build queued again (its graph launched)
+void gvx_topo_plan_replayed(gvx_grid* g)
+{
+    if (g->plan) g->plan->enqueued = true;
+}
+
+// the device error word into the plan's record, on `st` after the work that may set it (the
+// caller's: after the splat of the frame)
+gvx_status gvx_topo_plan_record_error(gvx_grid* g, cudaStream_t st)
+{
+    GVX_CK(cudaMemcpyAsync(g->plan->rec + kRecErr, g->d_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    return GVX_OK;
+}
+
+// a void planned build: nothing of the grid's tree, atlas or grouping is usable
+static void plan_void(gvx_grid* g)
+{
+    g->root_level = -1;
+    g->rebuild_topo = true;
+    g->lookup_valid = false;
+    g->group_valid = false;
+    g->nbr_valid = false;
+    g->atlas_valid = false;
+    g->atlas_prefix = -1;
+    g->oct_valid = false;
+    g->perm_valid = false;
+    g->used_leaves = 0;
+    for (int c = 0; c < GVX_MAXCH; c++) apron_invalidate(g->ch[c]);
+}
+
+gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held)
+{
+    *held = false;
+    if (!g->plan || !g->plan->enqueued) {
+        gvx_set_error("planned build: nothing queued");
+        return GVX_ERR_STATE;
+    }
+    gvx_topo_plan& P = *g->plan;
+    P.enqueued = false;
+    const uint32_t* rec = P.rec;
+    const int depth = P.fb.depth;
+    // as rebuild_begin / rebuild_after_bbox
+    g->sc_valid = false;
+    g->pools_appended = false;
+    g->topo_gen++;
+    g->atlas_gen++;
+    gvx_status rc = report_device_error(g, rec[kRecErr], "BatchFrame");  // (clears the word)
+    if (rc) {
+        plan_void(g);
+        return rc;
+    }
+    // did the plan hold?
+    float mn[3], mx[3];
+    int fdepth = -1, rootpos[3] = {0, 0, 0};
+    bbox_depth(g, rec + kRecBbox, mn, mx, &fdepth, rootpos);
+    bool ok = fdepth == depth;
+    for (int a = 0; a < 3; a++) ok = ok && rootpos[a] == P.fb.rootpos[a];
+    if (ok) {
+        KeySpace ks;
+        int hi[3];
+        if (full_key_space(g, P.fb.radius, depth, rootpos, mn, mx, ks, 0, hi) != GVX_OK) {
+            ok = false;
+        } else {
+            for (int a = 0; a < 3; a++)
+                ok = ok && ks.lo[a] >= P.fb.ks.lo[a] && (int64_t)hi[a] < (int64_t)P.fb.ks.lo[a] + (1ll << P.fb.ks.bits[a]);
+        }
+    }
+    uint64_t cnt[GVX_MAXLEV] = {};
+    for (int l = 0; l < depth && ok; l++) {
+        const int ci = l == 0 ? 0 : 2 + 2 * (l - 1);
+        cnt[l] = (uint64_t)rec[kRecCounts + ci] + rec[kRecCounts + ci + 1];
+        ok = cnt[l] <= P.cap[l];
+    }
+    ok = ok && rec[kRecCounts + kCntSlots] == cnt[0];  // every leaf of a full build is active
+    if (!ok) {
+        plan_void(g);
+        return GVX_OK;
+    }
+    // ---- the host state of a full build (topo_full_complete, full_status) ...
+    const uint32_t U0 = rec[kRecCounts + 0];
+    for (int l = 0; l < GVX_MAXLEV; l++) g->count[l] = 0;
+    for (int l = 0; l < depth; l++) g->count[l] = (int64_t)cnt[l];
+    g->count[depth] = 1;
+    g->lookup.ks = P.fb.ks;
+    g->lookup.a = BitRank{g->d0_bits.as<uint32_t>(), g->d0_prefix.as<uint32_t>(), P.fb.words0};
+    g->lookup.b = BitRank{g->x0_bits.as<uint32_t>(), g->x0_prefix.as<uint32_t>(), P.fb.words0};
+    g->lookup.b_offset = U0;
+    g->lookup.remap = nullptr;
+    g->lookup.b_offset_p = nullptr;
+    g->lookup.cap = 0;
+    g->lookup_valid = true;
+    g->nbr_valid = true;
+    g->sorted_buf = P.sorted_buf;
+    g->n_sorted = (uint32_t)P.fb.n;
+    for (int a = 0; a < 3; a++) {
+        g->sort_trans[a] = 0.f;
+        g->group_trans[a] = 0.f;
+        g->root_pos[a] = P.fb.rootpos[a];
+    }
+    g->group_valid = true;
+    g->group_pos = g->pts.pos;
+    g->group_n = P.fb.n;
+    g->root_level = depth;
+    g->used_leaves = (int64_t)cnt[0];
+    g->rebuild_topo = false;
+    g->last_rebuild = 1;
+    // ... of UpdateAtlas (gvx_topo_update_atlas: every brick in a new slot) ...
+    g->atlas_used = (int64_t)cnt[0];
+    g->atlas_valid = true;
+    for (int c = 0; c < GVX_MAXCH; c++) apron_invalidate(g->ch[c]);
+    g->atlas_prefix = g->atlas_used;
+    // ... and of the octant pass of InsertPoints (the attributes: the caller)
+    g->oct_leaves = (uint32_t)cnt[0];
+    g->oct_valid = true;
+    g->perm_valid = false;
+    *held = true;
+    return GVX_OK;
 }
 
 
@@ -2123,13 +2696,13 @@ gvx_status gvx_topo_update_atlas(gvx_grid* g)
     GVX_CK(gvx_ensure(g->bm_a_prefix, (size_t)fw * 4));
     GVX_CK(cudaMemsetAsync(g->bm_a.p, 0, (size_t)fw * 4, st));
     if (L0) {
-        k_flag_bits<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), L0, g->bm_a.as<uint32_t>());
+        k_flag_bits<<<blocks_for(L0, 256), 256, 0, st>>>(g->nodes[0].as<GvxNode>(), dc_host(L0), g->bm_a.as<uint32_t>());
         g->launches++;
         rc = gvx_bitmap_prefix(g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), fw, nullptr, g->tmp_scan, st,
                                &g->launches);
         if (rc) return rc;
         k_atlas_assign<<<blocks_for(L0, 256), 256, 0, st>>>(
-            g->nodes[0].as<GvxNode>(), L0, g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), g->sub[0],
+            g->nodes[0].as<GvxNode>(), dc_host(L0), g->bm_a.as<uint32_t>(), g->bm_a_prefix.as<uint32_t>(), g->sub[0],
             g->sub[1], g->P, g->apron, g->leaf_slot.as<int>(), g->slot_leaf.as<int>(), g->amap.as<int4>());
         g->launches++;
     }

@@ -110,6 +110,8 @@ def load(path=None):
         "gvx_batch_splat": ([vp, i, f, i, i, i, i], i),
         "gvx_batch_get_tuning": ([vp, ip, ip, fp], i),
         "gvx_batch_topology": ([vp, f, i, i], i),
+        "gvx_batch_frame": ([vp, f, i, f, i, i, i], i),
+        "gvx_batch_frame_path": ([vp, ip, ip], i),
         "gvx_test_sort_withheld_tile": ([vp, vp, vp, vp, vp, ctypes.c_uint32], i),
         "gvx_batch_kernel_launches": ([vp, ctypes.POINTER(i64)], i),
     }
@@ -475,6 +477,20 @@ class Batch:
         from this thread (threads 0) or as per-grid calls from a pool of host threads"""
         self._check(self.lib.gvx_batch_topology(self.h, float(radius), TOPO_FULL if mode is None else mode,
                                                 int(threads)))
+
+    def frame(self, topo_radius, mode, radius, chan_density=0, chan_vel=-1, graph=True, tune=False):
+        """gvx_batch_frame: full RebuildTopology + UpdateAtlas + InsertPoints of every grid, then the
+        batched splat; planned builds (and, with graph, one captured CUDA graph) once plans exist"""
+        flags = (BATCH_GRAPH if graph else 0) | (BATCH_TUNE if tune else 0)
+        self._check(self.lib.gvx_batch_frame(self.h, float(topo_radius), mode, float(radius), chan_density, chan_vel,
+                                              flags))
+
+    def frame_path(self):
+        """(path, rebuilt) of the last frame: path 0 unplanned, 1 planned, 2 graph replay; rebuilt =
+        grids built again without their plan"""
+        p, r = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self.lib.gvx_batch_frame_path(self.h, ctypes.byref(p), ctypes.byref(r)))
+        return p.value, r.value
 
     def tuning(self):
         la, bp, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0)

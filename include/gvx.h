@@ -404,6 +404,31 @@ gvx_status gvx_batch_get_tuning(gvx_batch* b, int* slab_layers, int* blocks_per_
  * host threads.  Grids that share a stream build one after another.  The first
  * failing grid's status is returned, its index in gvx_last_error(). */
 gvx_status gvx_batch_topology(gvx_batch* b, float radius, int mode, int threads);
+/* A whole frame of a batch (no reference counterpart; it replaces, per point cloud,
+ * the loop RebuildTopology gvdb_volume_gvdb.cpp:1181-1218 -> UpdateAtlas
+ * :2650-2690 -> InsertPoints :5219-5267 -> the splat with its aprons): every
+ * grid's full rebuild over its bound points (topo_radius, no origin), UpdateAtlas,
+ * InsertPoints, then gvx_batch_splat(mode, radius, chan_density, chan_vel, no
+ * accumulation).  Results are those of the per-grid calls, bit for bit.
+ * The first frame (and any frame after set_grids, a new topo_radius or rebound
+ * points) runs gvx_batch_topology staged and gvx_batch_splat, and makes every
+ * grid a PLAN from its build: the compact key space widened by an eighth of its
+ * extent and a leaf per side, the depth and root, and each pool's capacity (count + 25% +
+ * 64).  Later frames build under the plans: no host wait and no allocation
+ * inside the frame, counts read by the kernels from device memory.  With
+ * GVX_BATCH_GRAPH, from the second planned frame on, all grids' builds (each on
+ * its grid's stream, forked from the batch stream) and the splat run as ONE
+ * captured CUDA graph, replayed while no libgvx buffer has moved.  The call
+ * waits for the frame (one host synchronisation) and checks every plan: a grid
+ * whose points left the plan's root or key space, or outgrew a capacity, is built
+ * and splatted again without it and planned anew (gvx_batch_frame_path reports
+ * how many).  GVX_BATCH_TUNE as for gvx_batch_splat, on the first frame. */
+gvx_status gvx_batch_frame(gvx_batch* b, float topo_radius, int mode, float radius, int chan_density, int chan_vel,
+                           int flags);
+/* How the last gvx_batch_frame ran: *path 0 = unplanned (staged topology, plans
+ * made), 1 = planned without a graph, 2 = the captured graph replayed;
+ * *rebuilt = the grids built again without a plan. */
+gvx_status gvx_batch_frame_path(gvx_batch* b, int* path, int* rebuilt);
 
 /* Test hook (no reference counterpart): one pass of the radix sort over n > 4096
  * keys with its first tile withheld, so the decoupled look-back of the second
