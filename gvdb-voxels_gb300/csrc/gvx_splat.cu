@@ -487,7 +487,12 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     // an accumulating splat leaves a slab that no point reaches as it is: no load, no store
     if (a.accum && total == 0) return;
 
-    // ---- tile: previous values (accumulate) or zeros
+    // ---- tile: previous values (accumulate) or zeros, once the bulk store of the warp's last
+    // slab has read it (the wait is deferred to here: that read overlaps the ranges above)
+    if (BULK) {
+        if (lane == 0) bulk_wait_read_all();
+        __syncwarp();
+    }
     if (a.accum) {
         if (BULK) {
             if (lane == 0) {
@@ -523,6 +528,9 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     float4 bp = make_float4(0.f, 0.f, 0.f, 0.f), buv = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t bb0 = 0u, bb1 = 0u;
     int bnc = 0, nb = 0;  // this lane's cell count; points in the batch (warp-uniform)
+    // the regions of the padded slab (bit (dx+1)*9 + (dy+1)*3 + (dz+1): below, inside or above
+    // the interior on each axis) that this lane's hits reach
+    uint32_t touched = 0u;
     for (int base = 0;; base += 32) {
         const bool done = base >= total;  // one more pass deals the last batch
         const int v = base + lane;
@@ -563,6 +571,17 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
                 ncell = nch * ny * (zh - zl + 1);
                 box0 = (uint32_t)xl | ((uint32_t)xh << 8) | ((uint32_t)yl << 16) | ((uint32_t)yh << 24);
                 box1 = (uint32_t)zl | ((uint32_t)zh << 8);
+                // per axis: 1 = reaches below the interior, 2 = the interior, 4 = above it; the
+                // product of the three spread sets has one bit per region reached (no carries)
+                const int zpl = z0 + zl, zph = z0 + zh;
+                const uint32_t tx = (uint32_t)(xl < ap) | (uint32_t)(xl <= P - 1 - ap && xh >= ap) << 1 |
+                                    (uint32_t)(xh > P - 1 - ap) << 2;
+                const uint32_t ty = (uint32_t)(yl < ap) | (uint32_t)(yl <= P - 1 - ap && yh >= ap) << 1 |
+                                    (uint32_t)(yh > P - 1 - ap) << 2;
+                const uint32_t tz = (uint32_t)(zpl < ap) | (uint32_t)(zpl <= P - 1 - ap && zph >= ap) << 1 |
+                                    (uint32_t)(zph > P - 1 - ap) << 2;
+                touched |= ((tx & 1u) | (tx & 2u) << 8 | (tx & 4u) << 16) *
+                           ((ty & 1u) | (ty & 2u) << 2 | (ty & 4u) << 4) * tz;
             }
         }
         const uint32_t hm = __ballot_sync(kFull, ncell > 0);
@@ -610,11 +629,14 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     }
 
     // ---- apron voxels with no neighbouring brick take the boundary value (0):
-    // the apron region facing each missing neighbour (apron 1), clipped to the slab
-    if (ap && (nbmask & 0x7FFFFFFu) != 0x7FFFFFFu && !a.accum) {
+    // the apron region facing each missing neighbour (apron 1), clipped to the slab.  The tile
+    // was zeroed, so with the boundary value 0 only the regions that some hit reached are reset.
+    uint32_t reset = ~nbmask & 0x7FFFFFFu & ~(1u << 13);
+    if (a.boundval == 0.0f) reset &= __reduce_or_sync(kFull, touched);
+    if (ap && reset && !a.accum) {
 #pragma unroll 1
         for (int k = 0; k < 27; k++) {
-            if (k == 13 || ((nbmask >> k) & 1u)) continue;
+            if (!((reset >> k) & 1u)) continue;
             const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
             const int xb = dx < 0 ? 0 : (dx > 0 ? P - 1 : 1), yb = dy < 0 ? 0 : (dy > 0 ? P - 1 : 1);
             const int bx = dx == 0 ? a.lb : 0, by = dy == 0 ? a.lb : 0;  // log2 of the region's x, y extents
@@ -637,10 +659,8 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
         if (lane == 0) {
             if (HAS_DEN) bulk_s2g(a.den + gofs, tile, (uint32_t)T::bytes(nvox));
             else bulk_s2g(a.vel + gofs, tile, (uint32_t)T::bytes(nvox));
-            bulk_commit();
-            bulk_wait_read_all();
+            bulk_commit();  // (its read of the tile is waited for before the tile's next write)
         }
-        __syncwarp();
     } else {
         const float4* tv = (const float4*)tile;
         float* dg = a.den + gofs;
