@@ -52,12 +52,13 @@ __global__ void __launch_bounds__(kBackThreads) k_splat_backward(BackArgs a)
 {
     const int lane = threadIdx.x & 31;
     const int P = a.P, P3 = P * P * P, ap = a.apron, b = a.brick, lb = a.lb;
-    // points one at a time from a counter: their supports differ in size
+    // points one at a time from a counter (their supports differ in size), the next one claimed
+    // while the current one runs
+    uint32_t in = lane == 0 ? atomicAdd(a.next, 1u) : 0u;
     for (;;) {
-        uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(a.next, 1u);
-        i = __shfl_sync(0xFFFFFFFFu, i, 0);
+        const uint32_t i = __shfl_sync(0xFFFFFFFFu, in, 0);
         if (i >= a.n) break;
+        if (lane == 0) in = atomicAdd(a.next, 1u);
         const uint32_t key = a.skeys[i] >> a.kshift;
         const uint32_t orig = a.svals[i];
         // the point takes part iff its own brick is in the lookup (as in the forward)

@@ -674,8 +674,18 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     }
 }
 
+// resident blocks per SM the registers are budgeted for: 8 for the trilinear splats without
+// velocity (a few bytes of spill; sparse batched clouds, 2 points a brick: 2.30 -> 2.02 ms on
+// 800k bricks, the memory latency of a brick's short candidate chain hidden by more warps), 6 for
+// the others, whose registers would spill tens of bytes at 8
+template <bool HAS_VEL, int MODE>
+constexpr int splat_min_blocks()
+{
+    return !HAS_VEL && MODE == GVX_SPLAT_TRILINEAR ? 8 : kSlabMinBlocks;
+}
+
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
-__global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(SplatArgs a)
+__global__ void __launch_bounds__(kSlabWarps * 32, splat_min_blocks<HAS_VEL, MODE>()) k_splat_slab(SplatArgs a)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -691,15 +701,16 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t units = a.nslots * (uint32_t)a.slabs;
-    // units one at a time from a counter (zeroed before the launch): bricks differ widely in cost,
-    // and the costly ones cluster (dense regions, the surface of an accumulating frame), so claims
-    // of several units, or a next unit claimed ahead, leave warps idle at the end (measured: the
+    // units one at a time from a counter (zeroed before the launch), the next one claimed while
+    // the current one runs (its atomic's latency hidden: the 4M frame's splat 3.10 -> 3.04 ms):
+    // bricks differ widely in cost and the costly ones cluster (dense regions, the surface of an
+    // accumulating frame), so claims of several units leave warps idle at the end (measured: the
     // batched clouds' splats 16.7 -> 23.2 ms with claims of 4)
+    uint32_t un = lane == 0 ? atomicAdd(a.next, 1u) : 0u;
     for (;;) {
-        uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(a.next, 1u);
-        u = __shfl_sync(kFull, u, 0);
+        const uint32_t u = __shfl_sync(kFull, un, 0);
         if (u >= units) break;
+        if (lane == 0) un = atomicAdd(a.next, 1u);  // the next unit, claimed while this one runs
         splat_unit<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(a, u, tile, &s_bar[wid], s_rs[wid], s_ro[wid], phase, lane);
     }
     if (!(HAS_DEN && HAS_VEL) && lane == 0) bulk_wait_all();
@@ -709,7 +720,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks) k_splat_slab(
 // k are [ustart[k], ustart[k+1]) of one global range, taken by the warps from
 // a counter; every grid has the same brick and tile shape (slab_layers, P).
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
-__global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
+__global__ void __launch_bounds__(kSlabWarps * 32, splat_min_blocks<HAS_VEL, MODE>())
     k_splat_batch(const SplatArgs* __restrict__ args, uint32_t* __restrict__ ustart, int ngrids)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
@@ -729,14 +740,15 @@ __global__ void __launch_bounds__(kSlabWarps * 32, kSlabMinBlocks)
     uint32_t phase = 0;
     const uint32_t total = s_us[ngrids];
     // units are taken one at a time from a counter (ustart[ngrids + 1], zeroed before every
-    // launch): a brick of a dense cloud costs many times a sparse one, and a fixed stride
-    // would leave the warps that drew the dense ones running alone at the end
+    // launch), the next claimed while the current runs: a brick of a dense cloud costs many times
+    // a sparse one, and a fixed stride would leave the warps that drew the dense ones running
+    // alone at the end
     uint32_t* next = ustart + ngrids + 1;
+    uint32_t un = lane == 0 ? atomicAdd(next, 1u) : 0u;
     for (;;) {
-        uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(next, 1u);
-        u = __shfl_sync(kFull, u, 0);
+        const uint32_t u = __shfl_sync(kFull, un, 0);
         if (u >= total) break;
+        if (lane == 0) un = atomicAdd(next, 1u);  // the next unit, claimed while this one runs
         int lo = 0, hi = ngrids - 1;  // the grid k with ustart[k] <= u < ustart[k+1]
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
