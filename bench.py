@@ -656,6 +656,49 @@ def run_batched(dev, iters=5):
                      "2 = graph replay; frame_first_ms: the unplanned, the first planned and the capturing frame"}
 
 
+def run_batched_frames(dev, frames=3, graph=False, clouds=64, cloud_max=2_000_000):
+    """The batched workload's clouds through gvx_batch_frame alone: one grid per cloud on its own
+    stream, `frames` frames (the first unplanned, then planned; with graph, captured from the
+    third on).  Wall clock per frame and the path each took (for launch lists: graph=False keeps
+    every planned build's launches visible to a profiler as separate launches)."""
+    import torch
+
+    import gvx
+    import workloads
+
+    cl = workloads.batched_clouds(count=clouds, seed=7, nmax=cloud_max)
+    stream = torch.cuda.Stream(device=dev)
+    grids, keep, own = [], [], []
+    with torch.cuda.stream(stream):
+        for p, w in cl:
+            g = gvx.Grid(dev.index)
+            g.configure(LOGDIM)
+            g.add_channel(0, gvx.T_FLOAT, 1)
+            pd, wd = torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev)
+            keep.append((pd, wd))
+            g.set_points(len(p), pd)
+            g.set_point_attribs(weight=wd)
+            own.append(torch.cuda.Stream(device=dev))
+            g.set_stream(own[-1].cuda_stream)
+            grids.append(g)
+        b = gvx.Batch(dev.index)
+        b.set_stream(stream.cuda_stream)
+        b.set_grids(grids)
+        out = []
+        for f in range(frames):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.frame(1.0, gvx.SPLAT_TRILINEAR, 1.0, graph=graph)
+            torch.cuda.synchronize()
+            out.append({"ms": round((time.perf_counter() - t0) * 1e3, 3), "path": list(b.frame_path())})
+        bricks = sum(g.info()["used_leaves"] for g in grids)
+        b.close()
+    for g in grids:
+        g.close()
+    return {"workload": "%d batched clouds (N_i <= %d) through gvx_batch_frame" % (clouds, cloud_max),
+            "graph": graph, "points": int(sum(len(p) for p, _ in cl)), "active_bricks": int(bricks), "frames": out}
+
+
 def run_scatter_frame(dev, frames=3):
     """libgvx on the work of the reference arm's `reference_cuda` frame: the same 4M SPH frames
     (advected 1..3), full RebuildTopology (radius 2), UpdateAtlas, ClearChannel, InsertPoints +
@@ -953,16 +996,20 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the differentiable, batched, fusion and point-cloud workloads")
-    ap.add_argument("--extra", choices=["differentiable", "batched", "fusion", "point_cloud", "scatter_frame"],
+    ap.add_argument("--clouds", type=int, default=64, help="batched_frames: clouds (profiling a smaller case)")
+    ap.add_argument("--cloud-max", type=int, default=2_000_000, help="batched_frames: largest cloud's points")
+    ap.add_argument("--extra", choices=["differentiable", "batched", "batched_frames", "fusion", "point_cloud",
+                                        "scatter_frame"],
                     help="run only this workload and print its JSON (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.extra:
         import torch
 
-        fn = {"differentiable": run_differentiable, "batched": run_batched, "fusion": run_fusion,
-              "point_cloud": run_point_cloud, "scatter_frame": run_scatter_frame}[args.extra]
-        print(json.dumps(fn(torch.device("cuda", 0))))
+        fn = {"differentiable": run_differentiable, "batched": run_batched, "batched_frames": run_batched_frames,
+              "fusion": run_fusion, "point_cloud": run_point_cloud, "scatter_frame": run_scatter_frame}[args.extra]
+        kw = {"clouds": args.clouds, "cloud_max": args.cloud_max} if args.extra == "batched_frames" else {}
+        print(json.dumps(fn(torch.device("cuda", 0), **kw)))
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
