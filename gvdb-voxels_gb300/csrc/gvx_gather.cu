@@ -210,11 +210,16 @@ __device__ __forceinline__ uint32_t f2u_sat(float v)
 // of INT2CLR(c) / |p - v| from 0 (uninitialised in the reference) written as
 // particles.cuh's CLR2INT (components * 255 added, carries included).  Every
 // float step is rounded on its own, as the oracle restates them.
-template <int VPL>
-__global__ void k_gather_fp16(GatherQArgs a)
+// SHARE: what a lane's VPL voxels have in common (voxel v + 32 q): 2 = x and y (sc^2 divides 32),
+// 1 = x (sc divides 32), 0 = nothing
+template <int VPL, int SHARE>
+__global__ void __launch_bounds__(256) k_gather_fp16(GatherQArgs a)
 {
     const int lane = threadIdx.x & 31;
     const int sc = a.sc, nv = sc * sc * sc;
+    // the decoded entries of the current 32, read back by every lane (broadcast loads)
+    __shared__ float4 s_ent[8][32];
+    float4* ent = s_ent[threadIdx.x >> 5];
     // subcells from a counter (WarpUnits): their lists differ widely in length
     WarpUnits wu(a.next, lane);
     uint32_t s;
@@ -252,14 +257,31 @@ __global__ void k_gather_fp16(GatherQArgs a)
                     mine = make_float4(p[0], p[1], p[2], __uint_as_float(a.clr_out ? a.qclr[j0 + lane] : 0u));
                 }
                 const int cnt = (int)min(32u, je - j0);
+                __syncwarp();  // the last chunk's reads are done
+                ent[lane] = mine;
+                __syncwarp();
                 for (int e = 0; e < cnt; e++) {
-                const float p[3] = {__shfl_sync(0xFFFFFFFFu, mine.x, e), __shfl_sync(0xFFFFFFFFu, mine.y, e),
-                                    __shfl_sync(0xFFFFFFFFu, mine.z, e)};
-                const uint32_t cu = __float_as_uint(__shfl_sync(0xFFFFFFFFu, mine.w, e));
+                const float4 pe = ent[e];
+                const float p[3] = {pe.x, pe.y, pe.z};
+                const uint32_t cu = __float_as_uint(pe.w);
+                // dx^2 (+ dy^2) once per entry where the lane's voxels share them; the squared
+                // distance is summed in the same order either way
+                const float dx0 = __fsub_rn(p[0], wx[0]), dx20 = __fmul_rn(dx0, dx0);
+                const float dy0 = __fsub_rn(p[1], wy[0]), dxy0 = __fadd_rn(dx20, __fmul_rn(dy0, dy0));
 #pragma unroll
                 for (int q = 0; q < VPL; q++) {
-                    const float dx = __fsub_rn(p[0], wx[q]), dy = __fsub_rn(p[1], wy[q]), dz = __fsub_rn(p[2], wz[q]);
-                    const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    float dxy = dxy0;
+                    if (q > 0 && SHARE < 2) {
+                        float dx2 = dx20;
+                        if (SHARE < 1) {
+                            const float dx = __fsub_rn(p[0], wx[q]);
+                            dx2 = __fmul_rn(dx, dx);
+                        }
+                        const float dy = __fsub_rn(p[1], wy[q]);
+                        dxy = __fadd_rn(dx2, __fmul_rn(dy, dy));
+                    }
+                    const float dz = __fsub_rn(p[2], wz[q]);
+                    const float s2 = __fadd_rn(dxy, __fmul_rn(dz, dz));
                     m2[q] = fminf(m2[q], s2);
                     if (a.clr_out) {
                         const float c = __fsqrt_rn(s2);
@@ -575,9 +597,11 @@ gvx_status gvx_gather_levelset_fp16(gvx_grid* g, int subcell, int n, float radiu
     a.next = g->d_next.as<uint32_t>();
     const unsigned blocks = std::min<unsigned>(blocks_for((uint64_t)a.nsub * 32u, 256), 152u * 16u);
     if (subcell * subcell * subcell <= 64)
-        k_gather_fp16<2><<<blocks, 256, 0, g->stream>>>(a);
+        k_gather_fp16<2, 2><<<blocks, 256, 0, g->stream>>>(a);  // sc <= 4: sc^2 divides 32
+    else if (32 % subcell == 0)
+        k_gather_fp16<8, 1><<<blocks, 256, 0, g->stream>>>(a);
     else
-        k_gather_fp16<8><<<blocks, 256, 0, g->stream>>>(a);
+        k_gather_fp16<8, 0><<<blocks, 256, 0, g->stream>>>(a);
     g->launches++;
     GVX_CK(cudaGetLastError());
     apron_invalidate(g->ch[cl]);
