@@ -396,15 +396,22 @@ __device__ __forceinline__ uint32_t pfx_value(uint32_t v)
     return POPC ? (uint32_t)__popc(v) : v;
 }
 
+// per block of kPfxChunk words: the sum (all loads issued before any add: the block's chunk is
+// one round trip, not kPfxPerThread)
 template <bool POPC>
-__global__ void k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words, uint32_t* block_sums)
+__global__ void __launch_bounds__(kPfxThreads) k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words,
+                                                            uint32_t* block_sums)
 {
-    const uint32_t base = blockIdx.x * kPfxChunk;
-    uint32_t s = 0u;
-    for (uint32_t i = threadIdx.x; i < kPfxChunk; i += kPfxThreads) {
-        const uint32_t w = base + i;
-        if (w < words) s += pfx_value<POPC>(bits[w]);
+    const uint32_t base = blockIdx.x * kPfxChunk + threadIdx.x;
+    uint32_t v[kPfxPerThread];
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) {
+        const uint32_t w = base + (uint32_t)k * kPfxThreads;
+        v[k] = w < words ? bits[w] : 0u;
     }
+    uint32_t s = 0u;
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) s += pfx_value<POPC>(v[k]);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
     __shared__ uint32_t ws[kPfxThreads / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -416,12 +423,24 @@ __global__ void k_pfx_reduce(const uint32_t* __restrict__ bits, uint32_t words, 
     }
 }
 
+// the block's chunk in and out through shared memory (coalesced global loads and stores; index i
+// of the chunk at i + i/32, so that a thread's kPfxPerThread consecutive values and the warps'
+// strided rows are both free of bank conflicts), each thread scanning kPfxPerThread consecutive
+// values after the block offset from the earlier blocks' sums
 template <bool POPC>
-__global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words,
-                            const uint32_t* __restrict__ block_sums, uint32_t* prefix, uint32_t* total)
+__global__ void __launch_bounds__(kPfxThreads) k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words,
+                                                           const uint32_t* __restrict__ block_sums, uint32_t* prefix,
+                                                           uint32_t* total)
 {
+    __shared__ uint32_t s_v[kPfxChunk + kPfxChunk / 32];
     __shared__ uint32_t s_w[kPfxThreads / 32];
     __shared__ uint32_t s_off;
+    const uint32_t cbase = blockIdx.x * kPfxChunk;
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) {
+        const uint32_t i = (uint32_t)k * kPfxThreads + threadIdx.x, w = cbase + i;
+        s_v[i + (i >> 5)] = w < words ? pfx_value<POPC>(bits[w]) : 0u;
+    }
     {
         uint32_t o = 0u;
         for (uint32_t i = threadIdx.x; i < blockIdx.x; i += kPfxThreads) o += block_sums[i];
@@ -437,13 +456,12 @@ __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words,
         __syncthreads();
     }
     const uint32_t block_off = s_off;
-    const uint32_t base = blockIdx.x * kPfxChunk + threadIdx.x * kPfxPerThread;
     uint32_t cnt[kPfxPerThread];
     uint32_t s = 0u;
 #pragma unroll
     for (int k = 0; k < kPfxPerThread; k++) {
-        const uint32_t w = base + k;
-        cnt[k] = w < words ? pfx_value<POPC>(bits[w]) : 0u;
+        const uint32_t i = threadIdx.x * kPfxPerThread + k;
+        cnt[k] = s_v[i + (i >> 5)];
         s += cnt[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -459,9 +477,15 @@ __global__ void k_pfx_apply(const uint32_t* __restrict__ bits, uint32_t words,
     for (int k = 0; k < warp; k++) run += s_w[k];
 #pragma unroll
     for (int k = 0; k < kPfxPerThread; k++) {
-        const uint32_t w = base + k;
-        if (w < words) prefix[w] = run;
+        const uint32_t i = threadIdx.x * kPfxPerThread + k;
+        s_v[i + (i >> 5)] = run;
         run += cnt[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPfxPerThread; k++) {
+        const uint32_t i = (uint32_t)k * kPfxThreads + threadIdx.x, w = cbase + i;
+        if (w < words) prefix[w] = s_v[i + (i >> 5)];
     }
 }
 
