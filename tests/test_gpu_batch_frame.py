@@ -148,3 +148,93 @@ def test_cloud_leaving_its_plan_is_built_again(gvx_mod):
     b.close()
     for g in grids:
         g.close()
+
+
+@pytest.mark.parametrize("vel", [False, True])
+def test_replayed_frames_follow_moving_points(gvx_mod, vel):
+    """points jittered in place every frame (the plans hold, the graph replays): every frame's
+    pools, atlas map and bricks are those of one-by-one builds of that frame's points -- a replay
+    recomputes everything from the points it reads"""
+    torch = pytest.importorskip("torch")
+    cl = clouds(5, 17)
+    rng = np.random.default_rng(3)
+    mode = gvx_mod.SPLAT_CUBIC if vel else gvx_mod.SPLAT_TRILINEAR
+    radius = 2.0 if vel else 1.0
+    cv = 1 if vel else -1
+    grids, keep, vels = [], [], []
+    for p, w in cl:
+        g = gvx_mod.Grid(0)
+        g.configure(LOGDIM)
+        g.add_channel(0, gvx_mod.T_FLOAT, 1)
+        if vel:
+            g.add_channel(1, gvx_mod.T_FLOAT3, 1)
+        v = rng.normal(0, 1, p.shape).astype(np.float32)
+        pd, wd, vd = torch.from_numpy(p).cuda(), torch.from_numpy(w).cuda(), torch.from_numpy(v).cuda()
+        keep.append((pd, wd, vd))
+        vels.append(v)
+        g.set_points(len(p), pd, vel=vd if vel else None)
+        g.set_point_attribs(weight=wd)
+        grids.append(g)
+    b = gvx_mod.Batch(0)
+    b.set_grids(grids)
+    pts = [p.copy() for p, _ in cl]
+    paths = []
+    for f in range(5):
+        for k in range(len(pts)):
+            pts[k] = (pts[k] + rng.normal(0, 0.4, pts[k].shape)).astype(np.float32)
+            keep[k][0].copy_(torch.from_numpy(pts[k]))
+        torch.cuda.synchronize()
+        b.frame(1.0, mode, radius, chan_vel=cv)
+        paths.append(b.frame_path())
+        for g, p, (_, w), v in zip(grids, pts, cl, vels):
+            r = gvx_mod.Grid(0)
+            r.configure(LOGDIM)
+            r.add_channel(0, gvx_mod.T_FLOAT, 1)
+            if vel:
+                r.add_channel(1, gvx_mod.T_FLOAT3, 1)
+            r.commit_points_host(p, vel=v if vel else None, weight=w)
+            r.rebuild_topology(len(p), 1.0, mode=gvx_mod.TOPO_FULL)
+            r.update_atlas()
+            r.insert_points(len(p))
+            r.splat(mode, len(p), radius, chan_density=0, chan_vel=cv)
+            assert_same(snapshot(g), snapshot(r))
+            if vel:
+                u = g.info()["used_leaves"]
+                assert np.array_equal(g.read_channel(1)[:u], r.read_channel(1)[:u])
+            r.close()
+    # unplanned, planned, then replays (a plan outgrown by the jitter would rebuild its grid and
+    # the frame after it would run planned again)
+    assert paths[0] == (0, 0) and paths[1][0] == 1 and sum(p[0] == 2 for p in paths[2:]) >= 2
+    b.close()
+    for g in grids:
+        g.close()
+
+
+def test_bad_point_in_a_planned_frame(gvx_mod):
+    """a NaN position written in place into a replayed frame's points: the frame reports
+    GVX_ERR_INVALID_ARG (the device error word, as an unplanned build reports it), and once the
+    point is fixed the next frame builds again from scratch and matches one-by-one builds"""
+    torch = pytest.importorskip("torch")
+    cl = clouds(3, 21)
+    grids, keep = frame_grids(gvx_mod, torch, cl)
+    b = gvx_mod.Batch(0)
+    b.set_grids(grids)
+    tri = gvx_mod.SPLAT_TRILINEAR
+    for _ in range(3):
+        b.frame(1.0, tri, 1.0)
+    assert b.frame_path() == (2, 0)
+    saved = keep[1][0][7].clone()
+    keep[1][0][7, 0] = float("nan")
+    torch.cuda.synchronize()
+    with pytest.raises(gvx_mod.GvxError) as e:
+        b.frame(1.0, tri, 1.0)
+    assert e.value.status == 1 and "grid 1" in str(e.value)  # GVX_ERR_INVALID_ARG
+    keep[1][0][7] = saved
+    torch.cuda.synchronize()
+    b.frame(1.0, tri, 1.0)
+    assert b.frame_path()[0] == 0
+    for g, (p, w) in zip(grids, cl):
+        assert_same(snapshot(g), reference(gvx_mod, p, w, 1.0, tri, 1.0))
+    b.close()
+    for g in grids:
+        g.close()
