@@ -115,7 +115,12 @@ struct SplatArgs {
     float radius;
     float* den;          // channel data (slot-major, P^3 per slot) or nullptr
     float4* vel;         // or nullptr
-    int slabs, slab_layers;  // z-slabs per padded brick, layers per slab
+    int slabs, slab_layers;  // z-slabs per brick, layers per slab
+    // push (apron 1, not accumulating): a tile covers the interior rows and layers only (x with
+    // its apron), and the slab's boundary rows go to the neighbours' y/z aprons; else the whole
+    // padded brick.  tile_rows: rows of a tile layer (the brick, or the padded brick)
+    bool push;
+    int tile_rows;
     int lb;              // log2(brick)
     int reach;           // voxels a point's footprint reaches beyond its own voxel (neighbour pruning)
     const unsigned int* rmax;  // per-point radii: float bits of the largest (bounds `reach` on the device)
@@ -177,9 +182,10 @@ struct Tile {
 // for n = 1).
 template <bool HAS_DEN, bool HAS_VEL, int MODE, bool PPR, bool SMALL>
 __device__ __forceinline__ void deal_cells(unsigned char* tile, const float4 p, const float4 uv, uint32_t box0,
-                                           const uint32_t box1, int ncell, const int P, const int Ox, const int Oy,
-                                           const int Zlo, const float R0, const float h0, const float inv_h0,
-                                           const float norm0, const float r2h0, const float r2l0, const int lane)
+                                           const uint32_t box1, int ncell, const int P, const int TY, const int yoff,
+                                           const int Ox, const int Oy, const int Zlo, const float R0,
+                                           const float h0, const float inv_h0, const float norm0, const float r2h0,
+                                           const float r2l0, const int lane)
 {
     using T = Tile<HAS_DEN, HAS_VEL>;
     constexpr bool CUBIC = MODE == GVX_SPLAT_CUBIC;
@@ -284,7 +290,7 @@ __device__ __forceinline__ void deal_cells(unsigned char* tile, const float4 p, 
         // the lane's voxels lx .. min(lx + 3, xh) of row (ly, lz): values, and a bit per voxel touched
         float w[4] = {0.f, 0.f, 0.f, 0.f};
         uint32_t vm = 0u;
-        const int t0 = (lz * P + ly) * P + lx;
+        const int t0 = (lz * TY + (ly - yoff)) * P + lx;  // (the tile's rows start at padded y = yoff)
         if (act) {
             if (!CUBIC) {
                 const float fx0 = floorf(px), fy0 = floorf(py), fz0 = floorf(pz);
@@ -360,6 +366,130 @@ __device__ __forceinline__ void deal_cells(unsigned char* tile, const float4 p, 
     }
 }
 
+// one voxel out: the tile's (density in .w with velocity), or the boundary value
+template <bool HAS_DEN, bool HAS_VEL>
+__device__ __forceinline__ void put_voxel(const SplatArgs& a, const unsigned char* tile, int ti, size_t gi)
+{
+    if (HAS_VEL) {
+        const float4 o = ((const float4*)tile)[ti];
+        if (HAS_DEN) {
+            a.den[gi] = o.w;
+            a.vel[gi] = make_float4(o.x, o.y, o.z, 0.0f);
+        } else {
+            a.vel[gi] = o;
+        }
+    } else {
+        a.den[gi] = ((const float*)tile)[ti];
+    }
+}
+template <bool HAS_DEN, bool HAS_VEL>
+__device__ __forceinline__ void put_bound(const SplatArgs& a, size_t gi)
+{
+    const float v = a.boundval;
+    if (HAS_DEN) a.den[gi] = v;
+    if (HAS_VEL) a.vel[gi] = make_float4(v, v, v, HAS_DEN ? 0.0f : v);
+}
+
+// The slab of a push tile to HBM (apron 1).  The tile holds the brick's interior rows and
+// layers of the slab, x with its apron (computed from the points, exact copies of the
+// x-neighbours' interiors by the canonical sums).  Every voxel of the padded atlas has one
+// writer, the brick whose interior holds it:
+//  - the tile's rows go to the brick's own slot;
+//  - its boundary rows go to the y/z aprons of the neighbours B + (0, dy, dz) that exist,
+//    whole rows, x aprons included (the receiver's apron row in direction -(dy, dz) holds,
+//    x apart, this brick's voxels, and at its two ends the voxels of B -/+ x, which this
+//    brick's x apron holds);
+//  - where that neighbour B + (0, dy, dz) is missing, the end voxels of its would-be row go
+//    from the bricks B + (-1|+1, dy, dz) that exist, one voxel a row (this brick's first or
+//    last interior column), to B + (+1|-1, ...)'s row ends: with receiver offset (dx, dy, dz),
+//    dx != 0, this brick sends when B + (dx, 0, 0) is missing;
+//  - the brick's own y/z apron rows facing a missing B + (0, dy, dz) take the boundary value
+//    (their end voxels too where B + (-1|+1, dy, dz) is missing as well).
+// Rows of a receiver direction: dy = -1: the first interior row (to the receiver's last padded
+// row), +1: the last (to its row 0), 0: every row; likewise in z, where only the slab holding
+// the first (last) interior layer sends.  nbs: lane r < 27 holds the slot of neighbour r,
+// r = (dx+1)*9 + (dy+1)*3 + (dz+1).
+template <bool HAS_DEN, bool HAS_VEL>
+__device__ __forceinline__ void push_out(const SplatArgs& a, const unsigned char* tile, uint32_t s, int z0, int nl,
+                                         int nbs, int lane)
+{
+    const int P = a.P, P3 = P * P * P, b = a.brick, lb = a.lb, TY = b;
+    const uint32_t mP = 0xFFFFFFFFu / (uint32_t)P + 1u;  // e / P == umulhi(e, mP) for e < 2^16
+    // the brick's own rows: a tile layer is contiguous in the slot from padded (y 1, z)
+    const size_t own = (size_t)s * P3;
+    const int lay = TY * P, nvox = nl * lay;
+    const uint32_t mL = 0xFFFFFFFFu / (uint32_t)lay + 1u;
+    for (int e = lane; e < nvox; e += 32) {
+        const int lz = (int)__umulhi((uint32_t)e, mL);
+        put_voxel<HAS_DEN, HAS_VEL>(a, tile, e, own + (uint32_t)((z0 + lz) * P * P + P + (e - lz * lay)));
+    }
+    const bool xm = __shfl_sync(kFull, nbs, 4) >= 0, xp = __shfl_sync(kFull, nbs, 22) >= 0;  // B -/+ x
+#pragma unroll 1
+    for (int q = 0; q < 9; q++) {
+        const int dy = q / 3 - 1, dz = q % 3 - 1;
+        if (dy == 0 && dz == 0) continue;
+        // the sending rows (ly in [ly0, ly0 + nry), lz in [lz0, lz0 + nrz)) of direction (., dy, dz)
+        int ly0 = 0, nry = TY, lz0 = 0, nrz = nl;
+        if (dy != 0) {
+            ly0 = dy < 0 ? 0 : TY - 1;
+            nry = 1;
+        }
+        if (dz != 0) {
+            lz0 = dz < 0 ? 1 - z0 : P - 2 - z0;  // the first (last) interior layer
+            if (lz0 < 0 || lz0 >= nl) continue;
+            nrz = 1;
+        }
+        const int nrows = nry * nrz;
+        const int d0 = 9 + (dy + 1) * 3 + (dz + 1);  // (0, dy, dz); (-1|+1, dy, dz) at d0 -/+ 9
+        const int r0 = __shfl_sync(kFull, nbs, d0);
+        const int rm = __shfl_sync(kFull, nbs, d0 - 9), rp = __shfl_sync(kFull, nbs, d0 + 9);
+        // row r of the direction: tile row, and its padded (y, z) in a receiver (-1 -> P-1, +1 -> 0)
+        auto row = [&](int r, int& ti, int& yr, int& zr) {
+            const int ly = ly0 + (nry == 1 ? 0 : (r & (TY - 1))), lz = lz0 + (nry == 1 ? r : (r >> lb));
+            ti = (lz * TY + ly) * P;
+            yr = dy < 0 ? P - 1 : (dy > 0 ? 0 : ly + 1);
+            zr = dz < 0 ? P - 1 : (dz > 0 ? 0 : z0 + lz);
+        };
+        if (r0 >= 0) {  // whole rows to B + (0, dy, dz)
+            const size_t rb = (size_t)r0 * P3;
+            for (int e = lane; e < nrows * P; e += 32) {
+                const int r = (int)__umulhi((uint32_t)e, mP), x = e - r * P;
+                int ti, yr, zr;
+                row(r, ti, yr, zr);
+                put_voxel<HAS_DEN, HAS_VEL>(a, tile, ti + x, rb + (uint32_t)((zr * P + yr) * P + x));
+            }
+        } else if (!a.accum) {  // the brick's own apron rows facing the missing B + (0, dy, dz)
+            // (their end voxels too where B -/+ x + (0, dy, dz) is missing as well)
+            const bool lo = rm < 0, hi = rp < 0;
+            for (int e = lane; e < nrows * P; e += 32) {
+                const int r = (int)__umulhi((uint32_t)e, mP), x = e - r * P;
+                if ((x == 0 && !lo) || (x == P - 1 && !hi)) continue;
+                int ti, yr, zr;
+                row(r, ti, yr, zr);
+                const int yB = dy == 0 ? yr : P - 1 - yr, zB = dz == 0 ? zr : P - 1 - zr;  // the own side
+                put_bound<HAS_DEN, HAS_VEL>(a, own + (uint32_t)((zB * P + yB) * P + x));
+            }
+        }
+        // one voxel a row to B -/+ x + (0, dy, dz), whose row source B -/+ x is missing
+        if (!xm && rm >= 0) {
+            const size_t rb = (size_t)rm * P3;
+            for (int r = lane; r < nrows; r += 32) {
+                int ti, yr, zr;
+                row(r, ti, yr, zr);
+                put_voxel<HAS_DEN, HAS_VEL>(a, tile, ti + 1, rb + (uint32_t)((zr * P + yr) * P + P - 1));
+            }
+        }
+        if (!xp && rp >= 0) {
+            const size_t rb = (size_t)rp * P3;
+            for (int r = lane; r < nrows; r += 32) {
+                int ti, yr, zr;
+                row(r, ti, yr, zr);
+                put_voxel<HAS_DEN, HAS_VEL>(a, tile, ti + P - 2, rb + (uint32_t)((zr * P + yr) * P));
+            }
+        }
+    }
+}
+
 // One warp per (brick, z-slab): the padded brick's layers are split into
 // slabs of a.slab_layers layers, each with its own shared tile, so a warp's
 // tile is a fraction of the brick and more warps stay resident.  Every slab
@@ -380,11 +510,15 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     const float norm0 = kInvPi * inv_h0 * inv_h0 * inv_h0, r2h0 = R0 * R0, r2l0 = fmaf(R0, R0, -r2h0);
     const int P = a.P, P2 = P * P, P3 = P2 * P, ap = a.apron, b = a.brick;
     const int L = a.slab_layers, S = a.slabs;
+    // the tile: rows [yoff, yoff + TY) of layers [z0, z0 + nl) of the padded brick, x whole
+    constexpr bool PUSHABLE = HAS_DEN && HAS_VEL;  // the host sets push for these kernels only
+    const bool push = PUSHABLE && a.push;
+    const int TY = push ? a.tile_rows : P, yoff = push ? ap : 0, zend = push ? P - ap : P;
     const uint32_t s = u / (uint32_t)S;
-    const int z0 = (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
-    const int nl = min(L, P - z0);
-    const int nvox = nl * P2;
-    const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel
+    const int z0 = yoff + (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
+    const int nl = min(L, zend - z0);
+    const int nvox = nl * TY * P;
+    const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel (no push)
     const int leaf = a.slot_leaf[s];
     const GvxNode* nd = a.nodes0 + leaf;
     const int Ox = nd->pos[0] - ap, Oy = nd->pos[1] - ap, Oz = nd->pos[2] - ap;  // padded origin
@@ -400,6 +534,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     // with per-point radii the reach is that of the largest radius (ceil R voxels, at most brick - 1)
     const int reach = PPR && a.rmax ? min(a.reach, (int)ceilf(__uint_as_float(*a.rmax))) : a.reach;
     bool has_nb = false;
+    int nbs = -1;        // lane r < 27: the atlas slot of neighbour r (-1: none)
     uint32_t need = 0u;  // octants to read
     int oc[9];           // first index of each octant, and the end of the brick's points
 #pragma unroll
@@ -408,7 +543,8 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
         const int dx = lane / 9 - 1, dy = (lane / 3) % 3 - 1, dz = lane % 3 - 1;
         const int nl_ = a.nbr[(size_t)leaf * 27 + (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
         if (nl_ >= 0) {
-            has_nb = a.leaf_slot[nl_] >= 0;
+            nbs = a.leaf_slot[nl_];
+            has_nb = nbs >= 0;
             const int hb = b >> 1;
             const int cx = nd->pos[0] + dx * b, cy = nd->pos[1] + dy * b, cz = nd->pos[2] + dz * b;
             uint32_t mx = 0u, my = 0u, mz = 0u;
@@ -416,7 +552,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             for (int h = 0; h < 2; h++) {
                 const int x0 = cx + h * hb, y0 = cy + h * hb, z0h = cz + h * hb;
                 mx |= (uint32_t)(x0 - reach <= Ox + P - 1 && x0 + hb - 1 + reach >= Ox) << h;
-                my |= (uint32_t)(y0 - reach <= Oy + P - 1 && y0 + hb - 1 + reach >= Oy) << h;
+                my |= (uint32_t)(y0 - reach <= Oy + yoff + TY - 1 && y0 + hb - 1 + reach >= Oy + yoff) << h;
                 mz |= (uint32_t)(z0h - reach <= Zhi && z0h + hb - 1 + reach >= Zlo) << h;
             }
 #pragma unroll
@@ -556,14 +692,15 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             if (!CUBIC) {
                 const int x0 = (int)floorf(p.x) - Ox, y0 = (int)floorf(p.y) - Oy, zb = (int)floorf(p.z) - Zlo;
                 xl = max(x0, 0), xh = min(x0 + 1, P - 1);
-                yl = max(y0, 0), yh = min(y0 + 1, P - 1);
+                yl = max(y0, yoff), yh = min(y0 + 1, yoff + TY - 1);
                 zl = max(zb, 0), zh = min(zb + 1, nl - 1);
             } else {
                 // voxels strictly inside (p - R, p + R) on every axis
                 const float R = PPR ? uv.w : R0;
                 if (PPR && R > a.max_radius) atomicOr(a.err, GVX_DERR_RADIUS);
                 xl = max((int)floorf(p.x - R) + 1 - Ox, 0), xh = min((int)ceilf(p.x + R) - 1 - Ox, P - 1);
-                yl = max((int)floorf(p.y - R) + 1 - Oy, 0), yh = min((int)ceilf(p.y + R) - 1 - Oy, P - 1);
+                yl = max((int)floorf(p.y - R) + 1 - Oy, yoff);
+                yh = min((int)ceilf(p.y + R) - 1 - Oy, yoff + TY - 1);
                 zl = max((int)floorf(p.z - R) + 1 - Zlo, 0), zh = min((int)ceilf(p.z + R) - 1 - Zlo, nl - 1);
             }
             if (xl <= xh && yl <= yh && zl <= zh) {
@@ -587,8 +724,8 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
         const uint32_t hm = __ballot_sync(kFull, ncell > 0);
         const int h = __popc(hm);
         if (done ? nb > 0 : nb + h > 32) {
-            deal_cells<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(tile, bp, buv, bb0, bb1, bnc, P, Ox, Oy, Zlo, R0, h0, inv_h0,
-                                                    norm0, r2h0, r2l0, lane);
+            deal_cells<HAS_DEN, HAS_VEL, MODE, PPR, SMALL>(tile, bp, buv, bb0, bb1, bnc, P, TY, yoff, Ox, Oy, Zlo, R0,
+                                                           h0, inv_h0, norm0, r2h0, r2l0, lane);
             bnc = 0;
             nb = 0;
         }
@@ -633,6 +770,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     // was zeroed, so with the boundary value 0 only the regions that some hit reached are reset.
     uint32_t reset = ~nbmask & 0x7FFFFFFu & ~(1u << 13);
     if (a.boundval == 0.0f) reset &= __reduce_or_sync(kFull, touched);
+    if (push) reset &= (1u << 4) | (1u << 22);  // the tile's only apron voxels: the two x faces
     if (ap && reset && !a.accum) {
 #pragma unroll 1
         for (int k = 0; k < 27; k++) {
@@ -646,14 +784,16 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
             for (int c = lane; c < cnt; c += 32) {
                 const int x = xb + (c & ((1 << bx) - 1)), y = yb + ((c >> bx) & ((1 << by) - 1));
                 const int z = zlo + (c >> (bx + by));
-                T::set(tile, ((z - z0) * P + y) * P + x, a.boundval);
+                T::set(tile, ((z - z0) * TY + (y - yoff)) * P + x, a.boundval);
             }
         }
         __syncwarp();
     }
 
     // ---- out to HBM
-    if (BULK) {
+    if (push) {
+        if (PUSHABLE) push_out<HAS_DEN, HAS_VEL>(a, tile, s, z0, nl, nbs, lane);
+    } else if (BULK) {
         fence_async_smem();
         __syncwarp();
         if (lane == 0) {
@@ -690,7 +830,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, splat_min_blocks<HAS_VEL, MOD
     using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char* tile = smem + (size_t)wid * T::bytes(a.slab_layers * a.P * a.P);
+    unsigned char* tile = smem + (size_t)wid * T::bytes(a.slab_layers * a.tile_rows * a.P);
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
     __shared__ int s_rs[kSlabWarps][kMaxRanges + 1];
     __shared__ int s_ro[kSlabWarps][kMaxRanges + 1];
@@ -726,7 +866,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, splat_min_blocks<HAS_VEL, MOD
     using T = Tile<HAS_DEN, HAS_VEL>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned char* tile = smem + (size_t)wid * T::bytes(args[0].slab_layers * args[0].P * args[0].P);
+    unsigned char* tile = smem + (size_t)wid * T::bytes(args[0].slab_layers * args[0].tile_rows * args[0].P);
     __shared__ __align__(8) uint64_t s_bar[kSlabWarps];
     __shared__ int s_rs[kSlabWarps][kMaxRanges + 1];
     __shared__ int s_ro[kSlabWarps][kMaxRanges + 1];
@@ -1005,17 +1145,41 @@ static void* splat_kernel(const SplatKind& k, bool batch)
                    : pick_kernel<false, true>(k, batch);
 }
 
-// the largest slab (in layers) whose tile fits the per-warp budget, at most `want`
-static int clamp_layers(int P, size_t eb, int want)
+// Tile geometry of a grid's splat: a push tile (apron 1, not accumulating) covers the interior
+// rows and layers of the padded brick, else the whole padded brick; `span` layers to cover,
+// `rows` rows a layer
+struct SlabShape {
+    bool push;
+    int span, rows;
+};
+static SlabShape slab_shape(const gvx_grid* g, int accum, bool dense, bool den_vel)
 {
-    const int fit = (int)(kSlabTileMax / ((size_t)P * P * eb));
-    return std::min(std::min(want, P), fit);
+    const bool push = g->apron == 1 && !accum && dense && den_vel;
+    return SlabShape{push, push ? g->brick : g->P, push ? g->brick : g->P};
+}
+
+// Points per active brick from which the push tile is used (and only by the splat of density
+// with velocity, the only kernels compiled with it: the others keep their registers): its
+// scattered apron stores cost a slab several hundred more instructions, which the
+// interior-only dealing repays on dense clouds (4M SPH frame, 14 a brick: 3.04 -> 2.95 ms)
+// and not on sparse ones (the batched clouds, 4.6 a brick: 15.3 -> 18.8 ms with it)
+constexpr uint64_t kPushPointsPerBrick = 8;
+static bool dense_cloud(uint64_t points, uint64_t bricks)
+{
+    return bricks > 0 && points >= kPushPointsPerBrick * bricks;
+}
+
+// the largest slab (in layers) whose tile fits the per-warp budget, at most `want`
+static int clamp_layers(const SlabShape& sh, int P, size_t eb, int want)
+{
+    const int fit = (int)(kSlabTileMax / ((size_t)sh.rows * P * eb));
+    return std::min(std::min(want, sh.span), fit);
 }
 
 // validation of one grid's splat and its kernel kind; *layers in: the wanted slab height (<= 0:
 // half the padded brick), out: clamped to the tile budget
-static gvx_status splat_check(gvx_grid* g, int mode, float radius, int chan_d, int chan_v, int* layers,
-                              SplatKind* kind)
+static gvx_status splat_check(gvx_grid* g, int mode, float radius, int chan_d, int chan_v, int accum,
+                              bool dense, int* layers, SplatKind* kind)
 {
     if (mode != GVX_SPLAT_TRILINEAR && mode != GVX_SPLAT_CUBIC) {
         gvx_set_error("Splat: unknown mode %d", mode);
@@ -1048,7 +1212,8 @@ static gvx_status splat_check(gvx_grid* g, int mode, float radius, int chan_d, i
         return GVX_ERR_UNSUPPORTED;
     }
     const int P = g->P;
-    *layers = clamp_layers(P, has_v ? 16 : 4, *layers > 0 ? *layers : (P + 1) / 2);
+    const SlabShape sh = slab_shape(g, accum, dense, has_d && has_v);
+    *layers = clamp_layers(sh, P, has_v ? 16 : 4, *layers > 0 ? *layers : (sh.span + 1) / 2);
     if (*layers < 1) {
         gvx_set_error("Splat: a %d^2 layer of the padded brick exceeds the shared tile budget", P);
         return GVX_ERR_UNSUPPORTED;
@@ -1062,8 +1227,8 @@ static gvx_status splat_check(gvx_grid* g, int mode, float radius, int chan_d, i
 }
 
 // the kernel arguments of one grid's splat over its current grouping and atlas
-static void splat_fill(gvx_grid* g, const SplatKind& k, float radius, int chan_d, int chan_v, int accum, int layers,
-                       SplatArgs* out)
+static void splat_fill(gvx_grid* g, const SplatKind& k, float radius, int chan_d, int chan_v, int accum, bool dense,
+                       int layers, SplatArgs* out)
 {
     const bool need_svel = k.has_v || k.ppr;
     const int P = g->P;
@@ -1085,8 +1250,11 @@ static void splat_fill(gvx_grid* g, const SplatKind& k, float radius, int chan_d
     a.radius = radius;
     a.den = k.has_d ? g->ch[chan_d].data.as<float>() : nullptr;
     a.vel = k.has_v ? g->ch[chan_v].data.as<float4>() : nullptr;
+    const SlabShape sh = slab_shape(g, accum, dense, k.has_d && k.has_v);
+    a.push = sh.push;
+    a.tile_rows = sh.rows;
     a.slab_layers = layers;
-    a.slabs = (P + layers - 1) / layers;
+    a.slabs = (sh.span + layers - 1) / layers;
     a.lb = 0;
     while ((1 << a.lb) < g->brick) a.lb++;
     a.max_radius = (float)(g->brick - 1);
@@ -1098,19 +1266,24 @@ static void splat_fill(gvx_grid* g, const SplatKind& k, float radius, int chan_d
 }
 
 // validation, InsertPoints grouping and the kernel arguments of one grid's splat;
-// layers <= 0 picks the default slab height (half the padded brick)
+// layers <= 0 picks the default slab height (half the span); dense < 0: the tile shape from the
+// grid's own points per brick, else as given (a batch decides for all its grids)
 static gvx_status splat_prepare(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d,
-                                int chan_v, int accum, int layers, SplatArgs* out, SplatKind* kind)
+                                int chan_v, int accum, int layers, int dense, SplatArgs* out, SplatKind* kind)
 {
     gvx_status rc = check_splat_state(g, "Splat");
     if (rc) return rc;
-    rc = splat_check(g, mode, radius, chan_d, chan_v, &layers, kind);
+    const bool dn = dense < 0 ? dense_cloud((uint64_t)n, (uint64_t)g->atlas_used) : dense != 0;
+    rc = splat_check(g, mode, radius, chan_d, chan_v, accum, dn, &layers, kind);
     if (rc) return rc;
     rc = gvx_prepare_points(g, n, trans, kind->has_v || kind->ppr);
     if (rc) return rc;
-    splat_fill(g, *kind, radius, chan_d, chan_v, accum, layers, out);
+    splat_fill(g, *kind, radius, chan_d, chan_v, accum, dn, layers, out);
     return GVX_OK;
 }
+
+// one tile shape for the grids of a batch: from their points and bricks together
+static bool batch_dense(const gvx_batch* b);
 
 // apron state after the splat: exact copies with boundary value 0, unless an
 // accumulating splat started from an apron that was not a valid copy
@@ -1133,7 +1306,7 @@ static void splat_finish(gvx_grid* g, int chan_d, int chan_v, int accum)
 
 static size_t splat_smem(const SplatArgs& a, const SplatKind& k)
 {
-    return (size_t)a.slab_layers * a.P * a.P * (k.has_v ? 16 : 4) * kSlabWarps;
+    return (size_t)a.slab_layers * a.tile_rows * a.P * (k.has_v ? 16 : 4) * kSlabWarps;
 }
 
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
@@ -1141,7 +1314,7 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
 {
     SplatArgs a;
     SplatKind kind;
-    gvx_status rc = splat_prepare(g, mode, n, radius, trans, chan_d, chan_v, accum, 0, &a, &kind);
+    gvx_status rc = splat_prepare(g, mode, n, radius, trans, chan_d, chan_v, accum, 0, -1, &a, &kind);
     if (rc) return rc;
     if (a.nslots) {
         const size_t smem = splat_smem(a, kind);
@@ -1207,6 +1380,16 @@ struct gvx_batch {
     int f_path = 0, f_void = 0;          // how the last frame ran, its grids built again without a plan
 };
 
+static bool batch_dense(const gvx_batch* b)
+{
+    uint64_t pts = 0, bricks = 0;
+    for (const gvx_grid* g : b->grids) {
+        pts += (uint64_t)(g->group_valid ? g->group_n : g->pts.n);
+        bricks += (uint64_t)g->atlas_used;
+    }
+    return dense_cloud(pts, bricks);
+}
+
 static void frame_drop_graph(gvx_batch* b)
 {
     if (b->f_exec) cudaGraphExecDestroy(b->f_exec);
@@ -1231,8 +1414,8 @@ static std::string tune_key(int device, const SplatArgs& a, const SplatKind& k)
     memset(&prop, 0, sizeof(prop));
     cudaGetDeviceProperties(&prop, device);
     char buf[512];
-    snprintf(buf, sizeof(buf), "%s|%d|P%d|m%d|d%d|v%d|r%d|s%d", prop.name, device, a.P, k.mode, (int)k.has_d,
-             (int)k.has_v, (int)k.ppr, (int)k.small);
+    snprintf(buf, sizeof(buf), "%s|%d|P%d|p%d|m%d|d%d|v%d|r%d|s%d", prop.name, device, a.P, (int)a.push, k.mode,
+             (int)k.has_d, (int)k.has_v, (int)k.ppr, (int)k.small);
     return buf;
 }
 
@@ -1257,16 +1440,18 @@ static gvx_status batch_tables(gvx_batch* b, int mode, float radius, int chan_d,
     args.resize(b->grids.size());
     ustart.assign(b->grids.size() + 1, 0u);
     uint64_t tot = 0;
+    const int dense = batch_dense(b) ? 1 : 0;
     for (size_t i = 0; i < b->grids.size(); i++) {
         gvx_grid* g = b->grids[i];
         const int n = g->group_valid ? g->group_n : g->pts.n;
         const float* t = g->group_valid ? g->group_trans : nullptr;
         SplatKind k;
-        gvx_status rc = splat_prepare(g, mode, n, radius, t, chan_d, chan_v, accum, layers, &args[i], &k);
+        gvx_status rc = splat_prepare(g, mode, n, radius, t, chan_d, chan_v, accum, layers, dense, &args[i], &k);
         if (rc) return rc;
         if (i == 0) {
             kind = k;
-        } else if (!(k == kind) || args[i].P != args[0].P || args[i].slab_layers != args[0].slab_layers) {
+        } else if (!(k == kind) || args[i].P != args[0].P || args[i].slab_layers != args[0].slab_layers ||
+                   args[i].push != args[0].push) {
             gvx_set_error("BatchSplat: grid %zu differs from grid 0 in brick shape, channels or radius kind", i);
             return GVX_ERR_INVALID_ARG;
         }
@@ -1306,8 +1491,9 @@ static gvx_status batch_max_blocks(gvx_batch* b, const SplatKind& k, const Splat
 // keeps the fastest; each candidate: one warm-up, then the mean of two timed runs
 static gvx_status batch_tune(gvx_batch* b, int mode, float radius, int chan_d, int chan_v, BatchTuning* best)
 {
-    const int P = b->grids[0]->P;
-    const int cand_layers[3] = {(P + 1) / 2, P, (P + 2) / 3};
+    // (the tuning splat does not accumulate)
+    const int span = slab_shape(b->grids[0], 0, batch_dense(b), chan_d >= 0 && chan_v >= 0).span;
+    const int cand_layers[3] = {(span + 1) / 2, span, (span + 2) / 3};
     cudaEvent_t e0, e1;
     GVX_CK(cudaEventCreate(&e0));
     GVX_CK(cudaEventCreate(&e1));
@@ -1437,7 +1623,7 @@ static gvx_status frame_upload(gvx_batch* b, const SplatKind& kind, float radius
     std::vector<const uint32_t*> cnt(ng);
     std::vector<uint32_t> caps(ng);
     for (size_t i = 0; i < ng; i++) {
-        splat_fill(b->grids[i], kind, radius, chan_d, chan_v, 0, layers, &args[i]);
+        splat_fill(b->grids[i], kind, radius, chan_d, chan_v, 0, batch_dense(b), layers, &args[i]);
         cnt[i] = gvx_topo_plan_slots(b->grids[i], &caps[i]);
     }
     GVX_CK(cudaMemcpyAsync(b->f_args.p, args.data(), ng * sizeof(SplatArgs), cudaMemcpyHostToDevice, b->stream));
@@ -1476,7 +1662,8 @@ static std::vector<uint64_t> frame_key(gvx_batch* b, float topo_radius, int mode
         return (uint64_t)u;
     };
     std::vector<uint64_t> k = {gvx_alloc_epoch(), fb(topo_radius), (uint64_t)mode, fb(radius), (uint64_t)chan_d,
-                               (uint64_t)chan_v, (uint64_t)layers, (uint64_t)blocks, (uint64_t)(uintptr_t)b->stream};
+                               (uint64_t)chan_v, (uint64_t)layers, (uint64_t)blocks, (uint64_t)(uintptr_t)b->stream,
+                               (uint64_t)batch_dense(b)};
     for (gvx_grid* g : b->grids) {
         const GvxPoints& p = g->pts;
         for (uint64_t v : {gvx_topo_plan_id(g), (uint64_t)(uintptr_t)g->stream, (uint64_t)(uintptr_t)p.pos,
@@ -1863,7 +2050,7 @@ gvx_status gvx_batch_frame(gvx_batch* b, float topo_radius, int mode, float radi
         gvx_grid* g = b->grids[i];
         int l = b->tuning.layers;
         SplatKind k;
-        gvx_status rc = splat_check(g, mode, radius, chan_density, chan_vel, &l, &k);
+        gvx_status rc = splat_check(g, mode, radius, chan_density, chan_vel, 0, batch_dense(b), &l, &k);
         if (rc) return rc;
         if (i == 0) {
             kind = k;
@@ -1876,9 +2063,12 @@ gvx_status gvx_batch_frame(gvx_batch* b, float topo_radius, int mode, float radi
     }
     SplatArgs a0;
     memset(&a0, 0, sizeof(a0));
+    const SlabShape sh0 = slab_shape(b->grids[0], 0, batch_dense(b), kind.has_d && kind.has_v);
     a0.P = b->grids[0]->P;
+    a0.push = sh0.push;
+    a0.tile_rows = sh0.rows;
     a0.slab_layers = layers;
-    a0.slabs = (a0.P + layers - 1) / layers;
+    a0.slabs = (sh0.span + layers - 1) / layers;
     uint64_t units = 0;
     for (gvx_grid* g : b->grids) {
         uint32_t cap = 0;
