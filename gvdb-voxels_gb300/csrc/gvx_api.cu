@@ -225,8 +225,8 @@ gvx_status gvx_destroy(gvx_grid* g)
                       &g->keys[0], &g->keys[1], &g->vals[0], &g->vals[1], &g->spos, &g->svel,
                       &g->sort.hist, &g->sort.base, &g->sort.lookback, &g->sort.counter, &g->d0_bits,
                       &g->d0_prefix, &g->x0_bits, &g->x0_prefix, &g->masks, &g->upper, &g->lists, &g->tmp_scan,
-                      &g->d_counts, &g->d_err, &g->d_bbox, &g->d_rmax, &g->d_next, &g->host_stage, &g->api_keys[0],
-                      &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
+                      &g->d_counts, &g->d_err, &g->d_bbox, &g->d_rmax, &g->d_next, &g->touched, &g->host_stage,
+                      &g->api_keys[0], &g->api_keys[1], &g->api_vals[0], &g->api_vals[1], &g->lk_bits, &g->lk_prefix,
                       &g->inc0, &g->inc_remap, &g->sc_cnt, &g->sc_off, &g->sc_keys[0], &g->sc_keys[1],
                       &g->sc_vals[0], &g->sc_vals[1], &g->sc_pts, &g->sc_beg, &g->sc_end, &g->atlas_tmp,
                       &g->sc_q, &g->sc_qclr, &g->own_stage, &g->apron_tab, &g->apron_mark};

@@ -172,7 +172,8 @@ struct gvx_grid {
     DevBuf inc0, inc_remap;  // incremental build: linked + new level-0 bitmaps, linked rank -> pool index
     DevBuf d_err, d_bbox;
     DevBuf d_rmax;  // float bits of the largest per-point radius of the last point permute
-    DevBuf d_next;  // work-unit counter of the splat launch
+    DevBuf d_next;  // work-unit counter of the splat launch (+ the count of touched slots)
+    DevBuf touched; // slots an accumulating splat visits
     void* h_pin = nullptr;  // pinned staging of the topology's small readbacks
     struct gvx_topo_staged* staged = nullptr;  // a staged RebuildTopology between its stages (batches)
     struct gvx_topo_plan* plan = nullptr;      // fixed key space and capacities of planned builds (batches)

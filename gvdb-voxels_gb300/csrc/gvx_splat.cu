@@ -129,6 +129,10 @@ struct SplatArgs {
     float boundval;
     uint32_t* err;
     uint32_t* next;  // work-unit counter of the single-grid launch
+    // an accumulating single-grid splat may visit only the slots whose bricks some point can
+    // reach (unit_slots[0 .. *unit_count), in no particular order); null: every slot
+    const uint32_t* unit_slots;
+    const uint32_t* unit_count;
 };
 
 // Shared-memory tile of one padded brick.  Density only: float per voxel.
@@ -514,8 +518,9 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     constexpr bool PUSHABLE = HAS_DEN && HAS_VEL;  // the host sets push for these kernels only
     const bool push = PUSHABLE && a.push;
     const int TY = push ? a.tile_rows : P, yoff = push ? ap : 0, zend = push ? P - ap : P;
-    const uint32_t s = u / (uint32_t)S;
-    const int z0 = yoff + (int)(u - s * (uint32_t)S) * L;  // first padded layer of the slab
+    const uint32_t ui = u / (uint32_t)S;  // the unit's brick in the unit order, its slab u - ui * S
+    const uint32_t s = a.unit_slots ? a.unit_slots[ui] : ui;
+    const int z0 = yoff + (int)(u - ui * (uint32_t)S) * L;  // first padded layer of the slab
     const int nl = min(L, zend - z0);
     const int nvox = nl * TY * P;
     const size_t gofs = (size_t)s * P3 + (size_t)z0 * P2;  // slab start in the channel (no push)
@@ -840,7 +845,7 @@ __global__ void __launch_bounds__(kSlabWarps * 32, splat_min_blocks<HAS_DEN, HAS
     }
     __syncthreads();
     uint32_t phase = 0;
-    const uint32_t units = a.nslots * (uint32_t)a.slabs;
+    const uint32_t units = (a.unit_count ? min(*a.unit_count, a.nslots) : a.nslots) * (uint32_t)a.slabs;
     // units one at a time from a counter (zeroed before the launch), the next one claimed while
     // the current one runs (its atomic's latency hidden: the 4M frame's splat 3.10 -> 3.04 ms):
     // bricks differ widely in cost and the costly ones cluster (dense regions, the surface of an
@@ -1311,6 +1316,29 @@ static size_t splat_smem(const SplatArgs& a, const SplatKind& k)
     return (size_t)a.slab_layers * a.tile_rows * a.P * (k.has_v ? 16 : 4) * kSlabWarps;
 }
 
+// The slots whose brick has points of the current grouping in itself or one of its 26 neighbours:
+// the only bricks an accumulating splat changes (the others it leaves as they are, loading and
+// storing nothing).  A warp per slot, lane r < 27 testing neighbour r; compacted by an atomic
+// counter (each unit writes its own brick only, so their order does not matter).
+__global__ void k_touched_slots(const int* __restrict__ slot_leaf, uint32_t nslots, const int* __restrict__ nbr,
+                                const int2* __restrict__ leaf_range, uint32_t* __restrict__ out,
+                                uint32_t* __restrict__ count)
+{
+    const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslots) return;  // whole warps
+    const int leaf = slot_leaf[s];
+    bool has = false;
+    if (lane < 27 && leaf >= 0) {
+        const int nl = nbr[(size_t)leaf * 27 + lane];
+        if (nl >= 0) {
+            const int2 r = leaf_range[nl];
+            has = r.y > r.x;
+        }
+    }
+    if (__ballot_sync(0xFFFFFFFFu, has) && lane == 0) out[atomicAdd(count, 1u)] = s;
+}
+
 gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float trans[3], int chan_d, int chan_v,
                          int accum)
 {
@@ -1328,9 +1356,19 @@ gvx_status gvx_splat_run(gvx_grid* g, int mode, int n, float radius, const float
         const uint64_t ctas_needed = (units + kSlabWarps - 1) / kSlabWarps;
         const uint32_t grid =
             (uint32_t)std::min<uint64_t>(ctas_needed, (uint64_t)sm_count(g->device) * std::max(per_sm, 1));
-        GVX_CK(gvx_ensure(g->d_next, sizeof(uint32_t)));
-        GVX_CK(cudaMemsetAsync(g->d_next.p, 0, sizeof(uint32_t), g->stream));
+        GVX_CK(gvx_ensure(g->d_next, 2 * sizeof(uint32_t)));
+        GVX_CK(cudaMemsetAsync(g->d_next.p, 0, 2 * sizeof(uint32_t), g->stream));
         a.next = g->d_next.as<uint32_t>();
+        if (accum) {
+            // only the bricks that this grouping's points can reach (accumulating frames of a growing
+            // scene touch a small part of it: the fusion frames, about a tenth of 129k bricks)
+            GVX_CK(gvx_ensure(g->touched, (size_t)a.nslots * sizeof(uint32_t)));
+            a.unit_count = g->d_next.as<uint32_t>() + 1;
+            a.unit_slots = g->touched.as<uint32_t>();
+            k_touched_slots<<<blocks_for((uint64_t)a.nslots * 32u, 256), 256, 0, g->stream>>>(
+                a.slot_leaf, a.nslots, a.nbr, a.leaf_range, g->touched.as<uint32_t>(), g->d_next.as<uint32_t>() + 1);
+            g->launches++;
+        }
         void* args[] = {&a};
         GVX_CK(cudaLaunchKernel(kern, dim3(grid), dim3(kSlabWarps * 32), args, smem, g->stream));
         g->launches++;
