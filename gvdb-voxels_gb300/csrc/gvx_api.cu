@@ -299,6 +299,7 @@ gvx_status gvx_configure(gvx_grid* g, int levels, const int* logdim, const int* 
     g->configured = true;
     g->topo_gen++;
     g->root_level = -1;
+    gvx_topo_plan_free(g);  // a plan's depth and key space are in the old levels' terms
     g->vox_res_max_reset = true;  // VG.cpp:2428
     g->bounds_pending = false;
     for (int a = 0; a < 3; a++) g->obj_min[a] = g->obj_max[a] = g->vox_res_max[a] = 0.f;
@@ -778,6 +779,7 @@ gvx_status gvx_get_info(gvx_grid* g, gvx_info* out)
     for (int c = 0; c < GVX_MAXCH; c++) nch += g->ch[c].used;
     out->channels = nch;
     out->last_rebuild = g->last_rebuild;
+    out->planned_builds = g->planned_builds;
     return GVX_OK;
 }
 

@@ -176,7 +176,8 @@ struct gvx_grid {
     DevBuf touched; // slots an accumulating splat visits
     void* h_pin = nullptr;  // pinned staging of the topology's small readbacks
     struct gvx_topo_staged* staged = nullptr;  // a staged RebuildTopology between its stages (batches)
-    struct gvx_topo_plan* plan = nullptr;      // fixed key space and capacities of planned builds (batches)
+    struct gvx_topo_plan* plan = nullptr;      // fixed key space and capacities of planned builds
+    int64_t planned_builds = 0;                // single-grid full builds that ran under the plan
     DevBuf host_stage;  // pinned staging of small readbacks
 
     // subcell lists of InsertPointsSubcell: entries sorted by subcell index
@@ -236,17 +237,17 @@ gvx_status gvx_topo_stage2(gvx_grid* g);
 gvx_status gvx_topo_stage3(gvx_grid* g);
 void gvx_topo_staged_free(gvx_grid* g);
 gvx_status gvx_topo_read_bounds(gvx_grid* g);
-// Planned full builds (batches; see gvx_topology.cu): a plan made from the grid's last staged
-// full build; a planned build queues RebuildTopology (full) + UpdateAtlas with no host wait and
-// no allocation (capturable), with InsertPoints' octant pass writing `attr`; plan_finish, after
+// Planned full builds (see gvx_topology.cu): a plan made from the grid's last full build; a
+// planned build queues RebuildTopology (full) -- with frame, UpdateAtlas and InsertPoints' octant
+// pass writing `attr` too -- with no host wait and no allocation (capturable); plan_finish, after
 // the stream has passed it, checks that the plan held and sets the host state (*held false: the
 // build is void, the grid is to be built again without the plan)
 gvx_status gvx_topo_plan_make(gvx_grid* g);
 bool gvx_topo_plan_ready(const gvx_grid* g);
-gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr);
+gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr, bool frame);
 gvx_status gvx_topo_plan_record_error(gvx_grid* g, cudaStream_t st);
 void gvx_topo_plan_replayed(gvx_grid* g);  // its captured build was launched again
-gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held);
+gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held, bool frame);
 void gvx_topo_plan_free(gvx_grid* g);
 uint64_t gvx_topo_plan_id(const gvx_grid* g);  // changes whenever the plan is made again
 // device count of the atlas slots a planned build assigns (clamped to *cap by the reader)

@@ -1626,7 +1626,7 @@ static gvx_status frame_build(gvx_grid* g, bool want_svel)
     A.spos = g->spos.as<float4>();
     A.svel = want_svel ? g->svel.as<float4>() : nullptr;
     A.rmax = rmax;
-    return gvx_topo_plan_enqueue(g, &A);
+    return gvx_topo_plan_enqueue(g, &A, true);
 }
 
 // every grid's planned build on its own stream, forked from and joined back into the batch
@@ -2192,7 +2192,7 @@ gvx_status gvx_batch_frame(gvx_batch* b, float topo_radius, int mode, float radi
     for (size_t i = 0; i < ng; i++) {
         gvx_grid* g = b->grids[i];
         bool held = false;
-        rc = gvx_topo_plan_finish(g, &held);
+        rc = gvx_topo_plan_finish(g, &held, true);
         if (rc != GVX_OK) {
             if (first == GVX_OK) {
                 const std::string m = gvx_last_error();

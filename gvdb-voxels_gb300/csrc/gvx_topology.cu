@@ -1347,6 +1347,18 @@ struct FullBuild {
     float mn[3], mx[3];  // the points' bounding box (GetBoundingBox before its margins)
 };
 
+// A staged RebuildTopology between its stages (gvx_topo_stage1..3), and the last full build of the
+// grid (staged or not: what a plan is made from)
+struct gvx_topo_staged {
+    int n;
+    float radius;
+    int mode, min_depth;
+    bool pending;
+    FullBuild fb;
+    bool last_full;     // the last full build (fb) finished, and the tree is still that one
+    uint64_t last_gen;  // topo_gen after it
+};
+
 static gvx_status topo_full_launch_ks(gvx_grid* g, int n, float radius, const float o[3], int depth,
                                       const int rootpos[3], const KeySpace& ks, FullBuild& fb, bool queue_readback);
 
@@ -1649,7 +1661,13 @@ static gvx_status topo_full(gvx_grid* g, int n, float radius, const float o[3], 
 {
     FullBuild fb{};
     gvx_status rc = topo_full_launch(g, n, radius, o, depth, rootpos, mn, mx, fb);
-    return rc ? rc : topo_full_complete(g, fb);
+    if (rc == GVX_OK) rc = topo_full_complete(g, fb);
+    // recorded for a plan (gvx_topo_plan_make)
+    if (!g->staged) g->staged = new gvx_topo_staged();
+    g->staged->fb = fb;
+    g->staged->last_full = rc == GVX_OK;
+    g->staged->last_gen = g->topo_gen;
+    return rc;
 }
 
 // slots of d_counts read back by the incremental build
@@ -2153,15 +2171,6 @@ static gvx_status rebuild_after_bbox(gvx_grid* g, int n, float radius, const flo
     return full_status(g, rc);
 }
 
-gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
-{
-    gvx_status rc = rebuild_begin(g, n, radius, orig, mode);
-    if (rc) return rc;
-    uint32_t hb[14];
-    rc = readback_finish(g, hb, sizeof(hb), "GetBoundingBox");
-    if (rc) return rc;
-    return rebuild_after_bbox(g, n, radius, orig, mode, min_depth, hb, nullptr, nullptr);
-}
 
 // Staged RebuildTopology for batches of grids (gvx_batch_topology): stage 1
 // queues GetBoundingBox and its readback; stage 2, once the grid's stream has
@@ -2169,15 +2178,6 @@ gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3
 // other kind of build runs to its end here); stage 3 reads the counts and
 // finishes the full build.  The host waits on a grid only where its stream
 // has had the time of the other grids' stages to get there.
-struct gvx_topo_staged {
-    int n;
-    float radius;
-    int mode, min_depth;
-    bool pending;
-    FullBuild fb;
-    bool last_full;     // the last stage 3 finished a full build (fb), the tree is still that one
-    uint64_t last_gen;  // topo_gen after it
-};
 
 gvx_status gvx_topo_stage1(gvx_grid* g, int n, float radius, int mode, int min_depth)
 {
@@ -2439,7 +2439,7 @@ static gvx_status plan_atlas(gvx_grid* g, const gvx_topo_plan& P)
     return GVX_OK;
 }
 
-gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr)
+gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr, bool frame)
 {
     if (!gvx_topo_plan_ready(g)) {
         gvx_set_error("planned build: no plan for the grid's points");
@@ -2467,9 +2467,9 @@ gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr)
     P.fb.words0 = fb.words0;
     P.fb.ud = fb.ud;
     gvx_status rc = plan_pools(g, P, fb);
-    if (rc == GVX_OK) rc = plan_atlas(g, P);
+    if (rc == GVX_OK && frame) rc = plan_atlas(g, P);
     // ---- InsertPoints: octant order and the sorted attributes over the leaf capacity
-    if (rc == GVX_OK) {
+    if (rc == GVX_OK && frame) {
         g->oct_count = dc_dev(g->d_counts.as<uint32_t>(), 0, 1, cap0);
         g->oct_valid = false;
         rc = gvx_topo_octants(g, attr);
@@ -2482,6 +2482,7 @@ gvx_status gvx_topo_plan_enqueue(gvx_grid* g, const GvxSortedAttr* attr)
     if (rc) return rc;
     GVX_CK(cudaMemcpyAsync(P.rec + kRecCounts, g->d_counts.p, 64 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     GVX_CK(cudaMemcpyAsync(P.rec + kRecBbox, g->d_bbox.p, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (!frame) GVX_CK_STATUS(gvx_topo_plan_record_error(g, st));  // (a frame records it after its splat)
     GVX_CK(cudaGetLastError());
     P.sorted_buf = g->sorted_buf;
     P.enqueued = true;
@@ -2518,7 +2519,7 @@ static void plan_void(gvx_grid* g)
     for (int c = 0; c < GVX_MAXCH; c++) apron_invalidate(g->ch[c]);
 }
 
-gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held)
+gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held, bool frame)
 {
     *held = false;
     if (!g->plan || !g->plan->enqueued) {
@@ -2534,7 +2535,7 @@ gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held)
     g->pools_appended = false;
     g->topo_gen++;
     g->atlas_gen++;
-    gvx_status rc = report_device_error(g, rec[kRecErr], "BatchFrame");  // (clears the word)
+    gvx_status rc = report_device_error(g, rec[kRecErr], frame ? "BatchFrame" : "RebuildTopology");  // (clears it)
     if (rc) {
         plan_void(g);
         return rc;
@@ -2561,7 +2562,7 @@ gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held)
         cnt[l] = (uint64_t)rec[kRecCounts + ci] + rec[kRecCounts + ci + 1];
         ok = cnt[l] <= P.cap[l];
     }
-    ok = ok && rec[kRecCounts + kCntSlots] == cnt[0];  // every leaf of a full build is active
+    ok = ok && (!frame || rec[kRecCounts + kCntSlots] == cnt[0]);  // every leaf of a full build is active
     if (!ok) {
         plan_void(g);
         return GVX_OK;
@@ -2594,17 +2595,68 @@ gvx_status gvx_topo_plan_finish(gvx_grid* g, bool* held)
     g->used_leaves = (int64_t)cnt[0];
     g->rebuild_topo = false;
     g->last_rebuild = 1;
+    g->oct_leaves = (uint32_t)cnt[0];
+    g->perm_valid = false;
+    if (!frame) {  // the topology alone: UpdateAtlas and the octant pass are the caller's next calls
+        g->atlas_valid = false;
+        g->atlas_prefix = -1;
+        g->oct_valid = false;
+        *held = true;
+        return GVX_OK;
+    }
     // ... of UpdateAtlas (gvx_topo_update_atlas: every brick in a new slot) ...
     g->atlas_used = (int64_t)cnt[0];
     g->atlas_valid = true;
     for (int c = 0; c < GVX_MAXCH; c++) apron_invalidate(g->ch[c]);
     g->atlas_prefix = g->atlas_used;
     // ... and of the octant pass of InsertPoints (the attributes: the caller)
-    g->oct_leaves = (uint32_t)cnt[0];
     g->oct_valid = true;
-    g->perm_valid = false;
     *held = true;
     return GVX_OK;
+}
+
+// A full RebuildTopology under the plan of the grid's last full build (same point count and
+// radius, no origin): the whole build queued at once and one host wait at its end, for the
+// counts, the bounding box and the error word, instead of a wait for the bounding box and
+// another for the counts.  *done false: the plan did not hold (or there is none), nothing of
+// the grid's tree is left, and the caller builds without it.
+static gvx_status rebuild_planned(gvx_grid* g, int n, float radius, const float orig[3], int mode, bool* done)
+{
+    *done = false;
+    const bool no_orig = !orig || (orig[0] == 0.f && orig[1] == 0.f && orig[2] == 0.f);
+    if (mode != GVX_TOPO_FULL || !no_orig || !g->configured || !gvx_topo_plan_ready(g) || n != g->plan->fb.n ||
+        radius != g->plan->fb.radius)
+        return GVX_OK;
+    gvx_status rc = gvx_topo_plan_enqueue(g, nullptr, false);
+    if (rc == GVX_OK) GVX_CK(cudaStreamSynchronize(g->stream));
+    bool held = false;
+    if (rc == GVX_OK) rc = gvx_topo_plan_finish(g, &held, false);
+    if (rc) {
+        plan_void(g);
+        return rc;
+    }
+    *done = held;
+    if (held) {
+        g->staged->last_full = false;  // (the plan stays: it is not remade from its own builds)
+        g->planned_builds++;
+    }
+    return GVX_OK;
+}
+
+gvx_status gvx_topo_rebuild(gvx_grid* g, int n, float radius, const float orig[3], int mode, int min_depth)
+{
+    bool done = false;
+    gvx_status rc = rebuild_planned(g, n, radius, orig, mode, &done);
+    if (rc || done) return rc;
+    rc = rebuild_begin(g, n, radius, orig, mode);
+    if (rc) return rc;
+    uint32_t hb[14];
+    rc = readback_finish(g, hb, sizeof(hb), "GetBoundingBox");
+    if (rc) return rc;
+    rc = rebuild_after_bbox(g, n, radius, orig, mode, min_depth, hb, nullptr, nullptr);
+    // a full build plans the next ones (any points of the same count and radius)
+    if (rc == GVX_OK && mode == GVX_TOPO_FULL) (void)gvx_topo_plan_make(g);
+    return rc;
 }
 
 

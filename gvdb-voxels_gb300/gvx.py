@@ -45,7 +45,8 @@ class Info(ctypes.Structure):
                 ("atlas_subdim", ctypes.c_int * 3), ("atlas_res", ctypes.c_int * 3), ("channels", ctypes.c_int),
                 ("last_rebuild", ctypes.c_int), ("root_pos", ctypes.c_int * 3), ("bbox_min", ctypes.c_float * 3),
                 ("bbox_max", ctypes.c_float * 3), ("obj_min", ctypes.c_float * 3), ("obj_max", ctypes.c_float * 3),
-                ("vox_res", ctypes.c_float * 3), ("vox_res_max", ctypes.c_float * 3)]
+                ("vox_res", ctypes.c_float * 3), ("vox_res_max", ctypes.c_float * 3),
+                ("planned_builds", ctypes.c_int64)]
 
 
 _lib = None

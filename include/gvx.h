@@ -84,6 +84,8 @@ typedef struct gvx_info {
     float obj_max[3];      /*   mObjMin/mObjMax (= mVoxMin/mVoxMax), seeded by pool node 0 */
     float vox_res[3];      /* mVoxRes = obj_max - obj_min */
     float vox_res_max[3];  /* mVoxResMax: largest mVoxRes since Configure */
+    int64_t planned_builds;/* full RebuildTopology calls that ran under the plan of the previous
+                              full build (one host wait), since the grid was created */
 } gvx_info;
 
 const char* gvx_last_error(void);
