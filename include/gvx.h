@@ -134,7 +134,12 @@ gvx_status gvx_commit_points_host(gvx_grid* g, int n, const void* pos, int pos_s
                                   const float* radius);
 
 /* RebuildTopology (VG.h:429, VG.cpp:1181-1218) with mode GVX_TOPO_AUTO/FULL,
- * AccumulateTopology (VG.h:431) with GVX_TOPO_ACCUMULATE (min_depth = iDepth). */
+ * AccumulateTopology (VG.h:431) with GVX_TOPO_ACCUMULATE (min_depth = iDepth).
+ * A GVX_TOPO_FULL build with the point count and radius of the grid's previous full
+ * build (and no origin) runs under that build's plan: queued whole, one host wait
+ * instead of two, the same result (checked; rebuilt without the plan when the points
+ * left its key space or root or outgrew its pools' capacities, 25% over the counts
+ * it was made from).  gvx_info.planned_builds counts these. */
 gvx_status gvx_rebuild_topology(gvx_grid* g, int n, float radius, const float orig[3], int mode,
                                 int min_depth);
 /* RequestFullRebuild (VG.h:432) */
