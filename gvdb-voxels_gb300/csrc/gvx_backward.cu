@@ -219,7 +219,7 @@ extern "C" gvx_status gvx_splat_backward_ex(gvx_grid* g, int mode, int n, float 
     GVX_CK(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));
     // the grouping of the forward: reused when valid, else re-keyed and re-sorted.
     // GVX_BWD_RECOMPUTE drops it first, so the permutation is recomputed from the
-    // positions (keys, radix sort, octant partition with the sorted attributes)
+    // positions (keys with their octants, radix sort, the sorted attributes)
     // rather than taken from the forward; the sort is deterministic, so the new
     // grouping equals the forward's and the gradients are the same bit for bit.
     if (flags & GVX_BWD_RECOMPUTE) {

@@ -215,7 +215,7 @@ void gvx_host_tree_free(gvx_grid* g);
 gvx_status gvx_topo_import(gvx_grid* g, int root_level, const int64_t* counts, const GvxNode* const* nodes,
                            const uint64_t* const* clists);
 gvx_status gvx_topo_group_points(gvx_grid* g, int n, const float trans[3]);
-// sorted point attributes written together with the octant partition (spos null: none)
+// sorted point attributes written by the octant pass of InsertPoints (spos null: none)
 struct GvxSortedAttr {
     const char* vel;
     int vel_off, vel_stride;

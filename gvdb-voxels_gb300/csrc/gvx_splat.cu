@@ -534,7 +534,7 @@ __device__ __forceinline__ void splat_unit(const SplatArgs& a, const uint32_t u,
     // (dx, dy, dz), and inside a brick by octant 4 hx + 2 hy + hz.  Lane r < 27 takes the
     // neighbour (dx, dy, dz) = (r / 9, r / 3 % 3, r % 3) - 1.  Along each axis a half of a brick
     // (floor coordinates [c, c + b/2)) is read when its points, whose footprints reach `reach`
-    // voxels from their own, can touch the slab's padded extent.  A lane's octants are merged
+    // voxels from their own, can touch the tile's extent.  A lane's octants are merged
     // into runs of adjacent octants: at most 4 ranges a lane.
     // with per-point radii the reach is that of the largest radius (ceil R voxels, at most brick - 1)
     const int reach = PPR && a.rmax ? min(a.reach, (int)ceilf(__uint_as_float(*a.rmax))) : a.reach;
@@ -1060,7 +1060,8 @@ gvx_status gvx_prepare_points(gvx_grid* g, int n, const float trans[3], bool nee
         g->perm_r = g->pts.radius;
     };
     if (!g->oct_valid) {
-        // a new grouping: octant order and the sorted attributes in one pass over the points
+        // a new grouping: the octant pass (the sorted attributes; the octant order itself where the
+        // sort keys could not carry it)
         unsigned int* rmax = nullptr;
         rc = attr_buffers(&rmax);
         if (rc) return rc;
